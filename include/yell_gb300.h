@@ -1,0 +1,165 @@
+/*
+ * yell_gb300 — C ABI of the GB300 (sm_103a) implementation of YELL's RNS
+ * polynomial hot path: negacyclic forward / inverse NTT over 62-bit primes,
+ * pointwise Barrett mulmod, muladd, add/sub, negate and a fused polymul.
+ *
+ * Every entry point returns an int status (0 = YELL_OK) and never aborts;
+ * yell_last_error() gives a thread-local message for the last failure.
+ * Plain pointers and sizes only.  Residues are uint64 words; "limb" cm of a
+ * polynomial is reduced modulo prime yell_prime(cm) exactly as in the
+ * reference, where limb cm of yell::poly<N> uses params::P[cm]
+ * (include/yell/details/poly.hpp:170-186).
+ *
+ * Results are word-for-word those of the reference (fionser/YELL) on the
+ * same inputs: forward outputs in bit-reversed order, reduced to [0, p)
+ * (forward) or left in [0, 4p) (forward_lazy, the same lazy words as the
+ * reference); backward outputs in natural order in [0, p).
+ *
+ * Degrees: N = 2^log_n with log_n in [3, 17] (yell_min_log_degree() ..
+ * yell_max_log_degree()).  The reference's inverse at N = 4 applies its last
+ * layer twice (lib/ntt.cpp:174-187 followed by
+ * include/yell/details/ntt.hpp:220-228) and is not an inverse, so 4 is
+ * rejected with YELL_ERR_UNSUPPORTED_DEGREE.
+ *
+ * Three families of calls:
+ *   1. Drop-ins for the reference's host-memory calls (yell_ntt_*,
+ *      yell_poly_*): host pointers, copied to the GPU and back inside the
+ *      call.  Synchronous.
+ *   2. Device-resident calls (yell_dev_*): device pointers owned by the
+ *      caller, work queued on the given CUDA stream (NULL = the library's
+ *      stream of the current device), asynchronous.
+ *   3. Handles (yell_dev_poly_*), a batch queue (yell_batch_*) and a serving
+ *      loop (yell_server_*) built on 2.
+ */
+#ifndef YELL_GB300_H_
+#define YELL_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define YELL_GB300_ABI_VERSION 1
+
+enum yell_status_code {
+  YELL_OK = 0,
+  YELL_ERR_INVALID_ARGUMENT = 1,   /* null pointer, zero count, bad enum */
+  YELL_ERR_UNSUPPORTED_DEGREE = 2, /* log_n outside [3, 17] */
+  YELL_ERR_INVALID_MODULUS = 3,    /* cm >= yell_max_moduli() */
+  YELL_ERR_CUDA = 4,               /* a CUDA call failed; see yell_last_error() */
+  YELL_ERR_OUT_OF_MEMORY = 5,      /* device or pinned allocation refused */
+  YELL_ERR_BUDGET = 6,             /* request exceeds the server's HBM budget */
+  YELL_ERR_TIMEOUT = 7,            /* a bounded wait gave up */
+  YELL_ERR_CANCELLED = 8,          /* request cancelled before it ran */
+  YELL_ERR_NOT_FOUND = 9,          /* unknown request id */
+  YELL_ERR_NO_DEVICE = 10          /* no CUDA device visible */
+};
+
+enum yell_direction { YELL_FORWARD = 0, YELL_FORWARD_LAZY = 1, YELL_BACKWARD = 2 };
+
+enum yell_elementwise_op {
+  YELL_OP_MULMOD = 0, /* dst = mulmod(a, b)            include/yell/ops.hpp:103-112 */
+  YELL_OP_ADDMOD = 1, /* dst = addmod(a, b)            include/yell/ops.hpp:54-68   */
+  YELL_OP_SUBMOD = 2, /* dst = submod(a, b)            include/yell/ops.hpp:70-83   */
+  YELL_OP_MULADD = 3, /* dst = barrett(a*b + dst)      include/yell/ops.hpp:144-158 */
+  YELL_OP_NEGATE = 4  /* dst = p - a (b unused)        include/yell/details/poly.hpp:151-157 */
+};
+
+/* ---- library --------------------------------------------------------- */
+int yell_abi_version(void);
+const char* yell_status_string(int status);
+const char* yell_last_error(void);
+/* Number of kernels this library launched so far in this process. */
+uint64_t yell_kernel_launches(void);
+
+/* ---- params: replaces yell::params (include/yell/params_64.hpp:19-38) --- */
+uint32_t yell_max_moduli(void);       /* kMaxNbModuli = 1000 (params_64.hpp:19) */
+uint32_t yell_min_log_degree(void);
+uint32_t yell_max_log_degree(void);
+uint64_t yell_prime(uint32_t cm);          /* params::P[cm], 0 if out of range (:27) */
+uint64_t yell_prime_pn(uint32_t cm);       /* params::Pn[cm] (:31)                   */
+uint64_t yell_primitive_root(uint32_t cm); /* params::primitive_roots[cm] (:34)      */
+
+/* ---- twiddle tables: replaces ntt<N>::init_table / init_ntt_tables -----
+ * (include/yell/ntt.hpp:50-56, include/yell/details/ntt.hpp:97-173).  Tables
+ * live on the current device for the life of the process, like the
+ * reference's per-N singleton.  Other calls build them on first use; calling
+ * these first keeps table construction out of later timed or captured work. */
+int yell_init_table(uint32_t log_n, uint32_t cm);
+int yell_init_ntt_tables(uint32_t log_n, uint32_t K); /* cm = 0 .. K-1 */
+int yell_init_ntt_tables_range(uint32_t log_n, uint32_t cm0, uint32_t L); /* cm0 .. cm0+L-1 */
+/* Host copy of one table: out4n = phiTbl, shoupPhiTbl, invphiTbl,
+ * shoupInvphiTbl (N words each, bit-reversed); scalars4 = invDegree,
+ * shoupInvDegree, invphiInvDegree, shoupInvphiInvDegree (ntt.hpp:35-43). */
+int yell_ntt_tables(uint32_t log_n, uint32_t cm, uint64_t* out4n, uint64_t* scalars4);
+
+/* ---- drop-in, one limb in host memory, in place -------------------------
+ * Replace yell::ntt<N>::forward / forward_lazy / backward(T* op, size_t cm)
+ * (include/yell/ntt.hpp:59-65; details/ntt.hpp:175-235). */
+int yell_ntt_forward(uint64_t* op, uint32_t log_n, uint32_t cm);
+int yell_ntt_forward_lazy(uint64_t* op, uint32_t log_n, uint32_t cm);
+int yell_ntt_backward(uint64_t* op, uint32_t log_n, uint32_t cm);
+
+/* ---- drop-in, one poly in host memory -----------------------------------
+ * limbs = poly<N>::raw_data(): L separate arrays of N words, limb cm using
+ * prime cm.  Replace poly<N>::forward / forward_lazy / backward
+ * (include/yell/details/poly.hpp:170-186). */
+int yell_poly_forward(uint64_t* const* limbs, uint32_t L, uint32_t log_n);
+int yell_poly_forward_lazy(uint64_t* const* limbs, uint32_t L, uint32_t log_n);
+int yell_poly_backward(uint64_t* const* limbs, uint32_t L, uint32_t log_n);
+/* Replace the YELL_BINARY_OPERATOR / YELL_SELF_BINARY_OPERATOR loops
+ * (include/yell/ops.hpp:7-41) behind poly<N>::operator* + - *= += -=
+ * (include/yell/poly.hpp:163-168).  dst may alias a or b. */
+int yell_poly_mulmod(uint64_t* const* dst, const uint64_t* const* a, const uint64_t* const* b,
+                     uint32_t L, uint32_t log_n);
+int yell_poly_addmod(uint64_t* const* dst, const uint64_t* const* a, const uint64_t* const* b,
+                     uint32_t L, uint32_t log_n);
+int yell_poly_submod(uint64_t* const* dst, const uint64_t* const* a, const uint64_t* const* b,
+                     uint32_t L, uint32_t log_n);
+/* Replaces poly<N>::add_product_of: acc += a*b via ops::muladd
+ * (include/yell/details/poly.hpp:118-132). */
+int yell_poly_add_product_of(uint64_t* const* acc, const uint64_t* const* a,
+                             const uint64_t* const* b, uint32_t L, uint32_t log_n);
+/* Replaces poly<N>::negate (include/yell/details/poly.hpp:151-157). */
+int yell_poly_negate(uint64_t* const* limbs, uint32_t L, uint32_t log_n);
+
+/* ---- fused polymul on host memory ---------------------------------------
+ * c = a * b mod (X^N + 1) for `pairs` independent pairs laid out
+ * (pairs, L, N) contiguous, limb l using prime cm0 + l: the reference's
+ * a.forward(); b.forward(); c = a * b; c.backward(); per pair, fused on the
+ * GPU, with host<->device copies pipelined against the compute.  a and b are
+ * not modified.  Pinned host memory (yell_host_alloc) copies fastest. */
+int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_t pairs,
+                      uint32_t L, uint32_t log_n, uint32_t cm0);
+void* yell_host_alloc(size_t bytes); /* pinned; NULL on failure */
+void yell_host_free(void* p);
+
+/* ---- device-resident calls (device pointers, asynchronous on `stream`) --
+ * A batch is `count` polys of L limbs laid out (count, L, N) contiguous;
+ * limb l of every poly uses prime cm0 + l. */
+int yell_dev_ntt(uint64_t* d_polys, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
+                 int direction, void* stream);
+/* Limbs anywhere: d_limbs and d_cms are DEVICE arrays of `count` limb
+ * pointers and modulus indices. */
+int yell_dev_ntt_limbs(uint64_t* const* d_limbs, const uint32_t* d_cms, uint32_t count,
+                       uint32_t log_n, int direction, void* stream);
+int yell_dev_elementwise(int op, uint64_t* d_dst, const uint64_t* d_a, const uint64_t* d_b,
+                         uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0, void* stream);
+/* Fused polymul of `pairs` pairs; d_c may not alias d_a or d_b.  Degrees
+ * above the whole-limb path need scratch of yell_polymul_scratch_words()
+ * words; pass NULL to use the library's per-device scratch (grown on demand,
+ * serialised by a lock per device). */
+size_t yell_polymul_scratch_words(uint32_t pairs, uint32_t L, uint32_t log_n);
+int yell_dev_polymul(uint64_t* d_c, const uint64_t* d_a, const uint64_t* d_b, uint32_t pairs,
+                     uint32_t L, uint32_t log_n, uint32_t cm0, uint64_t* d_scratch,
+                     size_t scratch_words, void* stream);
+/* Waits for all work the library queued on its own stream of this device. */
+int yell_synchronize(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* YELL_GB300_H_ */

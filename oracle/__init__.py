@@ -1,0 +1,242 @@
+"""CPU oracle for the YELL RNS-polynomial hot path (test infrastructure only).
+
+Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this package, and only as the checker.  The product
+(``yell_gb300``) never imports it and has no CPU fallback.
+
+Two CPU implementations are exposed through ctypes:
+
+* ``port``: ``liboracle.so``, the plain-C restatement in ``yell_oracle.c`` of
+  the reference algorithm (fionser/YELL ``lib/ntt.cpp``, ``lib/ops.cpp``,
+  ``include/yell/details/ntt.hpp``), built by ``oracle/Makefile``.
+* ``ref``: ``_ref/libyellref.so``, the reference's own sources compiled
+  unmodified with ``ref_harness.cpp``; present only where the reference
+  checkout was available to build it (``ref_available()``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_U64P = ctypes.POINTER(ctypes.c_uint64)
+_port = None
+_ref = None
+
+
+def build(ref_dir: str | None = None) -> None:
+    """Compile liboracle.so (and _ref/libyellref.so when the reference exists)."""
+    cmd = ["make", "-s", "-C", _HERE, "oracle"]
+    subprocess.run(cmd, check=True)
+    ref = ref_dir or os.environ.get("YELL_REFERENCE_DIR", "/root/reference")
+    if os.path.isdir(os.path.join(ref, "lib")):
+        subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={ref}"], check=True)
+
+
+def _bind(lib, prefix: str):
+    u32, u64, sz = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_size_t
+    sig = {
+        "prime": (u64, [u32]),
+        "pn": (u64, [u32]),
+        "primitive_root": (u64, [u32]),
+        "forward": (ctypes.c_int, [_U64P, u32, u32]),
+        "forward_lazy": (ctypes.c_int, [_U64P, u32, u32]),
+        "backward": (ctypes.c_int, [_U64P, u32, u32]),
+        "ntt_tables": (ctypes.c_int, [u32, u32, _U64P, _U64P]),
+        "barrett": (u64, [u64, u64, u32]),
+        "shoupify": (u64, [u64, u32]),
+        "mulmod_n": (None, [_U64P, _U64P, _U64P, sz, u32]),
+        "addmod_n": (None, [_U64P, _U64P, _U64P, sz, u32]),
+        "submod_n": (None, [_U64P, _U64P, _U64P, sz, u32]),
+        "muladd_n": (None, [_U64P, _U64P, _U64P, sz, u32]),
+        "mulmod_shoup_n": (None, [_U64P, _U64P, u64, sz, u32]),
+    }
+    if prefix == "orc_":
+        sig.update({
+            "negate_n": (None, [_U64P, sz, u32]),
+            "negacyclic_schoolbook": (ctypes.c_int, [_U64P, _U64P, _U64P, u32, u32]),
+            "polymul": (ctypes.c_int, [_U64P, _U64P, _U64P, u32, u32, u32]),
+            "polymul_batch": (ctypes.c_double, [_U64P, _U64P, _U64P, u32, u32, u32, u32, u32]),
+        })
+    else:
+        sig["polymul_batch"] = (ctypes.c_double, [_U64P, _U64P, _U64P, u32, u32, u32, u32])
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, prefix + name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+def _load_port():
+    global _port
+    if _port is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        _port = _bind(ctypes.CDLL(path), "orc_")
+    return _port
+
+
+def ref_available() -> bool:
+    return os.path.exists(os.path.join(_HERE, "_ref", "libyellref.so"))
+
+
+def _load_ref():
+    global _ref
+    if _ref is None:
+        _ref = _bind(ctypes.CDLL(os.path.join(_HERE, "_ref", "libyellref.so")), "ref_")
+    return _ref
+
+
+def _ptr(a: np.ndarray):
+    assert a.dtype == np.uint64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_U64P)
+
+
+class Oracle:
+    """numpy-facing wrapper; ``which`` is "port" (the C restatement) or "ref"."""
+
+    def __init__(self, which: str = "port"):
+        self.which = which
+        self.lib = _load_port() if which == "port" else _load_ref()
+        self.pre = "orc_" if which == "port" else "ref_"
+
+    def _f(self, name):
+        return getattr(self.lib, self.pre + name)
+
+    # --- params ---------------------------------------------------------
+    def prime(self, cm: int) -> int:
+        return int(self._f("prime")(cm))
+
+    def pn(self, cm: int) -> int:
+        return int(self._f("pn")(cm))
+
+    def primitive_root(self, cm: int) -> int:
+        return int(self._f("primitive_root")(cm))
+
+    def primes(self, L: int, cm0: int = 0) -> np.ndarray:
+        return np.array([self.prime(cm0 + i) for i in range(L)], dtype=np.uint64)
+
+    # --- NTT on one limb (in place on a copy) ----------------------------
+    def _ntt(self, name, x, log_n, cm):
+        y = np.ascontiguousarray(x, dtype=np.uint64).copy()
+        assert y.size == 1 << log_n
+        rc = self._f(name)(_ptr(y), log_n, cm)
+        if rc != 0:
+            raise ValueError(f"oracle {name}: bad arguments log_n={log_n} cm={cm}")
+        return y
+
+    def forward(self, x, log_n, cm):
+        return self._ntt("forward", x, log_n, cm)
+
+    def forward_lazy(self, x, log_n, cm):
+        return self._ntt("forward_lazy", x, log_n, cm)
+
+    def backward(self, x, log_n, cm):
+        return self._ntt("backward", x, log_n, cm)
+
+    def tables(self, log_n, cm):
+        n = 1 << log_n
+        out = np.zeros(4 * n, dtype=np.uint64)
+        sc = np.zeros(4, dtype=np.uint64)
+        rc = self._f("ntt_tables")(log_n, cm, _ptr(out), _ptr(sc))
+        if rc != 0:
+            raise ValueError("oracle tables: bad arguments")
+        return out.reshape(4, n), sc
+
+    # --- whole-poly helpers: x has shape (L, N), limb l uses prime cm0+l --
+    def poly_forward(self, x, log_n, cm0=0, lazy=False):
+        x = np.asarray(x, dtype=np.uint64).reshape(-1, 1 << log_n)
+        f = self.forward_lazy if lazy else self.forward
+        return np.stack([f(x[i], log_n, cm0 + i) for i in range(x.shape[0])])
+
+    def poly_backward(self, x, log_n, cm0=0):
+        x = np.asarray(x, dtype=np.uint64).reshape(-1, 1 << log_n)
+        return np.stack([self.backward(x[i], log_n, cm0 + i) for i in range(x.shape[0])])
+
+    # --- element-wise ops on one limb -------------------------------------
+    def _ew(self, name, a, b, cm):
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        d = np.zeros_like(a)
+        self._f(name)(_ptr(d), _ptr(a), _ptr(b), a.size, cm)
+        return d
+
+    def mulmod(self, a, b, cm):
+        return self._ew("mulmod_n", a, b, cm)
+
+    def addmod(self, a, b, cm):
+        return self._ew("addmod_n", a, b, cm)
+
+    def submod(self, a, b, cm):
+        return self._ew("submod_n", a, b, cm)
+
+    def muladd(self, rop, a, b, cm):
+        r = np.ascontiguousarray(rop, dtype=np.uint64).copy()
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        self._f("muladd_n")(_ptr(r), _ptr(a), _ptr(b), a.size, cm)
+        return r
+
+    def mulmod_shoup(self, a, y, cm):
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        d = np.zeros_like(a)
+        self._f("mulmod_shoup_n")(_ptr(d), _ptr(a), int(y), a.size, cm)
+        return d
+
+    def negate(self, a, cm):
+        assert self.which == "port"
+        r = np.ascontiguousarray(a, dtype=np.uint64).copy()
+        self.lib.orc_negate_n(_ptr(r), r.size, cm)
+        return r
+
+    def barrett(self, x: int, cm: int) -> int:
+        return int(self._f("barrett")((x >> 64) & (2**64 - 1), x & (2**64 - 1), cm))
+
+    def shoupify(self, x: int, cm: int) -> int:
+        return int(self._f("shoupify")(x, cm))
+
+    # --- polymul ------------------------------------------------------------
+    def schoolbook(self, a, b, log_n, cm):
+        assert self.which == "port"
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        c = np.zeros_like(a)
+        if self.lib.orc_negacyclic_schoolbook(_ptr(c), _ptr(a), _ptr(b), log_n, cm) != 0:
+            raise ValueError("schoolbook: log_n must be <= 13")
+        return c
+
+    def polymul(self, a, b, log_n, cm0=0):
+        """Reference-style polymul on (L, N) polys: forward, mulmod, backward."""
+        n = 1 << log_n
+        a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, n)
+        b = np.ascontiguousarray(b, dtype=np.uint64).reshape(-1, n)
+        if self.which == "port":
+            c = np.zeros_like(a)
+            rc = self.lib.orc_polymul(_ptr(c), _ptr(a), _ptr(b), a.shape[0], log_n, cm0)
+            if rc != 0:
+                raise ValueError("polymul: bad arguments")
+            return c
+        out = []
+        for i in range(a.shape[0]):
+            fa = self.forward(a[i], log_n, cm0 + i)
+            fb = self.forward(b[i], log_n, cm0 + i)
+            out.append(self.backward(self.mulmod(fa, fb, cm0 + i), log_n, cm0 + i))
+        return np.stack(out)
+
+    def polymul_batch(self, a, b, pairs, L, log_n, threads):
+        """Batch of `pairs` polymuls laid out (pairs, L, N); returns (c, seconds)."""
+        n = 1 << log_n
+        a = np.ascontiguousarray(a, dtype=np.uint64).reshape(pairs, L, n)
+        b = np.ascontiguousarray(b, dtype=np.uint64).reshape(pairs, L, n)
+        c = np.zeros_like(a)
+        if self.which == "port":
+            t = self.lib.orc_polymul_batch(_ptr(c), _ptr(a), _ptr(b), pairs, L, log_n, 0, threads)
+        else:
+            t = self.lib.ref_polymul_batch(_ptr(c), _ptr(a), _ptr(b), pairs, L, log_n, threads)
+        if t < 0:
+            raise ValueError("polymul_batch: bad arguments")
+        return c, float(t)

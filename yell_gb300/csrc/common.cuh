@@ -1,0 +1,156 @@
+// Shared device arithmetic and descriptors for the YELL GB300 kernels.
+//
+// Residues are uint64 words modulo 62-bit primes p (p < 2^62), exactly as in
+// the reference (include/yell/params_64.hpp:19-24).  Every formula below is
+// the reference's own, evaluated with the same wrap-around uint64 semantics,
+// so a kernel that applies the same sequence of butterflies produces the same
+// words as the reference, not just the same residues.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace yell_gb300 {
+
+// Per-(log_n, cm) constants resident on the device.  fwd/inv point at N
+// {w, w'} pairs in the reference's bit-reversed order
+// (include/yell/details/ntt.hpp:114-140): fwd = phiTbl/shoupPhiTbl,
+// inv = invphiTbl/shoupInvphiTbl.
+struct alignas(16) DevMod {
+  const ulonglong2* fwd;
+  const ulonglong2* inv;
+  uint64_t p;
+  uint64_t pn;               // low word of floor(2^128/p) (params_64.hpp:29-31)
+  uint64_t inv_n, inv_n_s;   // N^-1 and its Shoup form (ntt.hpp:142-144)
+  uint64_t inv_n_iphi, inv_n_iphi_s;  // N^-1 * invphiTbl[1] and Shoup form (ntt.hpp:143-145)
+};
+
+// Which limbs a launch touches.  Limb k of the launch lives at
+// ptrs ? ptrs[k] : base + k * N, and uses modulus index
+// cms ? cms[k] : cm0 + k % L.
+struct LimbSet {
+  uint64_t* base;
+  uint64_t* const* ptrs;
+  const uint32_t* cms;
+  uint32_t count;
+  uint32_t L;
+  uint32_t cm0;
+  uint32_t pad_;
+
+  __device__ __forceinline__ uint64_t* limb(uint32_t k, uint32_t log_n) const {
+    return ptrs ? ptrs[k] : base + ((size_t)k << log_n);
+  }
+  __device__ __forceinline__ uint32_t cm(uint32_t k) const {
+    return cms ? cms[k] : cm0 + k % L;
+  }
+};
+
+struct ConstLimbSet {
+  const uint64_t* base;
+  const uint64_t* const* ptrs;
+  const uint32_t* cms;
+  uint32_t count;
+  uint32_t L;
+  uint32_t cm0;
+  uint32_t pad_;
+
+  __device__ __forceinline__ const uint64_t* limb(uint32_t k, uint32_t log_n) const {
+    return ptrs ? ptrs[k] : base + ((size_t)k << log_n);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Modular arithmetic.  64-bit products are formed from 32-bit IMAD/IMAD.HI by
+// the compiler; there is no 64-bit multiplier on the SM.
+// ---------------------------------------------------------------------------
+
+// Shoup product with the precomputed companion w' = floor(w * 2^64 / p):
+// x*w - hi64(x*w')*p (mod 2^64).  For x < 2^64 the value lies in [0, 2p).
+// lib/ntt.cpp:59-62 (GS) and :79-80 (CT).
+__device__ __forceinline__ uint64_t shoup_lazy(uint64_t x, uint64_t w, uint64_t wp, uint64_t p) {
+  const uint64_t q = __umul64hi(x, wp);
+  return x * w - q * p;
+}
+
+// Cooley-Tukey butterfly, lib/ntt.cpp:69-83.  In/out [0, 4p).
+__device__ __forceinline__ void ct_bfly(uint64_t& x0, uint64_t& x1, uint64_t w, uint64_t wp,
+                                        uint64_t p, uint64_t p2) {
+  uint64_t u0 = x0;
+  u0 = (u0 >= p2) ? u0 - p2 : u0;
+  const uint64_t t = shoup_lazy(x1, w, wp, p);
+  x0 = u0 + t;
+  x1 = u0 - t + p2;
+}
+
+// Gentleman-Sande butterfly, lib/ntt.cpp:47-63.  In/out [0, 2p).
+__device__ __forceinline__ void gs_bfly(uint64_t& x0, uint64_t& x1, uint64_t w, uint64_t wp,
+                                        uint64_t p, uint64_t p2) {
+  const uint64_t u0 = x0, u1 = x1;
+  uint64_t t0 = u0 + u1;
+  t0 = (t0 >= p2) ? t0 - p2 : t0;
+  const uint64_t t1 = u0 - u1 + p2;
+  x0 = t0;
+  x1 = shoup_lazy(t1, w, wp, p);
+}
+
+// ops::mulmod_shoup, include/yell/ops.hpp:122-132: Shoup product plus one
+// conditional subtraction of p.
+__device__ __forceinline__ uint64_t mulmod_shoup(uint64_t x, uint64_t y, uint64_t yp, uint64_t p) {
+  uint64_t r = shoup_lazy(x, y, yp, p);
+  return (r >= p) ? r - p : r;
+}
+
+// Last inverse layer with the N^-1 scaling fused in,
+// include/yell/details/ntt.hpp:220-228.
+__device__ __forceinline__ void gs_last(uint64_t& x0, uint64_t& x1, const DevMod& m) {
+  const uint64_t u = x0, v = x1;
+  x0 = mulmod_shoup(u + v, m.inv_n, m.inv_n_s, m.p);
+  x1 = mulmod_shoup(u - v + (m.p << 1), m.inv_n_iphi, m.inv_n_iphi_s, m.p);
+}
+
+// Final correction of ntt<N>::forward, include/yell/details/ntt.hpp:179-187:
+// v -= 2p if v >= 2p; v -= p if v >= p.
+__device__ __forceinline__ uint64_t fwd_correct(uint64_t v, uint64_t p, uint64_t p2) {
+  v = (v >= p2) ? v - p2 : v;
+  return (v >= p) ? v - p : v;
+}
+
+// Barrett reduction of the 128-bit value (xh:xl), lib/ops.cpp:5-21:
+// q = Pn*xh + (x << 2) (mod 2^128); r = xl - hi64(q)*p (mod 2^64);
+// one conditional subtraction.
+__device__ __forceinline__ uint64_t barrett128(uint64_t xh, uint64_t xl, uint64_t p, uint64_t pn) {
+  const uint64_t pl = pn * xh;
+  const uint64_t ph = __umul64hi(pn, xh);
+  const uint64_t sl = xl << 2;
+  const uint64_t sh = (xh << 2) | (xl >> 62);
+  const uint64_t lo = pl + sl;
+  const uint64_t qh = ph + sh + (lo < pl ? 1ull : 0ull);
+  const uint64_t r = xl - qh * p;
+  return (r >= p) ? r - p : r;
+}
+
+// ops::mulmod, include/yell/ops.hpp:103-112.
+__device__ __forceinline__ uint64_t mulmod_barrett(uint64_t x, uint64_t y, uint64_t p, uint64_t pn) {
+  return barrett128(__umul64hi(x, y), x * y, p, pn);
+}
+
+// ops::muladd, include/yell/ops.hpp:144-158: barrett(x*y + rop).
+__device__ __forceinline__ uint64_t muladd_barrett(uint64_t rop, uint64_t x, uint64_t y, uint64_t p,
+                                                   uint64_t pn) {
+  const uint64_t lo = x * y;
+  const uint64_t s = lo + rop;
+  const uint64_t hi = __umul64hi(x, y) + (s < lo ? 1ull : 0ull);
+  return barrett128(hi, s, p, pn);
+}
+
+// ops::addmod / ops::submod, include/yell/ops.hpp:54-83 (mod_correct :46-52).
+__device__ __forceinline__ uint64_t addmod(uint64_t x, uint64_t y, uint64_t p) {
+  x += y;
+  return (x >= p) ? x - p : x;
+}
+
+__device__ __forceinline__ uint64_t submod(uint64_t x, uint64_t y, uint64_t p) {
+  x += (p - y);
+  return (x >= p) ? x - p : x;
+}
+
+}  // namespace yell_gb300

@@ -1,0 +1,56 @@
+// Host-side launch interface of the NTT / pointwise kernels (internal).
+#pragma once
+#include <atomic>
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+namespace yell_gb300 {
+
+enum class NttDir : int { kForward = 0, kForwardLazy = 1, kBackward = 2 };
+enum class EwOp : int { kMulmod = 0, kAddmod = 1, kSubmod = 2, kMuladd = 3, kNegate = 4 };
+
+// Launch geometry chosen per degree (the autotuner may override it).
+struct NttShape {
+  uint32_t single_cta_max_log_n = 13;  // whole-limb-in-one-CTA up to this degree
+  uint32_t k1 = 0;                     // column-pass stages for the two-pass path (0 = default)
+};
+
+constexpr uint32_t kMinLogN = 3;
+constexpr uint32_t kMaxLogN = 17;
+
+uint32_t default_k1(uint32_t log_n);
+
+// Kernel launches made by this library (for the caller's accounting).
+extern std::atomic<uint64_t> g_kernel_launches;
+
+// In-place NTT over every limb of `ls`.  mods: the DevMod array of this
+// degree, indexed by modulus index.
+cudaError_t launch_ntt(const LimbSet& ls, uint32_t log_n, const DevMod* mods, NttDir dir,
+                       const NttShape& shape, cudaStream_t st);
+
+// c = INTT(NTT(a) * NTT(b)) per limb.  scratch: one operand's worth of words
+// (count << log_n) when log_n takes the two-pass path, else unused.
+cudaError_t launch_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
+                           uint32_t log_n, const DevMod* mods, uint64_t* scratch,
+                           const NttShape& shape, cudaStream_t st);
+
+// Element-wise op over `count` limbs of N words:
+//   mulmod/addmod/submod: dst = op(a, b);  muladd: dst = barrett(a*b + dst);
+//   negate: dst = p - a.
+cudaError_t launch_elementwise(EwOp op, const LimbSet& dst, const ConstLimbSet& a,
+                               const ConstLimbSet& b, uint32_t log_n, const DevMod* mods,
+                               cudaStream_t st);
+
+size_t polymul_scratch_words(uint32_t count, uint32_t log_n, const NttShape& shape);
+
+// Sets the dynamic shared-memory limits of every kernel on the current
+// device (called once per device, outside any stream capture).
+cudaError_t init_kernel_attributes();
+
+// Kernels launched by one call of launch_ntt / launch_polymul / elementwise.
+uint32_t ntt_launch_count(uint32_t log_n, const NttShape& shape);
+uint32_t polymul_launch_count(uint32_t log_n, const NttShape& shape);
+
+}  // namespace yell_gb300

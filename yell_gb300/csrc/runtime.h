@@ -1,0 +1,103 @@
+// Host runtime: prime table, twiddle-table registry, per-device context,
+// error reporting.
+#pragma once
+#include <atomic>
+#include <cstddef>
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+#include "common.cuh"
+#include "kernels.h"
+
+namespace yell_gb300 {
+
+constexpr uint32_t kMaxModuli = 1000;       // params_64.hpp:19 kMaxNbModuli
+constexpr uint32_t kLogMaxDegree = 20;      // params_64.hpp:21 kMaxPolyDegree = 2^20
+
+struct PrimeEntry {
+  uint64_t p, pn, root;
+};
+const PrimeEntry& prime_entry(uint32_t cm);
+
+// Status codes (mirrors enum yell_status_code in include/yell_gb300.h).
+enum Status : int {
+  kOk = 0,
+  kInvalidArgument = 1,
+  kUnsupportedDegree = 2,
+  kInvalidModulus = 3,
+  kCudaError = 4,
+  kOutOfMemory = 5,
+  kBudget = 6,
+  kTimeout = 7,
+  kCancelled = 8,
+  kNotFound = 9,
+  kNoDevice = 10,
+};
+
+// Records a thread-local message for yell_last_error() and returns `code`.
+int fail(int code, const std::string& msg);
+int fail_cuda(cudaError_t e, const char* what);
+const char* last_error();
+void clear_error();
+
+// Argument checks shared by the entry points.
+int check_degree(uint32_t log_n);
+int check_moduli(uint32_t cm0, uint32_t L);
+
+// Builds the reference's tables for (log_n, cm) on the host
+// (include/yell/details/ntt.hpp:97-146): out4n = phi, phi', invphi, invphi'
+// (N words each, bit-reversed); sc4 = N^-1, (N^-1)', N^-1*invphi[1], its '.
+void build_host_tables(uint32_t log_n, uint32_t cm, uint64_t* out4n, uint64_t* sc4);
+
+// One per CUDA device, created on first use with that device current.
+class DeviceContext {
+ public:
+  // Context of the current device; nullptr and a recorded error on failure.
+  static DeviceContext* current(int* status);
+
+  int device() const { return device_; }
+  cudaStream_t stream() const { return stream_; }
+
+  // DevMod array of this degree (kMaxModuli entries, device memory) with the
+  // tables of every listed modulus built and resident.  Safe to call from
+  // several threads; building takes the registry lock.  Issues no CUDA call
+  // when every table is already resident (so it is safe inside capture).
+  int ensure_tables(uint32_t log_n, uint32_t cm0, uint32_t L, const DevMod** mods);
+  int ensure_tables_list(uint32_t log_n, const uint32_t* cms, uint32_t n, const DevMod** mods);
+  const DevMod* mods_if_ready(uint32_t log_n) const;
+
+  // Device buffer of at least `words` words owned by the context; grows on
+  // demand.  The caller holds `lock` for as long as it uses the buffer.
+  struct Buffer {
+    std::mutex lock;
+    uint64_t* ptr = nullptr;
+    size_t words = 0;
+    int reserve(size_t words);  // under lock
+    ~Buffer();
+  };
+  Buffer scratch;   // polymul scratch for device-resident calls
+  Buffer staging;   // host-pointer drop-ins: operands / results
+
+  // Pipelined host polymul slots (streams + buffers), under `pipe_lock`.
+  std::mutex pipe_lock;
+  static constexpr int kPipeSlots = 3;
+  cudaStream_t pipe_stream[kPipeSlots] = {};
+  Buffer pipe_buf[kPipeSlots];
+
+  NttShape shape;  // launch shape (autotuner may adjust)
+
+ private:
+  explicit DeviceContext(int device);
+  int init();
+
+  int device_;
+  cudaStream_t stream_ = nullptr;
+  mutable std::mutex tables_mu_;
+  DevMod* d_mods_[kMaxLogN + 1] = {};
+  std::vector<uint8_t> built_[kMaxLogN + 1];
+  std::vector<void*> table_allocs_;
+};
+
+}  // namespace yell_gb300
