@@ -1,0 +1,428 @@
+#!/usr/bin/env python3
+"""Benchmark of the batched fused polymul (N = 2^16, L = 32, 16 pairs).
+
+One step = one fused polymul over the whole batch: for each of the 16 pairs
+and each of the 32 RNS limbs, NTT(a), NTT(b), Barrett product, INTT = 3
+limb-NTTs per limb, 1536 limb-NTTs per step.  A is uniform, B a centred
+discrete Gaussian (sigma 3.2, |e| <= 19) mapped per limb, both from
+splitmix64 seeds.  Each step touches 768 MiB of operands and results plus
+256 MiB of scratch, well above the 129 MB L2, so no flush is needed between
+steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank runs its own batch on its own GPU (weak scaling,
+no collective on the data path); the timed region is bracketed by barriers
+and the max over ranks is reported.  --impl reference times the reference's
+CPU algorithm (the reference's own sources when they were built here, else
+the oracle's C restatement of them) on all host cores, rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "limb-NTTs/s at N=2^16 batched vs per-call on 1 GB300; served p50/p99 polymul"
+UNIT = "limb-NTT/s"
+LOG_N, L, PAIRS = 16, 32, 16
+LIMB_NTTS_PER_STEP = 3 * L * PAIRS
+N = 1 << LOG_N
+SEED = 3
+WORKLOAD = f"fused polymul N=2^{LOG_N}, L={L} (P[0..{L - 1}]), {PAIRS} pairs"
+
+# Algorithmic bytes of one launch of each pipeline kernel per limb (pair):
+# reads + writes of the words it must move (twiddles excluded).
+ALGO_BYTES_PER_LIMB = {
+    "polymul_col_fwd_a": 16 * N,   # read a, write NTT-pass-1(a)
+    "polymul_col_fwd_b": 16 * N,   # read b, write NTT-pass-1(b)
+    "polymul_rows": 24 * N,        # read both pass-1 outputs, write pass-1 of the INTT
+    "polymul_col_inv": 16 * N,     # read, write the product
+    "polymul_whole": 24 * N,
+}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_inputs(rank: int, pairs: int = PAIRS):
+    from yell_gb300.inputs import gaussian_polys, uniform_polys
+    import yell_gb300 as y
+
+    ps = y.primes(L)
+    seed = SEED + 1000 * rank
+    a = uniform_polys(seed, PAIRS, L, LOG_N, ps)[:pairs]
+    b = gaussian_polys(seed, PAIRS, L, LOG_N, ps, offset=PAIRS * L * N)[:pairs]
+    return np.ascontiguousarray(a), np.ascontiguousarray(b)
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons in the background."""
+
+    FIELDS = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid: str | None):
+        self.uuid = (uuid or "").lower()
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        rows = self.rows
+        if self.uuid:
+            mine = [r for r in rows if self.uuid in r[0].lower()]
+            rows = mine or rows
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = [num(r[2]) for r in rows if num(r[2]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, val in zip(names, r[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(rows),
+                "power_w_max": max((num(r[3]) or 0.0) for r in rows),
+                "reasons": sorted(reasons)}
+
+
+def device_uuid(torch, dev: int):
+    try:
+        u = str(torch.cuda.get_device_properties(dev).uuid)
+        return u.replace("GPU-", "")
+    except Exception:
+        return None
+
+
+REF_SAMPLE_PAIRS = 4  # pairs per reference-arm step (a bounded sample of the batch)
+
+
+def cpu_reference_run(a, b, threads: int):
+    """One polymul batch of a.shape[0] pairs on the CPU; returns (seconds, kind)."""
+    import oracle
+
+    if oracle.ref_available():
+        try:
+            orc = oracle.Oracle("ref")
+            kind = "reference"
+        except OSError:
+            orc = oracle.Oracle("port")
+            kind = "port"
+    else:
+        orc = oracle.Oracle("port")
+        kind = "port"
+    _, secs = orc.polymul_batch(a, b, a.shape[0], L, LOG_N, threads)
+    return secs, kind
+
+
+def run_reference(args, rank: int, world: int) -> int:
+    if rank != 0:
+        return 0
+    import oracle
+
+    oracle_dir = os.path.join(ROOT, "oracle")
+    if not os.path.exists(os.path.join(oracle_dir, "liboracle.so")):
+        oracle.build()
+    from yell_gb300.inputs import gaussian_polys, uniform_polys
+
+    orc_port = oracle.Oracle("port")
+    ps = np.array([orc_port.prime(i) for i in range(L)], dtype=np.uint64)
+    a = uniform_polys(SEED, PAIRS, L, LOG_N, ps)[:REF_SAMPLE_PAIRS].copy()
+    b = gaussian_polys(SEED, PAIRS, L, LOG_N, ps, offset=PAIRS * L * N)[:REF_SAMPLE_PAIRS].copy()
+    per_step = 3 * L * REF_SAMPLE_PAIRS
+    threads = os.cpu_count() or 1
+    kind = None
+    for _ in range(args.warmup):
+        _, kind = cpu_reference_run(a, b, threads)
+    times = []
+    for _ in range(args.steps):
+        secs, kind = cpu_reference_run(a, b, threads)
+        times.append(secs)
+    total = sum(times)
+    value = per_step * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic: splitmix64 seed 3, B discrete Gaussian sigma 3.2",
+        "config": {"workload": WORKLOAD, "log_n": LOG_N, "L": L, "pairs": PAIRS,
+                   "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": f"{REF_SAMPLE_PAIRS} of the {PAIRS} pairs (x {L} limbs, "
+                                   f"{per_step} limb-NTTs) per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank: int, world: int, local_rank: int) -> int:
+    import torch
+
+    import yell_gb300 as y
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(v: float) -> float:
+        if dist is None:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    pairs = args.pairs
+    a, b = make_inputs(rank, pairs)
+    da = torch.from_numpy(a.view(np.int64)).cuda()
+    db = torch.from_numpy(b.view(np.int64)).cuda()
+    dc = torch.empty_like(da)
+    scratch = torch.empty(y.polymul_scratch_words(pairs, L, LOG_N), dtype=torch.int64,
+                          device="cuda")
+    y.init_ntt_tables(LOG_N, L)
+    stream = torch.cuda.Stream()
+
+    def step():
+        y.dev_polymul(dc, da, db, pairs, L, LOG_N, 0, scratch=scratch, stream=stream)
+
+    # ---- device-resident throughput (value) ---------------------------
+    for _ in range(max(args.warmup, 3)):
+        step()
+    barrier()
+    sampler = ClockSampler(device_uuid(torch, local_rank)) if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    barrier()
+    launches0 = y.kernel_launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = y.kernel_launches() - launches0
+    barrier()
+    if sampler:
+        sampler.stop()
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    ms_per_step = ms / args.steps
+    per_step = 3 * L * pairs
+    value = world * per_step * args.steps / (ms * 1e-3)
+
+    # ---- per-kernel device time (same workload, instrumented) -----------
+    prof_steps = min(args.steps, 20)
+    barrier()
+    y.profile_start()
+    for _ in range(prof_steps):
+        step()
+    torch.cuda.synchronize()
+    kernels = y.profile_stop()
+    total_ms = sum(t for _, t in kernels.values())
+    dom = max(kernels, key=lambda k: kernels[k][1])
+    dom_launches, dom_ms = kernels[dom]
+    per_launch_ms = dom_ms / dom_launches
+    algo = ALGO_BYTES_PER_LIMB[dom] * L * pairs
+    hbm, peak_kind = peaks()
+    achieved = algo / (per_launch_ms * 1e-3) / 1e9
+    traffic = read_ncu_traffic(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": algo, "launch_ms": per_launch_ms,
+                "traffic": traffic,
+                "share": {k: round(t / total_ms, 4) for k, (_, t) in kernels.items()},
+                "pipeline": {"algorithmic_bytes_per_step": 24 * N * L * pairs,
+                             "achieved": 24 * N * L * pairs / (ms_per_step * 1e-3) / 1e9,
+                             "frac": 24 * N * L * pairs / (ms_per_step * 1e-3) / 1e9 / hbm}}
+    if args.device_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT,
+                              "ms_per_step": ms_per_step, "pairs": pairs, "roofline": roofline,
+                              "gpu_launches": launches}), flush=True)
+        return 0
+
+    # ---- plain per-call path: one launch per reference call -------------
+    ta = da.clone().reshape(-1)
+    tb = db.clone().reshape(-1)
+
+    def per_call():
+        for pi in range(pairs):
+            for l in range(L):
+                off = (pi * L + l) * N
+                va = ta[off:off + N]
+                vb = tb[off:off + N]
+                y.dev_ntt(va, 1, 1, LOG_N, l, y.YELL_FORWARD, stream=stream)
+                y.dev_ntt(vb, 1, 1, LOG_N, l, y.YELL_FORWARD, stream=stream)
+                y.dev_elementwise(y.YELL_OP_MULMOD, va, va, vb, 1, 1, LOG_N, l, stream=stream)
+                y.dev_ntt(va, 1, 1, LOG_N, l, y.YELL_BACKWARD, stream=stream)
+
+    per_call()
+    barrier()
+    pc_steps = 2
+    e0.record(stream)
+    for _ in range(pc_steps):
+        per_call()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    pc_ms = max_over_ranks(e0.elapsed_time(e1)) / pc_steps
+    per_call_value = world * per_step / (pc_ms * 1e-3)
+    del ta, tb
+
+    # ---- end to end through the host-memory C ABI call --------------------
+    pa = y.PinnedBuffer(a.shape)
+    pb = y.PinnedBuffer(b.shape)
+    pc = y.PinnedBuffer(a.shape)
+    pa.array[:] = a
+    pb.array[:] = b
+    e2e_steps = max(3, min(args.steps, 20))
+    y.polymul_host(pa.array, pb.array, LOG_N, out=pc.array)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        y.polymul_host(pa.array, pb.array, LOG_N, out=pc.array)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = world * per_step * e2e_steps / e2e_s
+    e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(a.nbytes + b.nbytes),
+           "d2h_bytes_per_step": int(a.nbytes), "ms_per_step": 1e3 * e2e_s / e2e_steps,
+           "path": "yell_polymul_host from pinned host buffers"}
+    for buf in (pa, pb, pc):
+        buf.free()
+
+    # ---- CPU baseline (rank 0 at N=1 only) --------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        ns = min(pairs, REF_SAMPLE_PAIRS)
+        secs, kind = cpu_reference_run(a[:ns].copy(), b[:ns].copy(), threads)
+        cpu = {"value": 3 * L * ns / secs, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": f"{ns} of the {pairs} pairs x {L} limbs ({3 * L * ns} limb-NTTs, "
+                         f"{secs:.2f} s wall)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic: splitmix64 seed 3 (+1000 per rank), B discrete Gaussian sigma 3.2",
+            "config": {"workload": WORKLOAD, "log_n": LOG_N, "L": L, "pairs": PAIRS,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (768 MiB operands+result per step)"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": sampler.summary() if sampler else None,
+            "per_call": {"value": per_call_value, "unit": UNIT, "ms_per_step": pc_ms,
+                         "path": "one launch per reference call: forward(a), forward(b), "
+                                 "mulmod, backward per limb"},
+            "batched_vs_per_call": value / per_call_value,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def read_ncu_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 2 and parts[0] == kernel:
+                    return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--device-only", action="store_true",
+                    help="time only the device-resident batch (for profiler captures)")
+    ap.add_argument("--pairs", type=int, default=PAIRS,
+                    help="pairs per batch (profiling of a smaller case; default 16)")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus == 1 else 1)))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

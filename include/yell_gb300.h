@@ -158,6 +158,16 @@ int yell_dev_polymul(uint64_t* d_c, const uint64_t* d_a, const uint64_t* d_b, ui
 /* Waits for all work the library queued on its own stream of this device. */
 int yell_synchronize(void);
 
+/* ---- launch profiling (no counterpart in the reference) -----------------
+ * Between start and stop every kernel the library launches is bracketed by
+ * CUDA events on its stream; stop waits for them and totals the device time
+ * per kernel name.  get() returns the i-th kernel's name, launch count and
+ * total milliseconds. */
+int yell_profile_start(void);
+int yell_profile_stop(void);
+int yell_profile_count(void);
+int yell_profile_get(int i, char* name, size_t name_len, uint64_t* launches, double* total_ms);
+
 #ifdef __cplusplus
 }
 #endif

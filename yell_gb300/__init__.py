@@ -244,6 +244,24 @@ def synchronize() -> None:
     call("yell_synchronize")
 
 
+def profile_start() -> None:
+    call("yell_profile_start")
+
+
+def profile_stop() -> dict:
+    """Stops launch profiling; returns {kernel: (launches, total_ms)}."""
+    call("yell_profile_stop")
+    out = {}
+    lib = load()
+    for i in range(lib.yell_profile_count()):
+        name = ctypes.create_string_buffer(128)
+        n = ctypes.c_uint64()
+        ms = ctypes.c_double()
+        call("yell_profile_get", i, name, 128, ctypes.addressof(n), ctypes.addressof(ms))
+        out[name.value.decode()] = (int(n.value), float(ms.value))
+    return out
+
+
 class Poly:
     """Host polynomial mirroring yell::poly<N> (include/yell/poly.hpp:43-137):
     L limbs of N uint64 words, limb cm reduced mod prime(cm); every method

@@ -75,6 +75,10 @@ SIGNATURES = {
     "yell_polymul_scratch_words": (_sz, [_u32, _u32, _u32]),
     "yell_dev_polymul": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp, _sz, _vp]),
     "yell_synchronize": (_int, []),
+    "yell_profile_start": (_int, []),
+    "yell_profile_stop": (_int, []),
+    "yell_profile_count": (_int, []),
+    "yell_profile_get": (_int, [_int, ctypes.c_char_p, _sz, _vp, _vp]),
 }
 
 _lib = None

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "kernels.h"
+#include "profiler.h"
 #include "runtime.h"
 
 using namespace yell_gb300;
@@ -400,6 +401,23 @@ int yell_dev_polymul(uint64_t* d_c, const uint64_t* d_a, const uint64_t* d_b, ui
                            ctx->shape, st),
             "launch polymul");
   YELL_CUDA(cudaStreamSynchronize(st), "synchronize");
+  return kOk;
+}
+
+int yell_profile_start(void) { return profile_start() == 0 ? kOk : fail(kCudaError, "profile start"); }
+
+int yell_profile_stop(void) {
+  return profile_stop() == 0 ? kOk : fail(kCudaError, "profile stop: event wait failed");
+}
+
+int yell_profile_count(void) { return profile_count(); }
+
+int yell_profile_get(int i, char* name, size_t name_len, uint64_t* launches, double* total_ms) {
+  if (!name || name_len == 0 || !launches || !total_ms) return fail(kInvalidArgument, "null output");
+  std::string n;
+  if (profile_get(i, &n, launches, total_ms) != 0) return fail(kNotFound, "no such profile entry");
+  std::strncpy(name, n.c_str(), name_len - 1);
+  name[name_len - 1] = '\0';
   return kOk;
 }
 

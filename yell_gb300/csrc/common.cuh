@@ -63,40 +63,79 @@ struct ConstLimbSet {
 // the compiler; there is no 64-bit multiplier on the SM.
 // ---------------------------------------------------------------------------
 
+// lo64(a*w + q*np) from 32-bit IMAD.WIDE / IMAD: with np = 2^64 - p this is
+// a*w - q*p (mod 2^64) without a 64-bit subtraction.
+__device__ __forceinline__ uint64_t lo_mul_add(uint64_t a, uint64_t w, uint64_t q, uint64_t np) {
+  uint64_t r;
+  asm("{\n\t"
+      ".reg .u32 a0, a1, w0, w1, q0, q1, n0, n1, rl, rh;\n\t"
+      ".reg .u64 t;\n\t"
+      "mov.b64 {a0, a1}, %1;\n\t"
+      "mov.b64 {w0, w1}, %2;\n\t"
+      "mov.b64 {q0, q1}, %3;\n\t"
+      "mov.b64 {n0, n1}, %4;\n\t"
+      "mul.wide.u32 t, a0, w0;\n\t"
+      "mad.wide.u32 t, q0, n0, t;\n\t"
+      "mov.b64 {rl, rh}, t;\n\t"
+      "mad.lo.u32 rh, a0, w1, rh;\n\t"
+      "mad.lo.u32 rh, a1, w0, rh;\n\t"
+      "mad.lo.u32 rh, q0, n1, rh;\n\t"
+      "mad.lo.u32 rh, q1, n0, rh;\n\t"
+      "mov.b64 %0, {rl, rh};\n\t"
+      "}"
+      : "=l"(r)
+      : "l"(a), "l"(w), "l"(q), "l"(np));
+  return r;
+}
+
+// u >= m ? u - m : u, as a borrow mask and a bitwise select per 32-bit half.
+__device__ __forceinline__ uint64_t csub(uint64_t u, uint64_t m) {
+  uint64_t r;
+  asm("{\n\t"
+      ".reg .u32 ul, uh, ml, mh, dl, dh, b;\n\t"
+      "mov.b64 {ul, uh}, %1;\n\t"
+      "mov.b64 {ml, mh}, %2;\n\t"
+      "sub.cc.u32 dl, ul, ml;\n\t"
+      "subc.cc.u32 dh, uh, mh;\n\t"
+      "subc.u32 b, 0, 0;\n\t"
+      "lop3.b32 dl, ul, dl, b, 0xE4;\n\t"
+      "lop3.b32 dh, uh, dh, b, 0xE4;\n\t"
+      "mov.b64 %0, {dl, dh};\n\t"
+      "}"
+      : "=l"(r)
+      : "l"(u), "l"(m));
+  return r;
+}
+
 // Shoup product with the precomputed companion w' = floor(w * 2^64 / p):
 // x*w - hi64(x*w')*p (mod 2^64).  For x < 2^64 the value lies in [0, 2p).
-// lib/ntt.cpp:59-62 (GS) and :79-80 (CT).
-__device__ __forceinline__ uint64_t shoup_lazy(uint64_t x, uint64_t w, uint64_t wp, uint64_t p) {
-  const uint64_t q = __umul64hi(x, wp);
-  return x * w - q * p;
+// lib/ntt.cpp:59-62 (GS) and :79-80 (CT).  np = 2^64 - p.
+__device__ __forceinline__ uint64_t shoup_lazy(uint64_t x, uint64_t w, uint64_t wp, uint64_t np) {
+  return lo_mul_add(x, w, __umul64hi(x, wp), np);
 }
 
 // Cooley-Tukey butterfly, lib/ntt.cpp:69-83.  In/out [0, 4p).
 __device__ __forceinline__ void ct_bfly(uint64_t& x0, uint64_t& x1, uint64_t w, uint64_t wp,
-                                        uint64_t p, uint64_t p2) {
-  uint64_t u0 = x0;
-  u0 = (u0 >= p2) ? u0 - p2 : u0;
-  const uint64_t t = shoup_lazy(x1, w, wp, p);
+                                        uint64_t np, uint64_t p2) {
+  const uint64_t u0 = csub(x0, p2);
+  const uint64_t t = shoup_lazy(x1, w, wp, np);
   x0 = u0 + t;
   x1 = u0 - t + p2;
 }
 
 // Gentleman-Sande butterfly, lib/ntt.cpp:47-63.  In/out [0, 2p).
 __device__ __forceinline__ void gs_bfly(uint64_t& x0, uint64_t& x1, uint64_t w, uint64_t wp,
-                                        uint64_t p, uint64_t p2) {
+                                        uint64_t np, uint64_t p2) {
   const uint64_t u0 = x0, u1 = x1;
-  uint64_t t0 = u0 + u1;
-  t0 = (t0 >= p2) ? t0 - p2 : t0;
   const uint64_t t1 = u0 - u1 + p2;
-  x0 = t0;
-  x1 = shoup_lazy(t1, w, wp, p);
+  x0 = csub(u0 + u1, p2);
+  x1 = shoup_lazy(t1, w, wp, np);
 }
 
 // ops::mulmod_shoup, include/yell/ops.hpp:122-132: Shoup product plus one
 // conditional subtraction of p.
 __device__ __forceinline__ uint64_t mulmod_shoup(uint64_t x, uint64_t y, uint64_t yp, uint64_t p) {
-  uint64_t r = shoup_lazy(x, y, yp, p);
-  return (r >= p) ? r - p : r;
+  return csub(shoup_lazy(x, y, yp, 0 - p), p);
 }
 
 // Last inverse layer with the N^-1 scaling fused in,
@@ -110,8 +149,7 @@ __device__ __forceinline__ void gs_last(uint64_t& x0, uint64_t& x1, const DevMod
 // Final correction of ntt<N>::forward, include/yell/details/ntt.hpp:179-187:
 // v -= 2p if v >= 2p; v -= p if v >= p.
 __device__ __forceinline__ uint64_t fwd_correct(uint64_t v, uint64_t p, uint64_t p2) {
-  v = (v >= p2) ? v - p2 : v;
-  return (v >= p) ? v - p : v;
+  return csub(csub(v, p2), p);
 }
 
 // Barrett reduction of the 128-bit value (xh:xl), lib/ops.cpp:5-21:

@@ -10,19 +10,26 @@
 //     contiguous blocks of B words.  The inverse runs the same passes in the
 //     opposite order; its column pass ends with the scaled last layer.
 //   * fused polymul: NTT(a), NTT(b), Barrett product and INTT in one kernel
-//     (whole-limb) or three (two-pass: column pass of a and b, then one row
+//     (whole-limb) or three (two-pass: column pass of a and of b, one row
 //     kernel doing forward rows of both, the product and inverse rows, then
 //     the inverse column pass).  The last forward round of both operands,
 //     the product and the first inverse round share one register set.
+//
+// Global I/O goes straight between registers and HBM in rounds whose lanes
+// cover contiguous words (the top round of a row tile, every round of a
+// column tile); the other ends are staged through shared memory so that the
+// HBM accesses stay coalesced.
+#include <utility>
+
 #include "kernels.h"
 #include "ntt_tile.cuh"
+#include "profiler.h"
 
 namespace yell_gb300 {
 
 namespace {
 
-constexpr uint32_t kTwoPassTileLog = 12;  // 4096 words per two-pass tile
-constexpr uint32_t kTwoPassThreads = 1u << (kTwoPassTileLog - 4);
+constexpr int kTileLog = 12;  // 4096 words per two-pass tile
 
 __device__ __forceinline__ ulonglong2 ld_pair(const uint64_t* p) {
   return __ldg(reinterpret_cast<const ulonglong2*>(p));
@@ -32,250 +39,419 @@ __device__ __forceinline__ void st_pair(uint64_t* p, uint64_t a, uint64_t b) {
   *reinterpret_cast<ulonglong2*>(p) = make_ulonglong2(a, b);
 }
 
-// ---------------------------------------------------------------------------
-// Whole-limb NTT.  Tile of 2^T words = 2^(T - log_n) limbs; 2^(T - LOGE)
-// threads.  dir: 0 forward (reduced), 1 forward lazy, 2 backward.
-// ---------------------------------------------------------------------------
-template <int LOGE>
-__global__ void __launch_bounds__(512) k_ntt_whole(LimbSet ls, uint32_t log_n, uint32_t T,
-                                                   const DevMod* __restrict__ mods, int dir) {
-  extern __shared__ __align__(16) uint64_t smem[];
-  const uint32_t tid = threadIdx.x;
-  const uint32_t K = log_n, N = 1u << K, words = 1u << T;
-  const uint32_t limb0 = blockIdx.x << (T - K);
-  for (uint32_t v = tid * 2; v < words; v += blockDim.x * 2) {
-    const uint32_t limb = limb0 + (v >> K);
-    if (limb < ls.count) {
-      const ulonglong2 d = ld_pair(ls.limb(limb, log_n) + (v & (N - 1)));
-      smem[sidx(v)] = d.x;
-      smem[sidx(v + 1)] = d.y;
+// ---- direct global access for one round ---------------------------------------
+// Row-type region: word u of the region at g[u]; base_u and offsets are
+// u-space (tile bits below LB + K, LB = 0).
+template <class RG>
+__device__ __forceinline__ void gload_rows(uint64_t* x, const uint64_t* g, uint32_t base_u) {
+  constexpr int R = RG::R;
+  const uint64_t* gb = g + base_u;
+  if constexpr (RG::PAIRS) {
+#pragma unroll
+    for (int m = 0; m < RG::E / 2; ++m)
+#pragma unroll
+      for (int j = 0; j < (1 << R); ++j) {
+        const ulonglong2 v = ld_pair(gb + RG::off(2 * m, j));
+        x[((2 * m) << R) | j] = v.x;
+        x[((2 * m + 1) << R) | j] = v.y;
+      }
+  } else {
+#pragma unroll
+    for (int ex = 0; ex < RG::E; ++ex)
+#pragma unroll
+      for (int j = 0; j < (1 << R); ++j) x[(ex << R) | j] = __ldg(gb + RG::off(ex, j));
+  }
+}
+
+template <class RG>
+__device__ __forceinline__ void gstore_rows(const uint64_t* x, uint64_t* g, uint32_t base_u) {
+  constexpr int R = RG::R;
+  uint64_t* gb = g + base_u;
+  if constexpr (RG::PAIRS) {
+#pragma unroll
+    for (int m = 0; m < RG::E / 2; ++m)
+#pragma unroll
+      for (int j = 0; j < (1 << R); ++j)
+        st_pair(gb + RG::off(2 * m, j), x[((2 * m) << R) | j], x[((2 * m + 1) << R) | j]);
+  } else {
+#pragma unroll
+    for (int ex = 0; ex < RG::E; ++ex)
+#pragma unroll
+      for (int j = 0; j < (1 << R); ++j) gb[RG::off(ex, j)] = x[(ex << R) | j];
+  }
+}
+
+// Column tile: tile word v (row c = v >> LB, column v & (2^LB - 1)) is at
+// g[(c << LOGB) + column], g = limb + first column of the tile.
+template <class RG, int LOGB>
+__device__ __forceinline__ size_t col_base(uint32_t base_v) {
+  return ((size_t)(base_v >> RG::LB) << LOGB) + (base_v & ((1u << RG::LB) - 1u));
+}
+
+template <class RG, int LOGB>
+__device__ __forceinline__ void gload_cols(uint64_t* x, const uint64_t* g, uint32_t base_v) {
+  constexpr int R = RG::R;
+  const uint64_t* gb = g + col_base<RG, LOGB>(base_v);
+#pragma unroll
+  for (int ex = 0; ex < RG::E; ++ex)
+#pragma unroll
+    for (int j = 0; j < (1 << R); ++j)
+      x[(ex << R) | j] = __ldg(gb + ((size_t)(RG::off(ex, j) >> RG::LB) << LOGB));
+}
+
+template <class RG, int LOGB>
+__device__ __forceinline__ void gstore_cols(const uint64_t* x, uint64_t* g, uint32_t base_v) {
+  constexpr int R = RG::R;
+  uint64_t* gb = g + col_base<RG, LOGB>(base_v);
+#pragma unroll
+  for (int ex = 0; ex < RG::E; ++ex)
+#pragma unroll
+    for (int j = 0; j < (1 << R); ++j) gb[(size_t)(RG::off(ex, j) >> RG::LB) << LOGB] = x[(ex << R) | j];
+}
+
+// ---- staged (coalesced) copies between a whole tile and HBM ------------------
+// Whole-limb tile: 2^T words = 2^(T-K) limbs of 2^K words.
+template <class C>
+__device__ __forceinline__ void stage_in_limbs(uint64_t* s, const ConstLimbSet& src, uint32_t limb0,
+                                               uint32_t count, uint32_t log_n) {
+  for (uint32_t v = threadIdx.x * 2; v < (1u << C::T); v += C::THREADS * 2) {
+    const uint32_t limb = limb0 + (v >> C::K);
+    if (limb < count)
+      *reinterpret_cast<ulonglong2*>(s + sidx(v)) =
+          ld_pair(src.limb(limb, log_n) + (v & ((1u << C::K) - 1u)));
+  }
+}
+
+// Copies the tile out; `reduce` applies ntt<N>::forward's final reduction.
+template <class C>
+__device__ __forceinline__ void stage_out_limbs(const uint64_t* s, const LimbSet& dst, uint32_t limb0,
+                                                uint32_t log_n, const DevMod* __restrict__ mods,
+                                                bool reduce) {
+  for (uint32_t v = threadIdx.x * 2; v < (1u << C::T); v += C::THREADS * 2) {
+    const uint32_t limb = limb0 + (v >> C::K);
+    if (limb < dst.count) {
+      ulonglong2 d = *reinterpret_cast<const ulonglong2*>(s + sidx(v));
+      if (reduce) {
+        const uint64_t p = __ldg(&mods[dst.cm(limb)].p);
+        d.x = fwd_correct(d.x, p, p << 1);
+        d.y = fwd_correct(d.y, p, p << 1);
+      }
+      *reinterpret_cast<ulonglong2*>(dst.limb(limb, log_n) + (v & ((1u << C::K) - 1u))) = d;
     }
   }
-  __syncthreads();
-  const uint32_t my_limb = limb0 + (tid >> (K - LOGE));
+}
+
+// Contiguous 2^T-word region.
+template <class C>
+__device__ __forceinline__ void stage_in_region(uint64_t* s, const uint64_t* g) {
+  for (uint32_t v = threadIdx.x * 2; v < (1u << C::T); v += C::THREADS * 2)
+    *reinterpret_cast<ulonglong2*>(s + sidx(v)) = ld_pair(g + v);
+}
+
+template <class C>
+__device__ __forceinline__ void stage_out_region(const uint64_t* s, uint64_t* g, uint64_t p, bool reduce) {
+  for (uint32_t v = threadIdx.x * 2; v < (1u << C::T); v += C::THREADS * 2) {
+    ulonglong2 d = *reinterpret_cast<const ulonglong2*>(s + sidx(v));
+    if (reduce) {
+      d.x = fwd_correct(d.x, p, p << 1);
+      d.y = fwd_correct(d.y, p, p << 1);
+    }
+    st_pair(g + v, d.x, d.y);
+  }
+}
+
+__host__ __device__ ConstLimbSet as_const(const LimbSet& l) {
+  ConstLimbSet c;
+  c.base = l.base;
+  c.ptrs = l.ptrs;
+  c.cms = l.cms;
+  c.count = l.count;
+  c.L = l.L;
+  c.cm0 = l.cm0;
+  c.pad_ = 0;
+  return c;
+}
+
+// ===========================================================================
+// Whole-limb NTT.  DIR: 0 forward (reduced), 1 forward lazy, 2 backward.
+// ===========================================================================
+template <class C, int DIR>
+__global__ void __launch_bounds__(C::THREADS) k_ntt_whole(LimbSet ls, const DevMod* __restrict__ mods) {
+  extern __shared__ __align__(16) uint64_t smem[];
+  constexpr int K = C::K, NR = C::NR;
+  const uint32_t log_n = K;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t limb0 = blockIdx.x << (C::T - K);
+  const uint32_t my_limb = limb0 + C::sub(tid);
   const bool active = my_limb < ls.count;
   const DevMod m = load_mod(mods, ls.cm(active ? my_limb : 0));
-  if (dir == 2)
-    inv_tile<LOGE>(smem, tid, 0, K, log_n, 0, 0, m, active, true);
-  else
-    fwd_tile<LOGE>(smem, tid, 0, K, 0, 0, m.fwd, m.p, active);
-  for (uint32_t v = tid * 2; v < words; v += blockDim.x * 2) {
-    const uint32_t limb = limb0 + (v >> K);
-    if (limb < ls.count) {
-      uint64_t a = smem[sidx(v)], b = smem[sidx(v + 1)];
-      if (dir == 0) {
-        const uint64_t p = __ldg(&mods[ls.cm(limb)].p);
-        a = fwd_correct(a, p, p << 1);
-        b = fwd_correct(b, p, p << 1);
+  const uint32_t umask = (1u << K) - 1u;
+  if constexpr (DIR != 2) {
+    // forward: round 0 straight from HBM when it is not also the last round
+    if constexpr (NR > 1) {
+      using RG = Round<C, 0>;
+      uint64_t x[1 << C::LOGE];
+      const uint32_t b = RG::base(tid);
+      if (active) {
+        gload_rows<RG>(x, ls.limb(my_limb, log_n), b & umask);
+        ct_round<RG>(x, m.fwd, RG::HI, RG::gr(b, 0), m.p);
+        smem_store<RG>(x, smem, b);
       }
-      st_pair(ls.limb(limb, log_n) + (v & (N - 1)), a, b);
+      __syncthreads();
+      fwd_rounds<C, 1, NR>(smem, tid, 0, 0, m.fwd, m.p, active);
+    } else {
+      stage_in_limbs<C>(smem, as_const(ls), limb0, ls.count, log_n);
+      __syncthreads();
+      fwd_rounds<C, 0, NR>(smem, tid, 0, 0, m.fwd, m.p, active);
+    }
+    stage_out_limbs<C>(smem, ls, limb0, log_n, mods, DIR == 0);
+  } else {
+    stage_in_limbs<C>(smem, as_const(ls), limb0, ls.count, log_n);
+    __syncthreads();
+    if constexpr (NR > 1) {
+      inv_rounds<C, NR - 1, 0, true>(smem, tid, log_n, 0, 0, m, active);
+      using RG = Round<C, 0>;
+      uint64_t x[1 << C::LOGE];
+      const uint32_t b = RG::base(tid);
+      if (active) {
+        smem_load<RG>(x, smem, b);
+        gs_round<RG, true>(x, log_n, RG::BETA, RG::gr(b, 0), m);
+        gstore_rows<RG>(x, ls.limb(my_limb, log_n), b & umask);
+      }
+    } else {
+      inv_rounds<C, 0, -1, true>(smem, tid, log_n, 0, 0, m, active);
+      stage_out_limbs<C>(smem, ls, limb0, log_n, mods, false);
     }
   }
 }
 
-// ---------------------------------------------------------------------------
-// Two-pass: column pass.  Tile = C x ncols words, C = 2^k1, ncols = 2^lb,
-// lb = 12 - k1; tile word v = c * ncols + col is global word c*B + col0 + col.
-// Forward: stages 0..k1-1.  Inverse: stages log2(B)..log_n-1 ending with the
-// scaled last layer.  src and dst may be the same limbs (in place).
-// ---------------------------------------------------------------------------
-template <bool INV>
-__global__ void __launch_bounds__(256) k_col_pass(ConstLimbSet src, LimbSet dst, uint32_t log_n,
-                                                  uint32_t k1, const DevMod* __restrict__ mods) {
+// ===========================================================================
+// Two-pass column pass.  Tile = 2^K rows x 2^LB columns (K + LB = 12);
+// limb word (c << LOGB) + col0 + col.  Forward: stages 0..K-1; inverse:
+// stages LOGB..log_n-1 with the scaled last layer.  src and dst may alias.
+// ===========================================================================
+template <class C, int LOGB, bool INV>
+__global__ void __launch_bounds__(C::THREADS) k_col_pass(ConstLimbSet src, LimbSet dst,
+                                                         const DevMod* __restrict__ mods) {
   extern __shared__ __align__(16) uint64_t smem[];
+  constexpr int K = C::K, LB = C::LB, NR = C::NR;
+  constexpr uint32_t log_n = K + LOGB;
+  constexpr int TPL = LOGB - LB;  // log2(tiles per limb)
   const uint32_t tid = threadIdx.x;
-  const uint32_t lb = kTwoPassTileLog - k1, logB = log_n - k1;
-  const uint32_t tpl_log = logB - lb;  // log2(tiles per limb)
-  const uint32_t limb = blockIdx.x >> tpl_log;
-  const uint32_t col0 = (blockIdx.x & ((1u << tpl_log) - 1u)) << lb;
-  const uint64_t* in = src.limb(limb, log_n);
-  uint64_t* out = dst.limb(limb, log_n);
-  const uint32_t cmask = (1u << lb) - 1u;
-  for (uint32_t v = tid * 2; v < (1u << kTwoPassTileLog); v += kTwoPassThreads * 2) {
-    const ulonglong2 d = ld_pair(in + ((size_t)(v >> lb) << logB) + col0 + (v & cmask));
-    smem[sidx(v)] = d.x;
-    smem[sidx(v + 1)] = d.y;
-  }
-  __syncthreads();
+  const uint32_t limb = blockIdx.x >> TPL;
+  const uint32_t col0 = (blockIdx.x & ((1u << TPL) - 1u)) << LB;
+  const uint64_t* in = src.limb(limb, log_n) + col0;
+  uint64_t* out = dst.limb(limb, log_n) + col0;
   const DevMod m = load_mod(mods, dst.cm(limb));
-  if (INV)
-    inv_tile<4>(smem, tid, lb, k1, log_n, logB, 0, m, true, true);
-  else
-    fwd_tile<4>(smem, tid, lb, k1, 0, 0, m.fwd, m.p, true);
-  for (uint32_t v = tid * 2; v < (1u << kTwoPassTileLog); v += kTwoPassThreads * 2)
-    st_pair(out + ((size_t)(v >> lb) << logB) + col0 + (v & cmask), smem[sidx(v)], smem[sidx(v + 1)]);
-}
-
-// ---------------------------------------------------------------------------
-// Two-pass: row pass over 4096 contiguous words (4096 / B blocks of B).
-// Forward: stages k1..log_n-1 (+ the reduction of ntt::forward when
-// fwd_full); inverse: stages 0..log2(B)-1.  In place.
-// ---------------------------------------------------------------------------
-template <bool INV>
-__global__ void __launch_bounds__(256) k_row_pass(LimbSet ls, uint32_t log_n, uint32_t k1,
-                                                  const DevMod* __restrict__ mods, int fwd_full) {
-  extern __shared__ __align__(16) uint64_t smem[];
-  const uint32_t tid = threadIdx.x;
-  const uint32_t logB = log_n - k1;
-  const uint32_t tpl_log = log_n - kTwoPassTileLog;
-  const uint32_t limb = blockIdx.x >> tpl_log;
-  const uint32_t off = (blockIdx.x & ((1u << tpl_log) - 1u)) << kTwoPassTileLog;
-  uint64_t* data = ls.limb(limb, log_n) + off;
-  for (uint32_t v = tid * 2; v < (1u << kTwoPassTileLog); v += kTwoPassThreads * 2) {
-    const ulonglong2 d = ld_pair(data + v);
-    smem[sidx(v)] = d.x;
-    smem[sidx(v + 1)] = d.y;
-  }
-  __syncthreads();
-  const DevMod m = load_mod(mods, ls.cm(limb));
-  const uint32_t G = (off >> logB) + (tid >> (logB - 4));
-  if (INV)
-    inv_tile<4>(smem, tid, 0, logB, log_n, 0, G, m, true, false);
-  else
-    fwd_tile<4>(smem, tid, 0, logB, k1, G, m.fwd, m.p, true);
-  const uint64_t p = m.p, p2 = m.p << 1;
-  for (uint32_t v = tid * 2; v < (1u << kTwoPassTileLog); v += kTwoPassThreads * 2) {
-    uint64_t a = smem[sidx(v)], b = smem[sidx(v + 1)];
-    if (!INV && fwd_full) {
-      a = fwd_correct(a, p, p2);
-      b = fwd_correct(b, p, p2);
+  uint64_t x[1 << C::LOGE];
+  if constexpr (!INV) {
+    using R0 = Round<C, 0>;
+    const uint32_t b0 = R0::base(tid);
+    gload_cols<R0, LOGB>(x, in, b0);
+    ct_round<R0>(x, m.fwd, R0::HI, R0::gr(b0, 0), m.p);
+    if constexpr (NR == 1) {
+      gstore_cols<R0, LOGB>(x, out, b0);
+    } else {
+      smem_store<R0>(x, smem, b0);
+      __syncthreads();
+      fwd_rounds<C, 1, NR - 1>(smem, tid, 0, 0, m.fwd, m.p, true);
+      using RL = Round<C, NR - 1>;
+      const uint32_t bl = RL::base(tid);
+      smem_load<RL>(x, smem, bl);
+      ct_round<RL>(x, m.fwd, RL::HI, RL::gr(bl, 0), m.p);
+      gstore_cols<RL, LOGB>(x, out, bl);
     }
-    st_pair(data + v, a, b);
+  } else {
+    using RB = Round<C, NR - 1>;  // bottom round, executed first
+    const uint32_t bb = RB::base(tid);
+    gload_cols<RB, LOGB>(x, in, bb);
+    if constexpr (NR == 1) {
+      gs_round<RB, true>(x, log_n, LOGB + RB::BETA, RB::gr(bb, 0), m);
+      gstore_cols<RB, LOGB>(x, out, bb);
+    } else {
+      gs_round<RB, false>(x, log_n, LOGB + RB::BETA, RB::gr(bb, 0), m);
+      smem_store<RB>(x, smem, bb);
+      __syncthreads();
+      inv_rounds<C, NR - 2, 0, false>(smem, tid, log_n, LOGB, 0, m, true);
+      using RT = Round<C, 0>;
+      const uint32_t bt = RT::base(tid);
+      smem_load<RT>(x, smem, bt);
+      gs_round<RT, true>(x, log_n, LOGB + RT::BETA, RT::gr(bt, 0), m);
+      gstore_cols<RT, LOGB>(x, out, bt);
+    }
   }
 }
 
-// ---------------------------------------------------------------------------
-// Fused product step shared by both polymul kernels: the last forward round
-// (R = LOGE at bit 0) of both operands, the reduction of ntt::forward, the
-// Barrett product of ops::mulmod and the first inverse round (R = LOGE at bit
-// 0), all on one register set; the result goes back to sa.
-// ---------------------------------------------------------------------------
-template <int LOGE>
-__device__ __forceinline__ void fused_product_round(uint64_t* sa, const uint64_t* sb, uint32_t tid,
-                                                    uint32_t K, uint32_t log_n, uint32_t s_off,
-                                                    uint32_t G, const DevMod& m, bool active,
-                                                    bool inv_last) {
-  constexpr int E = 1 << LOGE;
-  if (!active) return;
-  const uint32_t base = thread_base<LOGE, LOGE>(tid, 0, 0);
-  const uint32_t hi_bits = K - LOGE;
-  const uint32_t u_hi = (base >> LOGE) & ((1u << hi_bits) - 1u);
-  const uint32_t gr = (G << hi_bits) + u_hi;
+// ===========================================================================
+// Two-pass row pass over 4096 contiguous words (2^(12-K) blocks of 2^K).
+// Forward: stages k1..log_n-1 (+ the final reduction when reduce); inverse:
+// stages 0..K-1.  In place.
+// ===========================================================================
+template <class C, int K1, bool INV>
+__global__ void __launch_bounds__(C::THREADS) k_row_pass(LimbSet ls, const DevMod* __restrict__ mods,
+                                                         int reduce) {
+  extern __shared__ __align__(16) uint64_t smem[];
+  constexpr int K = C::K, NR = C::NR;
+  constexpr uint32_t log_n = K + K1;
+  constexpr int TPL = log_n - kTileLog;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t limb = blockIdx.x >> TPL;
+  const uint32_t off = (blockIdx.x & ((1u << TPL) - 1u)) << kTileLog;
+  uint64_t* data = ls.limb(limb, log_n) + off;
+  const DevMod m = load_mod(mods, ls.cm(limb));
+  const uint32_t G = (off >> K) + C::sub(tid);
+  if constexpr (!INV) {
+    using R0 = Round<C, 0>;
+    uint64_t x[1 << C::LOGE];
+    const uint32_t b0 = R0::base(tid);
+    gload_rows<R0>(x, data, b0);
+    ct_round<R0>(x, m.fwd, K1 + R0::HI, R0::gr(b0, G), m.p);
+    smem_store<R0>(x, smem, b0);
+    __syncthreads();
+    fwd_rounds<C, 1, NR>(smem, tid, K1, G, m.fwd, m.p, true);
+    stage_out_region<C>(smem, data, m.p, reduce != 0);
+  } else {
+    stage_in_region<C>(smem, data);
+    __syncthreads();
+    inv_rounds<C, NR - 1, 0, false>(smem, tid, log_n, 0, G, m, true);
+    using RT = Round<C, 0>;
+    uint64_t x[1 << C::LOGE];
+    const uint32_t bt = RT::base(tid);
+    smem_load<RT>(x, smem, bt);
+    gs_round<RT, false>(x, log_n, RT::BETA, RT::gr(bt, G), m);
+    gstore_rows<RT>(x, data, bt);
+  }
+}
+
+// ===========================================================================
+// Fused product round shared by both polymul kernels: the bottom forward
+// round (R = LOGE at bit 0) of both operands with shared twiddles, the
+// reduction of ntt<N>::forward, the Barrett product of ops::mulmod and the
+// bottom inverse round, on one register set.
+// ===========================================================================
+template <class C, bool INV_LAST>
+__device__ __forceinline__ void fused_product(uint64_t* xa, uint64_t* xb, uint32_t b, uint32_t log_n,
+                                              uint32_t s_off, uint32_t G, const DevMod& m) {
+  using RB = Round<C, C::NR - 1>;
+  static_assert(RB::R == C::LOGE && RB::BETA == 0, "bottom round must be full width");
+  constexpr int E = 1 << C::LOGE;
   const uint64_t p = m.p, p2 = m.p << 1;
-  uint64_t xa[E], xb[E];
-  load_regs<LOGE, LOGE>(xa, sa, base, 0, 0);
-  ct_round<LOGE, LOGE>(xa, s_off + hi_bits, gr, m.fwd, p, p2);
-  load_regs<LOGE, LOGE>(xb, sb, base, 0, 0);
-  ct_round<LOGE, LOGE>(xb, s_off + hi_bits, gr, m.fwd, p, p2);
+  const uint32_t gr = RB::gr(b, G);
+  ct_stages2<RB::R, RB::E, 0>(xa, xb, m.fwd, s_off + RB::HI, gr, 0 - p, p2);
 #pragma unroll
   for (int i = 0; i < E; ++i)
     xa[i] = mulmod_barrett(fwd_correct(xa[i], p, p2), fwd_correct(xb[i], p, p2), p, m.pn);
-  if (inv_last)
-    gs_round<LOGE, LOGE, true>(xa, log_n, 0, gr, m.inv, m);
-  else
-    gs_round<LOGE, LOGE, false>(xa, log_n, 0, gr, m.inv, m);
-  store_regs<LOGE, LOGE>(xa, sa, base, 0, 0);
+  gs_round<RB, INV_LAST>(xa, log_n, 0, gr, m);
 }
 
 // Whole-limb fused polymul: c = INTT(NTT(a) * NTT(b)), N <= 2^13.
-template <int LOGE>
-__global__ void __launch_bounds__(512) k_polymul_whole(LimbSet c, ConstLimbSet a, ConstLimbSet b,
-                                                       uint32_t log_n, uint32_t T,
-                                                       const DevMod* __restrict__ mods) {
+template <class C>
+__global__ void __launch_bounds__(C::THREADS) k_polymul_whole(LimbSet c, ConstLimbSet a, ConstLimbSet b,
+                                                              const DevMod* __restrict__ mods) {
   extern __shared__ __align__(16) uint64_t smem[];
+  constexpr int K = C::K, NR = C::NR;
+  constexpr uint32_t log_n = K;
   uint64_t* sa = smem;
-  uint64_t* sb = smem + padded_words(1u << T);
+  uint64_t* sb = smem + tile_smem_words(1u << C::T);
   const uint32_t tid = threadIdx.x;
-  const uint32_t K = log_n, N = 1u << K, words = 1u << T;
-  const uint32_t limb0 = blockIdx.x << (T - K);
-  for (uint32_t v = tid * 2; v < words; v += blockDim.x * 2) {
-    const uint32_t limb = limb0 + (v >> K);
-    if (limb < c.count) {
-      const ulonglong2 da = ld_pair(a.limb(limb, log_n) + (v & (N - 1)));
-      const ulonglong2 db = ld_pair(b.limb(limb, log_n) + (v & (N - 1)));
-      sa[sidx(v)] = da.x;
-      sa[sidx(v + 1)] = da.y;
-      sb[sidx(v)] = db.x;
-      sb[sidx(v + 1)] = db.y;
-    }
-  }
-  __syncthreads();
-  const uint32_t my_limb = limb0 + (tid >> (K - LOGE));
+  const uint32_t limb0 = blockIdx.x << (C::T - K);
+  const uint32_t my_limb = limb0 + C::sub(tid);
   const bool active = my_limb < c.count;
   const DevMod m = load_mod(mods, c.cm(active ? my_limb : 0));
-  const RoundPlan fp = make_plan(K, LOGE, false);
-  for (uint32_t r = 0; r + 1 < fp.n; ++r) {
-    uint32_t R, beta;
-    fp.geom(r, R, beta);
-    fwd_round<LOGE>(sa, tid, 0, K, R, beta, 0, 0, m.fwd, m.p, active);
-    fwd_round<LOGE>(sb, tid, 0, K, R, beta, 0, 0, m.fwd, m.p, active);
+  const uint32_t umask = (1u << K) - 1u;
+  constexpr int E = 1 << C::LOGE;
+  uint64_t xa[E], xb[E];
+  if constexpr (NR == 1) {
+    stage_in_limbs<C>(sa, a, limb0, c.count, log_n);
+    stage_in_limbs<C>(sb, b, limb0, c.count, log_n);
     __syncthreads();
-  }
-  fused_product_round<LOGE>(sa, sb, tid, K, log_n, 0, 0, m, active, fp.n == 1);
-  __syncthreads();
-  const RoundPlan ip = make_plan(K, LOGE, true);
-  for (uint32_t r = 1; r < ip.n; ++r) {
-    uint32_t R, beta;
-    ip.geom(r, R, beta);
-    inv_round<LOGE>(sa, tid, 0, K, R, beta, log_n, 0, 0, m, active, r + 1 == ip.n);
+    using RB = Round<C, 0>;
+    const uint32_t bb = RB::base(tid);
+    if (active) {
+      smem_load<RB>(xa, sa, bb);
+      smem_load<RB>(xb, sb, bb);
+      fused_product<C, true>(xa, xb, bb, log_n, 0, 0, m);
+      smem_store<RB>(xa, sa, bb);
+    }
     __syncthreads();
-  }
-  for (uint32_t v = tid * 2; v < words; v += blockDim.x * 2) {
-    const uint32_t limb = limb0 + (v >> K);
-    if (limb < c.count) st_pair(c.limb(limb, log_n) + (v & (N - 1)), sa[sidx(v)], sa[sidx(v + 1)]);
+    stage_out_limbs<C>(sa, c, limb0, log_n, mods, false);
+  } else {
+    using R0 = Round<C, 0>;
+    const uint32_t b0 = R0::base(tid);
+    if (active) {
+      gload_rows<R0>(xa, a.limb(my_limb, log_n), b0 & umask);
+      gload_rows<R0>(xb, b.limb(my_limb, log_n), b0 & umask);
+      ct_stages2<R0::R, R0::E, 0>(xa, xb, m.fwd, R0::HI, R0::gr(b0, 0), 0 - m.p, m.p << 1);
+      smem_store<R0>(xa, sa, b0);
+      smem_store<R0>(xb, sb, b0);
+    }
+    __syncthreads();
+    fwd_rounds<C, 1, NR - 1>(sa, tid, 0, 0, m.fwd, m.p, active);
+    fwd_rounds<C, 1, NR - 1>(sb, tid, 0, 0, m.fwd, m.p, active);
+    using RB = Round<C, NR - 1>;
+    const uint32_t bb = RB::base(tid);
+    if (active) {
+      smem_load<RB>(xa, sa, bb);
+      smem_load<RB>(xb, sb, bb);
+      fused_product<C, false>(xa, xb, bb, log_n, 0, 0, m);
+      smem_store<RB>(xa, sa, bb);
+    }
+    __syncthreads();
+    inv_rounds<C, NR - 2, 0, true>(sa, tid, log_n, 0, 0, m, active);
+    if (active) {
+      smem_load<R0>(xa, sa, b0);
+      gs_round<R0, true>(xa, log_n, R0::BETA, R0::gr(b0, 0), m);
+      gstore_rows<R0>(xa, c.limb(my_limb, log_n), b0 & umask);
+    }
   }
 }
 
 // Two-pass fused row step: ca holds a's column-pass output and receives the
 // row-pass output of the product; sbuf holds b's column-pass output.
-__global__ void __launch_bounds__(256, 2) k_polymul_rows(LimbSet ca, ConstLimbSet sbuf,
-                                                         uint32_t log_n, uint32_t k1,
-                                                         const DevMod* __restrict__ mods) {
+template <class C, int K1>
+__global__ void __launch_bounds__(C::THREADS, 2) k_polymul_rows(LimbSet ca, ConstLimbSet sbuf,
+                                                                const DevMod* __restrict__ mods) {
   extern __shared__ __align__(16) uint64_t smem[];
+  constexpr int K = C::K, NR = C::NR;
+  constexpr uint32_t log_n = K + K1;
+  constexpr int TPL = log_n - kTileLog;
   uint64_t* sa = smem;
-  uint64_t* sb = smem + padded_words(1u << kTwoPassTileLog);
+  uint64_t* sb = smem + tile_smem_words(1u << kTileLog);
   const uint32_t tid = threadIdx.x;
-  const uint32_t logB = log_n - k1;
-  const uint32_t tpl_log = log_n - kTwoPassTileLog;
-  const uint32_t limb = blockIdx.x >> tpl_log;
-  const uint32_t off = (blockIdx.x & ((1u << tpl_log) - 1u)) << kTwoPassTileLog;
+  const uint32_t limb = blockIdx.x >> TPL;
+  const uint32_t off = (blockIdx.x & ((1u << TPL) - 1u)) << kTileLog;
   uint64_t* pa = ca.limb(limb, log_n) + off;
   const uint64_t* pb = sbuf.limb(limb, log_n) + off;
-  for (uint32_t v = tid * 2; v < (1u << kTwoPassTileLog); v += kTwoPassThreads * 2) {
-    const ulonglong2 da = ld_pair(pa + v);
-    const ulonglong2 db = ld_pair(pb + v);
-    sa[sidx(v)] = da.x;
-    sa[sidx(v + 1)] = da.y;
-    sb[sidx(v)] = db.x;
-    sb[sidx(v + 1)] = db.y;
-  }
-  __syncthreads();
   const DevMod m = load_mod(mods, ca.cm(limb));
-  const uint32_t G = (off >> logB) + (tid >> (logB - 4));
-  const RoundPlan fp = make_plan(logB, 4, false);
-  for (uint32_t r = 0; r + 1 < fp.n; ++r) {
-    uint32_t R, beta;
-    fp.geom(r, R, beta);
-    fwd_round<4>(sa, tid, 0, logB, R, beta, k1, G, m.fwd, m.p, true);
-    fwd_round<4>(sb, tid, 0, logB, R, beta, k1, G, m.fwd, m.p, true);
-    __syncthreads();
-  }
-  fused_product_round<4>(sa, sb, tid, logB, log_n, k1, G, m, true, false);
+  const uint32_t G = (off >> K) + C::sub(tid);
+  constexpr int E = 1 << C::LOGE;
+  uint64_t xa[E], xb[E];
+  using R0 = Round<C, 0>;
+  const uint32_t b0 = R0::base(tid);
+  gload_rows<R0>(xa, pa, b0);
+  gload_rows<R0>(xb, pb, b0);
+  ct_stages2<R0::R, R0::E, 0>(xa, xb, m.fwd, K1 + R0::HI, R0::gr(b0, G), 0 - m.p, m.p << 1);
+  smem_store<R0>(xa, sa, b0);
+  smem_store<R0>(xb, sb, b0);
   __syncthreads();
-  const RoundPlan ip = make_plan(logB, 4, true);
-  for (uint32_t r = 1; r < ip.n; ++r) {
-    uint32_t R, beta;
-    ip.geom(r, R, beta);
-    inv_round<4>(sa, tid, 0, logB, R, beta, log_n, 0, G, m, true, false);
-    __syncthreads();
-  }
-  for (uint32_t v = tid * 2; v < (1u << kTwoPassTileLog); v += kTwoPassThreads * 2)
-    st_pair(pa + v, sa[sidx(v)], sa[sidx(v + 1)]);
+  fwd_rounds<C, 1, NR - 1>(sa, tid, K1, G, m.fwd, m.p, true);
+  fwd_rounds<C, 1, NR - 1>(sb, tid, K1, G, m.fwd, m.p, true);
+  using RB = Round<C, NR - 1>;
+  const uint32_t bb = RB::base(tid);
+  smem_load<RB>(xa, sa, bb);
+  smem_load<RB>(xb, sb, bb);
+  fused_product<C, false>(xa, xb, bb, log_n, K1, G, m);
+  smem_store<RB>(xa, sa, bb);
+  __syncthreads();
+  inv_rounds<C, NR - 2, 0, false>(sa, tid, log_n, 0, G, m, true);
+  smem_load<R0>(xa, sa, b0);
+  gs_round<R0, false>(xa, log_n, R0::BETA, R0::gr(b0, G), m);
+  gstore_rows<R0>(xa, pa, b0);
 }
 
-// ---------------------------------------------------------------------------
+// ===========================================================================
 // Element-wise ops, two words per thread with 128-bit accesses.
-// ---------------------------------------------------------------------------
+// ===========================================================================
 template <int OP>
 __global__ void __launch_bounds__(256) k_elementwise(LimbSet dst, ConstLimbSet a, ConstLimbSet b,
                                                      uint32_t log_n, const DevMod* __restrict__ mods) {
@@ -318,6 +494,9 @@ __global__ void __launch_bounds__(256) k_elementwise(LimbSet dst, ConstLimbSet a
   }
 }
 
+// ===========================================================================
+// Host-side dispatch.
+// ===========================================================================
 int g_num_sms = 0;
 
 int num_sms() {
@@ -335,129 +514,206 @@ cudaError_t set_smem(KernelT kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-inline uint32_t whole_tile_log(uint32_t log_n) { return log_n > 12 ? log_n : 12u; }
-inline int whole_loge(uint32_t log_n) { return log_n >= 4 ? 4 : 3; }
+// Whole-limb tile: 2^max(log_n, 12) words; 16 words per thread (8 at N = 8).
+template <int LOGN>
+using WholeCfg = TileCfg<(LOGN > 12 ? LOGN : 12), LOGN, 0, (LOGN >= 4 ? 4 : 3)>;
 
-ConstLimbSet as_const(const LimbSet& l) {
-  ConstLimbSet c;
-  c.base = l.base;
-  c.ptrs = l.ptrs;
-  c.cms = l.cms;
-  c.count = l.count;
-  c.L = l.L;
-  c.cm0 = l.cm0;
-  c.pad_ = 0;
-  return c;
+// Two-pass split: k1 column stages, log_n - k1 row stages.
+constexpr int k1_of(int log_n) { return log_n <= 15 ? 7 : 8; }
+template <int LOGN>
+using ColCfg = TileCfg<kTileLog, k1_of(LOGN), kTileLog - k1_of(LOGN), 4>;
+template <int LOGN>
+using RowCfg = TileCfg<kTileLog, LOGN - k1_of(LOGN), 0, 4>;
+
+template <int LOGN>
+size_t whole_smem_bytes() {
+  return tile_smem_words(1u << WholeCfg<LOGN>::T) * sizeof(uint64_t);
 }
+constexpr size_t kTileSmemBytes = tile_smem_words(1u << kTileLog) * sizeof(uint64_t);
 
-}  // namespace
-
-uint32_t default_k1(uint32_t log_n) {
-  uint32_t k1 = log_n / 2;
-  return k1 > 8 ? 8u : k1;
-}
-
-static uint32_t pick_k1(uint32_t log_n, const NttShape& shape) {
-  uint32_t k1 = shape.k1 ? shape.k1 : default_k1(log_n);
-  // column tiles need >= 2 columns (lb >= 1) and rows must fit a 4096-word tile
-  if (k1 > kTwoPassTileLog - 1) k1 = kTwoPassTileLog - 1;
-  if (log_n - k1 > kTwoPassTileLog) k1 = log_n - kTwoPassTileLog;
-  if (log_n - k1 < 4) k1 = log_n - 4;
-  return k1;
-}
-
-static bool use_whole(uint32_t log_n, const NttShape& shape) {
-  return log_n <= shape.single_cta_max_log_n && log_n <= 13;
-}
-
-cudaError_t launch_ntt(const LimbSet& ls, uint32_t log_n, const DevMod* mods, NttDir dir,
-                       const NttShape& shape, cudaStream_t st) {
-  if (ls.count == 0) return cudaSuccess;
-  if (use_whole(log_n, shape)) {
-    const uint32_t T = whole_tile_log(log_n);
-    const uint32_t grid = (ls.count + (1u << (T - log_n)) - 1) >> (T - log_n);
-    const size_t smem = padded_words(1u << T) * sizeof(uint64_t);
-    if (whole_loge(log_n) == 4) {
-      k_ntt_whole<4><<<grid, 1u << (T - 4), smem, st>>>(ls, log_n, T, mods, (int)dir);
-    } else {
-      k_ntt_whole<3><<<grid, 1u << (T - 3), smem, st>>>(ls, log_n, T, mods, (int)dir);
-    }
-    g_kernel_launches += 1;
-    return cudaGetLastError();
+template <int LOGN>
+cudaError_t launch_whole_ntt(const LimbSet& ls, const DevMod* mods, NttDir dir, cudaStream_t st) {
+  using C = WholeCfg<LOGN>;
+  const uint32_t per = 1u << (C::T - LOGN);
+  const uint32_t grid = (ls.count + per - 1) / per;
+  const size_t smem = whole_smem_bytes<LOGN>();
+  LaunchScope ps(dir == NttDir::kBackward ? "ntt_whole_inv" : "ntt_whole_fwd", st);
+  switch (dir) {
+    case NttDir::kForward: k_ntt_whole<C, 0><<<grid, C::THREADS, smem, st>>>(ls, mods); break;
+    case NttDir::kForwardLazy: k_ntt_whole<C, 1><<<grid, C::THREADS, smem, st>>>(ls, mods); break;
+    case NttDir::kBackward: k_ntt_whole<C, 2><<<grid, C::THREADS, smem, st>>>(ls, mods); break;
   }
-  const uint32_t k1 = pick_k1(log_n, shape);
-  const size_t smem = padded_words(1u << kTwoPassTileLog) * sizeof(uint64_t);
-  const uint32_t tiles = ls.count << (log_n - kTwoPassTileLog);
+  g_kernel_launches += 1;
+  return cudaGetLastError();
+}
+
+template <int LOGN>
+cudaError_t launch_two_pass_ntt(const LimbSet& ls, const DevMod* mods, NttDir dir, cudaStream_t st) {
+  constexpr int K1 = k1_of(LOGN), LOGB = LOGN - K1;
+  using CC = ColCfg<LOGN>;
+  using RC = RowCfg<LOGN>;
+  const uint32_t tiles = ls.count << (LOGN - kTileLog);
   const ConstLimbSet cls = as_const(ls);
   if (dir == NttDir::kBackward) {
-    k_row_pass<true><<<tiles, kTwoPassThreads, smem, st>>>(ls, log_n, k1, mods, 0);
-    k_col_pass<true><<<tiles, kTwoPassThreads, smem, st>>>(cls, ls, log_n, k1, mods);
+    {
+      LaunchScope ps("row_pass_inv", st);
+      k_row_pass<RC, K1, true><<<tiles, RC::THREADS, kTileSmemBytes, st>>>(ls, mods, 0);
+    }
+    LaunchScope ps("col_pass_inv", st);
+    k_col_pass<CC, LOGB, true><<<tiles, CC::THREADS, kTileSmemBytes, st>>>(cls, ls, mods);
   } else {
-    k_col_pass<false><<<tiles, kTwoPassThreads, smem, st>>>(cls, ls, log_n, k1, mods);
-    k_row_pass<false><<<tiles, kTwoPassThreads, smem, st>>>(ls, log_n, k1, mods,
-                                                            dir == NttDir::kForward ? 1 : 0);
+    {
+      LaunchScope ps("col_pass_fwd", st);
+      k_col_pass<CC, LOGB, false><<<tiles, CC::THREADS, kTileSmemBytes, st>>>(cls, ls, mods);
+    }
+    LaunchScope ps("row_pass_fwd", st);
+    k_row_pass<RC, K1, false><<<tiles, RC::THREADS, kTileSmemBytes, st>>>(
+        ls, mods, dir == NttDir::kForward ? 1 : 0);
   }
   g_kernel_launches += 2;
   return cudaGetLastError();
 }
 
-cudaError_t init_kernel_attributes() {
-  const size_t whole = padded_words(1u << 13) * sizeof(uint64_t);
-  const size_t tile = padded_words(1u << kTwoPassTileLog) * sizeof(uint64_t);
+template <int LOGN>
+cudaError_t launch_whole_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
+                                 const DevMod* mods, cudaStream_t st) {
+  using C = WholeCfg<LOGN>;
+  const uint32_t per = 1u << (C::T - LOGN);
+  const uint32_t grid = (c.count + per - 1) / per;
+  LaunchScope ps("polymul_whole", st);
+  k_polymul_whole<C><<<grid, C::THREADS, 2 * whole_smem_bytes<LOGN>(), st>>>(c, a, b, mods);
+  g_kernel_launches += 1;
+  return cudaGetLastError();
+}
+
+template <int LOGN>
+cudaError_t launch_two_pass_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
+                                    const DevMod* mods, uint64_t* scratch, cudaStream_t st) {
+  constexpr int K1 = k1_of(LOGN), LOGB = LOGN - K1;
+  using CC = ColCfg<LOGN>;
+  using RC = RowCfg<LOGN>;
+  const uint32_t tiles = c.count << (LOGN - kTileLog);
+  LimbSet sl = c;
+  sl.base = scratch;
+  sl.ptrs = nullptr;
+  {
+    LaunchScope ps("polymul_col_fwd_a", st);
+    k_col_pass<CC, LOGB, false><<<tiles, CC::THREADS, kTileSmemBytes, st>>>(a, c, mods);
+  }
+  {
+    LaunchScope ps("polymul_col_fwd_b", st);
+    k_col_pass<CC, LOGB, false><<<tiles, CC::THREADS, kTileSmemBytes, st>>>(b, sl, mods);
+  }
+  {
+    LaunchScope ps("polymul_rows", st);
+    k_polymul_rows<RC, K1><<<tiles, RC::THREADS, 2 * kTileSmemBytes, st>>>(c, as_const(sl), mods);
+  }
+  {
+    LaunchScope ps("polymul_col_inv", st);
+    k_col_pass<CC, LOGB, true><<<tiles, CC::THREADS, kTileSmemBytes, st>>>(as_const(c), c, mods);
+  }
+  g_kernel_launches += 4;
+  return cudaGetLastError();
+}
+
+template <int LOGN>
+cudaError_t set_attrs_for() {
   cudaError_t e;
-  if ((e = set_smem(k_ntt_whole<4>, whole)) != cudaSuccess) return e;
-  if ((e = set_smem(k_ntt_whole<3>, whole)) != cudaSuccess) return e;
-  if ((e = set_smem(k_polymul_whole<4>, 2 * whole)) != cudaSuccess) return e;
-  if ((e = set_smem(k_polymul_whole<3>, 2 * whole)) != cudaSuccess) return e;
-  if ((e = set_smem(k_polymul_rows, 2 * tile)) != cudaSuccess) return e;
-  if ((e = set_smem(k_col_pass<false>, tile)) != cudaSuccess) return e;
-  if ((e = set_smem(k_col_pass<true>, tile)) != cudaSuccess) return e;
-  if ((e = set_smem(k_row_pass<false>, tile)) != cudaSuccess) return e;
-  if ((e = set_smem(k_row_pass<true>, tile)) != cudaSuccess) return e;
+  if constexpr (LOGN <= 13) {
+    using C = WholeCfg<LOGN>;
+    const size_t s = whole_smem_bytes<LOGN>();
+    if ((e = set_smem(k_ntt_whole<C, 0>, s)) != cudaSuccess) return e;
+    if ((e = set_smem(k_ntt_whole<C, 1>, s)) != cudaSuccess) return e;
+    if ((e = set_smem(k_ntt_whole<C, 2>, s)) != cudaSuccess) return e;
+    if ((e = set_smem(k_polymul_whole<C>, 2 * s)) != cudaSuccess) return e;
+  } else {
+    constexpr int K1 = k1_of(LOGN), LOGB = LOGN - K1;
+    using CC = ColCfg<LOGN>;
+    using RC = RowCfg<LOGN>;
+    if ((e = set_smem(k_col_pass<CC, LOGB, false>, kTileSmemBytes)) != cudaSuccess) return e;
+    if ((e = set_smem(k_col_pass<CC, LOGB, true>, kTileSmemBytes)) != cudaSuccess) return e;
+    if ((e = set_smem(k_row_pass<RC, K1, false>, kTileSmemBytes)) != cudaSuccess) return e;
+    if ((e = set_smem(k_row_pass<RC, K1, true>, kTileSmemBytes)) != cudaSuccess) return e;
+    if ((e = set_smem(k_polymul_rows<RC, K1>, 2 * kTileSmemBytes)) != cudaSuccess) return e;
+  }
   return cudaSuccess;
 }
 
-uint32_t ntt_launch_count(uint32_t log_n, const NttShape& shape) {
-  return use_whole(log_n, shape) ? 1u : 2u;
+template <int... LOGNS>
+cudaError_t set_all_attrs(std::integer_sequence<int, LOGNS...>) {
+  cudaError_t e = cudaSuccess;
+  ((e = (e == cudaSuccess ? set_attrs_for<LOGNS>() : e)), ...);
+  return e;
 }
 
-uint32_t polymul_launch_count(uint32_t log_n, const NttShape& shape) {
-  return use_whole(log_n, shape) ? 1u : 4u;
+template <int LOGN>
+cudaError_t ntt_dispatch(const LimbSet& ls, const DevMod* mods, NttDir dir, cudaStream_t st) {
+  if constexpr (LOGN <= 13)
+    return launch_whole_ntt<LOGN>(ls, mods, dir, st);
+  else
+    return launch_two_pass_ntt<LOGN>(ls, mods, dir, st);
 }
 
-size_t polymul_scratch_words(uint32_t count, uint32_t log_n, const NttShape& shape) {
-  return use_whole(log_n, shape) ? 0 : ((size_t)count << log_n);
+template <int LOGN>
+cudaError_t polymul_dispatch(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
+                             const DevMod* mods, uint64_t* scratch, cudaStream_t st) {
+  if constexpr (LOGN <= 13)
+    return launch_whole_polymul<LOGN>(c, a, b, mods, st);
+  else
+    return launch_two_pass_polymul<LOGN>(c, a, b, mods, scratch, st);
+}
+
+}  // namespace
+
+uint32_t default_k1(uint32_t log_n) { return (uint32_t)k1_of((int)log_n); }
+
+cudaError_t init_kernel_attributes() {
+  return set_all_attrs(std::integer_sequence<int, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17>{});
+}
+
+uint32_t ntt_launch_count(uint32_t log_n, const NttShape&) { return log_n <= 13 ? 1u : 2u; }
+uint32_t polymul_launch_count(uint32_t log_n, const NttShape&) { return log_n <= 13 ? 1u : 4u; }
+
+size_t polymul_scratch_words(uint32_t count, uint32_t log_n, const NttShape&) {
+  return log_n <= 13 ? 0 : ((size_t)count << log_n);
+}
+
+#define YELL_DEGREE_SWITCH(LOGN, CALL) \
+  switch (LOGN) {                      \
+    case 3: return CALL(3);            \
+    case 4: return CALL(4);            \
+    case 5: return CALL(5);            \
+    case 6: return CALL(6);            \
+    case 7: return CALL(7);            \
+    case 8: return CALL(8);            \
+    case 9: return CALL(9);            \
+    case 10: return CALL(10);          \
+    case 11: return CALL(11);          \
+    case 12: return CALL(12);          \
+    case 13: return CALL(13);          \
+    case 14: return CALL(14);          \
+    case 15: return CALL(15);          \
+    case 16: return CALL(16);          \
+    case 17: return CALL(17);          \
+    default: return cudaErrorInvalidValue; \
+  }
+
+cudaError_t launch_ntt(const LimbSet& ls, uint32_t log_n, const DevMod* mods, NttDir dir,
+                       const NttShape&, cudaStream_t st) {
+  if (ls.count == 0) return cudaSuccess;
+#define YELL_NTT_CALL(L) ntt_dispatch<L>(ls, mods, dir, st)
+  YELL_DEGREE_SWITCH(log_n, YELL_NTT_CALL)
+#undef YELL_NTT_CALL
 }
 
 cudaError_t launch_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
                            uint32_t log_n, const DevMod* mods, uint64_t* scratch,
-                           const NttShape& shape, cudaStream_t st) {
+                           const NttShape&, cudaStream_t st) {
   if (c.count == 0) return cudaSuccess;
-  if (use_whole(log_n, shape)) {
-    const uint32_t T = whole_tile_log(log_n);
-    const uint32_t grid = (c.count + (1u << (T - log_n)) - 1) >> (T - log_n);
-    const size_t smem = 2 * padded_words(1u << T) * sizeof(uint64_t);
-    if (whole_loge(log_n) == 4) {
-      k_polymul_whole<4><<<grid, 1u << (T - 4), smem, st>>>(c, a, b, log_n, T, mods);
-    } else {
-      k_polymul_whole<3><<<grid, 1u << (T - 3), smem, st>>>(c, a, b, log_n, T, mods);
-    }
-    g_kernel_launches += 1;
-    return cudaGetLastError();
-  }
-  if (scratch == nullptr) return cudaErrorInvalidValue;
-  const uint32_t k1 = pick_k1(log_n, shape);
-  const size_t smem = padded_words(1u << kTwoPassTileLog) * sizeof(uint64_t);
-  const uint32_t tiles = c.count << (log_n - kTwoPassTileLog);
-  LimbSet sl = c;
-  sl.base = scratch;
-  sl.ptrs = nullptr;
-  k_col_pass<false><<<tiles, kTwoPassThreads, smem, st>>>(a, c, log_n, k1, mods);
-  k_col_pass<false><<<tiles, kTwoPassThreads, smem, st>>>(b, sl, log_n, k1, mods);
-  k_polymul_rows<<<tiles, kTwoPassThreads, 2 * smem, st>>>(c, as_const(sl), log_n, k1, mods);
-  k_col_pass<true><<<tiles, kTwoPassThreads, smem, st>>>(as_const(c), c, log_n, k1, mods);
-  g_kernel_launches += 4;
-  return cudaGetLastError();
+  if (log_n > 13 && scratch == nullptr) return cudaErrorInvalidValue;
+#define YELL_PM_CALL(L) polymul_dispatch<L>(c, a, b, mods, scratch, st)
+  YELL_DEGREE_SWITCH(log_n, YELL_PM_CALL)
+#undef YELL_PM_CALL
 }
 
 cudaError_t launch_elementwise(EwOp op, const LimbSet& dst, const ConstLimbSet& a,
@@ -468,6 +724,7 @@ cudaError_t launch_elementwise(EwOp op, const LimbSet& dst, const ConstLimbSet& 
   const size_t want = (pairs + 255) / 256;
   const size_t cap = (size_t)num_sms() * 8;
   const uint32_t grid = (uint32_t)(want < cap ? want : cap);
+  LaunchScope ps("elementwise", st);
   switch (op) {
     case EwOp::kMulmod: k_elementwise<0><<<grid, 256, 0, st>>>(dst, a, b, log_n, mods); break;
     case EwOp::kAddmod: k_elementwise<1><<<grid, 256, 0, st>>>(dst, a, b, log_n, mods); break;

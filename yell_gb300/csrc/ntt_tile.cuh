@@ -1,160 +1,206 @@
-// Tile engine shared by every NTT kernel.
+// Tile engine shared by every NTT kernel (all geometry known at compile time).
 //
-// A CTA holds a tile of 2^T uint64 words in shared memory.  The transform
-// acts on the bit range [lb, lb + K) of the tile index v ("u" bits); the other
-// bits select independent sub-transforms (columns below lb, blocks or limbs
-// above lb + K).  Each thread owns E = 2^LOGE words per round and applies R
-// consecutive radix-2 stages to them in registers; rounds exchange through
-// shared memory.  The butterflies, their order within a dependency chain and
-// their twiddle indices are exactly the reference's (lib/ntt.cpp:89-210), so
-// the lazy words produced are identical to the reference's, not only
-// congruent: a radix-2 butterfly is a pure function of its two inputs and its
-// twiddle, and every butterfly here sees the same inputs as its reference
-// counterpart.
+// A CTA owns a tile of 2^T uint64 words.  The transform acts on the bit range
+// [LB, LB + K) of the tile index v (the "u" bits); the other bits select
+// independent sub-transforms (columns below LB; blocks or limbs above
+// LB + K).  Each thread owns 2^LOGE words per round and applies R consecutive
+// radix-2 stages to them in registers; rounds exchange through shared memory.
+// The butterflies, their pairing and their twiddle indices are exactly the
+// reference's (lib/ntt.cpp:89-210), so the lazy words produced are identical
+// to the reference's, not only congruent: a radix-2 butterfly is a pure
+// function of its two inputs and its twiddle, and every butterfly here sees
+// the same inputs as its reference counterpart.
 //
-// Twiddle indices.  Forward stage s (m = 2^s groups, half-size h = N/2^(s+1))
+// Rounds.  A K-stage transform is split into NR = ceil(K / LOGE) rounds.  The
+// round on the lowest u bits always has LOGE stages, so every other round has
+// beta >= LOGE and takes its LOGE - R extra in-register bits from the lowest
+// u bits.  Forward (CT) rounds run from the top bits down, inverse (GS)
+// rounds from the bottom up.  Round geometry is indexed by its position I
+// counted from the top bits.
+//
+// Twiddle indices.  Forward stage s (m = 2^s groups, half-size N/2^(s+1))
 // uses w[m + (i >> (log_n - s))] for the pair at global index i
-// (lib/ntt.cpp:105-110).  Inverse stage sigma (h = 2^sigma,
+// (lib/ntt.cpp:105-110); inverse stage sigma (pair distance 2^sigma,
 // m = N/2^(sigma+1)) uses w[m + (i >> (sigma + 1))] (lib/ntt.cpp:193-198).
 // Inside a round both reduce to a per-thread group number gr plus the top
-// bits of the in-register index j, worked out in ct_round/gs_round below.
+// bits of the in-register index j.
+//
+// Shared memory layout: word v lives at v + 2*(v >> 4) (two pad words per
+// 16), which keeps 16-byte alignment for adjacent pairs and spreads the
+// strided accesses of the low-bit rounds across banks.
 #pragma once
 #include "common.cuh"
 
 namespace yell_gb300 {
 
-// One pad word after every 16 words: rows of 16 words shift by two banks,
-// which keeps the strided per-thread access of the low-bit rounds at the
-// two-wavefront minimum for 8-byte accesses.
-constexpr uint32_t kPadShift = 4;
-__device__ __forceinline__ uint32_t sidx(uint32_t v) { return v + (v >> kPadShift); }
-__host__ __device__ constexpr uint32_t padded_words(uint32_t n) { return n + (n >> kPadShift); }
+__host__ __device__ constexpr uint32_t sidx(uint32_t v) { return v + ((v >> 4) << 1); }
+__host__ __device__ constexpr uint32_t tile_smem_words(uint32_t n) { return n + (n >> 3); }
 
-// Round split of a K-stage transform into rounds of at most LOGE stages.  The
-// round on the lowest u bits always has LOGE stages, so every other round has
-// beta >= LOGE and can take its (LOGE - R) extra in-register bits from the
-// lowest u bits.  Forward rounds run from the top bits down (CT, stage 0 has
-// the largest distance); inverse rounds run from the bottom up (GS).
-struct RoundPlan {
-  uint32_t n;     // number of rounds
-  uint32_t q;     // base width of the rounds above the bottom one
-  uint32_t rem;   // the first `rem` of those are one stage wider
-  uint32_t K;
-  uint32_t loge;
-  bool inverse;
+template <int T_, int K_, int LB_, int LOGE_>
+struct TileCfg {
+  static constexpr int T = T_, K = K_, LB = LB_, LOGE = LOGE_;
+  static constexpr int THREADS = 1 << (T - LOGE);
+  static constexpr int NR = (K + LOGE - 1) / LOGE;
+  static constexpr int Q = NR > 1 ? (K - LOGE) / (NR - 1) : K;
+  static constexpr int REM = NR > 1 ? (K - LOGE) % (NR - 1) : 0;
+  __host__ __device__ static constexpr int width(int i) { return (i + 1 == NR) ? (NR == 1 ? K : LOGE) : Q + (i < REM ? 1 : 0); }
+  __host__ __device__ static constexpr int beta(int i) {
+    return (i + 1 == NR) ? 0 : K - (i + 1) * Q - ((i + 1) < REM ? (i + 1) : REM);
+  }
+  // Tile bits above LB + K (sub-transform index) of thread tid.
+  __device__ static __forceinline__ uint32_t sub(uint32_t tid) { return tid >> (LB + K - LOGE); }
+  static_assert(K >= LOGE, "transform narrower than a thread's word set");
+  static_assert(T >= K + LB, "tile smaller than one sub-transform");
+};
 
-  // Width R and lowest butterfly bit beta of round r in execution order.
-  __device__ __forceinline__ void geom(uint32_t r, uint32_t& R, uint32_t& beta) const {
-    const uint32_t i = inverse ? n - 1 - r : r;   // index counted from the top bits
-    if (i + 1 == n) {
-      R = (n == 1) ? K : loge;
-      beta = 0;
-    } else {
-      R = q + (i < rem ? 1u : 0u);
-      beta = K - (i + 1) * q - ((i + 1) < rem ? (i + 1) : rem);
-    }
+// Geometry of round I of tile C.
+template <class C, int I>
+struct Round {
+  static constexpr int R = C::width(I);
+  static constexpr int BETA = C::beta(I);
+  static constexpr int LB = C::LB, LOGE = C::LOGE, K = C::K;
+  static constexpr int EB = LOGE - R;          // extra (non-butterfly) bits per thread
+  static constexpr int E = 1 << EB;
+  static constexpr int MID = BETA - EB;        // u bits between the extra and butterfly bits
+  static constexpr int HI = K - BETA - R;      // u bits above the butterfly bits
+  // Adjacent word pairs (ex = 2m, 2m+1) when the extra bits are the tile's
+  // lowest bits: moved as one 16-byte access.
+  static constexpr bool PAIRS = (LB == 0 && EB >= 1);
+  static_assert(MID >= 0, "round plan broke the extra-bits-below rule");
+
+  // Tile index of the thread's element (ex = 0, j = 0): thread id bits fill
+  // [0, LB), [LB + EB, LB + BETA) and [LB + BETA + R, T) in increasing order.
+  __device__ static __forceinline__ uint32_t base(uint32_t tid) {
+    uint32_t v = tid & ((1u << LB) - 1u);
+    v |= ((tid >> LB) & ((1u << MID) - 1u)) << (LB + EB);
+    v |= (tid >> (LB + MID)) << (LB + BETA + R);
+    return v;
+  }
+  __host__ __device__ static constexpr uint32_t off(int ex, int j) {
+    return ((uint32_t)ex << LB) + ((uint32_t)j << (LB + BETA));
+  }
+  // Group number at the round's first stage: sub-transform group G (at the
+  // transform's top stage) followed by the u bits above the butterfly range.
+  __device__ static __forceinline__ uint32_t gr(uint32_t base_v, uint32_t G) {
+    return (G << HI) + ((base_v >> (LB + BETA + R)) & ((1u << HI) - 1u));
   }
 };
 
-__device__ __forceinline__ RoundPlan make_plan(uint32_t K, uint32_t LOGE, bool inverse) {
-  RoundPlan pl;
-  pl.n = (K + LOGE - 1) / LOGE;
-  pl.K = K;
-  pl.loge = LOGE;
-  pl.inverse = inverse;
-  if (pl.n > 1) {
-    const uint32_t rest = K - LOGE;
-    pl.q = rest / (pl.n - 1);
-    pl.rem = rest % (pl.n - 1);
+// ---- register <-> shared memory ----------------------------------------------
+template <class RG>
+__device__ __forceinline__ void smem_load(uint64_t* x, const uint64_t* s, uint32_t base_v) {
+  constexpr int R = RG::R;
+  const uint64_t* sb = s + sidx(base_v);
+  if constexpr (RG::PAIRS) {
+#pragma unroll
+    for (int m = 0; m < RG::E / 2; ++m)
+#pragma unroll
+      for (int j = 0; j < (1 << R); ++j) {
+        const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(sb + sidx(RG::off(2 * m, j)));
+        x[((2 * m) << R) | j] = v.x;
+        x[((2 * m + 1) << R) | j] = v.y;
+      }
   } else {
-    pl.q = K;
-    pl.rem = 0;
+#pragma unroll
+    for (int ex = 0; ex < RG::E; ++ex)
+#pragma unroll
+      for (int j = 0; j < (1 << R); ++j) x[(ex << R) | j] = sb[sidx(RG::off(ex, j))];
   }
-  return pl;
 }
 
-// Tile index of this thread's element (ex = 0, j = 0) in a round with
-// butterfly bits [beta, beta + R) and extra bits [0, LOGE - R) of u.  The
-// thread id fills the remaining tile bits in increasing order, so consecutive
-// lanes take consecutive columns (bits below lb) first.
-template <int LOGE, int R>
-__device__ __forceinline__ uint32_t thread_base(uint32_t tid, uint32_t lb, uint32_t beta) {
-  constexpr uint32_t e = LOGE - R;
-  const uint32_t mid = beta - e;
-  uint32_t v = tid & ((1u << lb) - 1u);
-  v |= ((tid >> lb) & ((1u << mid) - 1u)) << (lb + e);
-  v |= (tid >> (lb + mid)) << (lb + beta + R);
-  return v;
+template <class RG>
+__device__ __forceinline__ void smem_store(const uint64_t* x, uint64_t* s, uint32_t base_v) {
+  constexpr int R = RG::R;
+  uint64_t* sb = s + sidx(base_v);
+  if constexpr (RG::PAIRS) {
+#pragma unroll
+    for (int m = 0; m < RG::E / 2; ++m)
+#pragma unroll
+      for (int j = 0; j < (1 << R); ++j)
+        *reinterpret_cast<ulonglong2*>(sb + sidx(RG::off(2 * m, j))) =
+            make_ulonglong2(x[((2 * m) << R) | j], x[((2 * m + 1) << R) | j]);
+  } else {
+#pragma unroll
+    for (int ex = 0; ex < RG::E; ++ex)
+#pragma unroll
+      for (int j = 0; j < (1 << R); ++j) sb[sidx(RG::off(ex, j))] = x[(ex << R) | j];
+  }
 }
 
-template <int LOGE, int R>
-__device__ __forceinline__ void load_regs(uint64_t* x, const uint64_t* s, uint32_t base, uint32_t lb,
-                                          uint32_t beta) {
-  constexpr int E = 1 << (LOGE - R);
-#pragma unroll
-  for (int ex = 0; ex < E; ++ex)
-#pragma unroll
-    for (int j = 0; j < (1 << R); ++j)
-      x[(ex << R) | j] = s[sidx(base + ((uint32_t)ex << lb) + ((uint32_t)j << (lb + beta)))];
-}
-
-template <int LOGE, int R>
-__device__ __forceinline__ void store_regs(const uint64_t* x, uint64_t* s, uint32_t base, uint32_t lb,
-                                           uint32_t beta) {
-  constexpr int E = 1 << (LOGE - R);
-#pragma unroll
-  for (int ex = 0; ex < E; ++ex)
-#pragma unroll
-    for (int j = 0; j < (1 << R); ++j)
-      s[sidx(base + ((uint32_t)ex << lb) + ((uint32_t)j << (lb + beta)))] = x[(ex << R) | j];
-}
-
-// Forward (CT) round on registers.  s_first: absolute stage of the round's
-// first sub-stage.  gr: group number of this thread at stage s_first.  At
-// sub-stage k the pair (j, j + 2^(R-1-k)) uses twiddle
-// w[2^(s_first+k) + (gr << k) + (j >> (R-k))].  Sub-stages recurse at compile
-// time so every loop bound and register index is a constant.
-template <int LOGE, int R, int k>
-__device__ __forceinline__ void ct_stage(uint64_t* x, uint32_t s_first, uint32_t gr,
-                                         const ulonglong2* __restrict__ tw, uint64_t p, uint64_t p2) {
+// ---- butterfly stages on registers -------------------------------------------
+// Forward sub-stage k of a round pairs (j, j + 2^(R-1-k)) with twiddle
+// w[2^(s_first+k) + (gr << k) + (j >> (R-k))].  The twiddles of sub-stage
+// k+1 are requested before sub-stage k computes.
+template <int R, int E, int k>
+__device__ __forceinline__ void ct_stages(uint64_t* x, const ulonglong2* __restrict__ tw,
+                                          uint32_t s_first, uint32_t gr, uint64_t np, uint64_t p2,
+                                          const ulonglong2* wk) {
   if constexpr (k < R) {
-    constexpr int E = 1 << (LOGE - R);
     constexpr int d = 1 << (R - 1 - k);
     constexpr int NJ = 1 << k;
-    const uint32_t tbase = (1u << (s_first + k)) + (gr << k);
+    constexpr int NN = (k + 1 < R) ? (2 << k) : 1;
+    ulonglong2 wn[NN];
+    if constexpr (k + 1 < R) {
+      const ulonglong2* src = tw + (1u << (s_first + k + 1)) + (gr << (k + 1));
 #pragma unroll
-    for (int jj = 0; jj < NJ; ++jj) {
-      const ulonglong2 w = __ldg(tw + tbase + jj);
+      for (int jj = 0; jj < NN; ++jj) wn[jj] = __ldg(src + jj);
+    }
+#pragma unroll
+    for (int jj = 0; jj < NJ; ++jj)
 #pragma unroll
       for (int ex = 0; ex < E; ++ex)
 #pragma unroll
         for (int q = 0; q < d; ++q) {
           const int j = jj * 2 * d + q;
-          ct_bfly(x[(ex << R) | j], x[(ex << R) | (j + d)], w.x, w.y, p, p2);
+          ct_bfly(x[(ex << R) | j], x[(ex << R) | (j + d)], wk[jj].x, wk[jj].y, np, p2);
         }
-    }
-    ct_stage<LOGE, R, k + 1>(x, s_first, gr, tw, p, p2);
+    ct_stages<R, E, k + 1>(x, tw, s_first, gr, np, p2, wn);
   }
 }
 
-template <int LOGE, int R>
-__device__ __forceinline__ void ct_round(uint64_t* x, uint32_t s_first, uint32_t gr,
-                                         const ulonglong2* __restrict__ tw, uint64_t p, uint64_t p2) {
-  ct_stage<LOGE, R, 0>(x, s_first, gr, tw, p, p2);
+template <class RG>
+__device__ __forceinline__ void ct_round(uint64_t* x, const ulonglong2* __restrict__ tw,
+                                         uint32_t s_first, uint32_t gr, uint64_t p) {
+  ulonglong2 w0[1];
+  w0[0] = __ldg(tw + (1u << s_first) + gr);
+  ct_stages<RG::R, RG::E, 0>(x, tw, s_first, gr, 0 - p, p << 1, w0);
 }
 
-// Inverse (GS) round on registers.  sigma_first: absolute inverse stage of
-// the first sub-stage (pair distance 2^sigma in the global index).  At
-// sub-stage k the pair (j, j + 2^k) uses twiddle
-// w[2^(log_n-1-sigma) + (gr << (R-1-k)) + (j >> (k+1))].  With LAST, the
-// round's final sub-stage is the reference's last layer with the N^-1
-// scaling fused (include/yell/details/ntt.hpp:220-228) instead of a GS stage.
-template <int LOGE, int R, bool LAST, int k>
-__device__ __forceinline__ void gs_stage(uint64_t* x, uint32_t log_n, uint32_t sigma_first,
-                                         uint32_t gr, const ulonglong2* __restrict__ itw,
-                                         const DevMod& m) {
+// The same round applied to two operands that share twiddles (the two
+// inputs of a polymul at the same limb and position).
+template <int R, int E, int k>
+__device__ __forceinline__ void ct_stages2(uint64_t* x, uint64_t* y, const ulonglong2* __restrict__ tw,
+                                           uint32_t s_first, uint32_t gr, uint64_t np, uint64_t p2) {
   if constexpr (k < R) {
-    constexpr int E = 1 << (LOGE - R);
+    constexpr int d = 1 << (R - 1 - k);
+    constexpr int NJ = 1 << k;
+    const ulonglong2* src = tw + (1u << (s_first + k)) + (gr << k);
+#pragma unroll
+    for (int jj = 0; jj < NJ; ++jj) {
+      const ulonglong2 w = __ldg(src + jj);
+#pragma unroll
+      for (int ex = 0; ex < E; ++ex)
+#pragma unroll
+        for (int q = 0; q < d; ++q) {
+          const int j = jj * 2 * d + q;
+          ct_bfly(x[(ex << R) | j], x[(ex << R) | (j + d)], w.x, w.y, np, p2);
+          ct_bfly(y[(ex << R) | j], y[(ex << R) | (j + d)], w.x, w.y, np, p2);
+        }
+    }
+    ct_stages2<R, E, k + 1>(x, y, tw, s_first, gr, np, p2);
+  }
+}
+
+// Inverse sub-stage k pairs (j, j + 2^k) with twiddle
+// w[2^(log_n-1-sigma_first-k) + (gr << (R-1-k)) + (j >> (k+1))].  With
+// LAST, the round's final sub-stage is the reference's last layer with the
+// N^-1 scaling fused (include/yell/details/ntt.hpp:220-228).
+// top = log_n - 1 - sigma_first, so sub-stage k uses m = 2^(top - k).
+template <int R, int E, bool LAST, int k>
+__device__ __forceinline__ void gs_stages(uint64_t* x, const ulonglong2* __restrict__ itw,
+                                          uint32_t top, uint32_t gr, const DevMod& m,
+                                          const ulonglong2* wk) {
+  if constexpr (k < R) {
     constexpr int d = 1 << k;
     if constexpr (LAST && k == R - 1) {
 #pragma unroll
@@ -163,28 +209,43 @@ __device__ __forceinline__ void gs_stage(uint64_t* x, uint32_t log_n, uint32_t s
         for (int q = 0; q < d; ++q) gs_last(x[(ex << R) | q], x[(ex << R) | (q + d)], m);
     } else {
       constexpr int NJ = 1 << (R - 1 - k);
-      const uint64_t p = m.p, p2 = m.p << 1;
-      const uint32_t tbase = (1u << (log_n - 1 - (sigma_first + k))) + (gr << (R - 1 - k));
+      constexpr bool NEXT = (k + 1 < R) && !(LAST && k + 2 == R);
+      constexpr int NN = NEXT ? (1 << (R - 2 - k)) : 1;
+      ulonglong2 wn[NN];
+      if constexpr (NEXT) {
+        const ulonglong2* src = itw + (1u << (top - k - 1)) + (gr << (R - 2 - k));
 #pragma unroll
-      for (int jj = 0; jj < NJ; ++jj) {
-        const ulonglong2 w = __ldg(itw + tbase + jj);
+        for (int jj = 0; jj < NN; ++jj) wn[jj] = __ldg(src + jj);
+      }
+      const uint64_t np = 0 - m.p, p2 = m.p << 1;
+#pragma unroll
+      for (int jj = 0; jj < NJ; ++jj)
 #pragma unroll
         for (int ex = 0; ex < E; ++ex)
 #pragma unroll
           for (int q = 0; q < d; ++q) {
             const int j = jj * 2 * d + q;
-            gs_bfly(x[(ex << R) | j], x[(ex << R) | (j + d)], w.x, w.y, p, p2);
+            gs_bfly(x[(ex << R) | j], x[(ex << R) | (j + d)], wk[jj].x, wk[jj].y, np, p2);
           }
-      }
-      gs_stage<LOGE, R, LAST, k + 1>(x, log_n, sigma_first, gr, itw, m);
+      gs_stages<R, E, LAST, k + 1>(x, itw, top, gr, m, wn);
     }
   }
 }
 
-template <int LOGE, int R, bool LAST>
-__device__ __forceinline__ void gs_round(uint64_t* x, uint32_t log_n, uint32_t sigma_first, uint32_t gr,
-                                         const ulonglong2* __restrict__ itw, const DevMod& m) {
-  gs_stage<LOGE, R, LAST, 0>(x, log_n, sigma_first, gr, itw, m);
+template <class RG, bool LAST>
+__device__ __forceinline__ void gs_round(uint64_t* x, uint32_t log_n, uint32_t sigma_first,
+                                         uint32_t gr, const DevMod& m) {
+  constexpr int R = RG::R;
+  const uint32_t top = log_n - 1 - sigma_first;
+  constexpr bool ONLY_LAST = LAST && R == 1;
+  constexpr int N0 = ONLY_LAST ? 1 : (1 << (R - 1));
+  ulonglong2 w0[N0];
+  if constexpr (!ONLY_LAST) {
+    const ulonglong2* src = m.inv + (1u << top) + (gr << (R - 1));
+#pragma unroll
+    for (int jj = 0; jj < N0; ++jj) w0[jj] = __ldg(src + jj);
+  }
+  gs_stages<R, RG::E, LAST, 0>(x, m.inv, top, gr, m, w0);
 }
 
 // Reads the DevMod for modulus index cm with read-only loads.
@@ -203,122 +264,58 @@ __device__ __forceinline__ DevMod load_mod(const DevMod* __restrict__ mods, uint
   return m;
 }
 
-// Runs one forward round of the plan on the tile in shared memory.
-//   lb, K     : position and width of the transform bits in the tile index
-//   s_off     : absolute stage of the transform's u-bit K-1 (0 for a whole
-//               NTT or a column pass, k1 for a row pass)
-//   G         : group number of the sub-transform at stage s_off
-//   active    : false for threads whose sub-transform is padding
-template <int LOGE, int R>
-__device__ __forceinline__ void fwd_round_smem(uint64_t* s, uint32_t tid, uint32_t lb, uint32_t K,
-                                               uint32_t beta, uint32_t s_off, uint32_t G,
+// ---- whole rounds through shared memory ---------------------------------------
+// Forward round I: load from s, CT stages, store to s.  s_off: absolute stage
+// of the transform's top u bit; G: the thread's sub-transform group number.
+template <class C, int I>
+__device__ __forceinline__ void fwd_round_smem(uint64_t* s, uint32_t tid, uint32_t s_off, uint32_t G,
                                                const ulonglong2* tw, uint64_t p, bool active) {
-  uint64_t x[1 << LOGE];
-  const uint32_t base = thread_base<LOGE, R>(tid, lb, beta);
+  using RG = Round<C, I>;
+  uint64_t x[1 << C::LOGE];
+  const uint32_t b = RG::base(tid);
   if (active) {
-    load_regs<LOGE, R>(x, s, base, lb, beta);
-    const uint32_t hi_bits = K - beta - R;
-    const uint32_t u_hi = (base >> (lb + beta + R)) & ((1u << hi_bits) - 1u);
-    const uint32_t gr = (G << hi_bits) + u_hi;
-    ct_round<LOGE, R>(x, s_off + hi_bits, gr, tw, p, p << 1);
-    store_regs<LOGE, R>(x, s, base, lb, beta);
+    smem_load<RG>(x, s, b);
+    ct_round<RG>(x, tw, s_off + RG::HI, RG::gr(b, G), p);
+    smem_store<RG>(x, s, b);
   }
 }
 
-// Inverse counterpart.  sig_off: absolute inverse stage of the transform's
-// u-bit 0 (0 for a whole NTT or a row pass, log2(B) for a column pass).
-template <int LOGE, int R, bool LAST>
-__device__ __forceinline__ void inv_round_smem(uint64_t* s, uint32_t tid, uint32_t lb, uint32_t K,
-                                               uint32_t beta, uint32_t log_n, uint32_t sig_off,
-                                               uint32_t G, const DevMod& m, bool active) {
-  uint64_t x[1 << LOGE];
-  const uint32_t base = thread_base<LOGE, R>(tid, lb, beta);
+// Inverse round at top-index I: sig_off is the absolute inverse stage of the
+// transform's u-bit 0.
+template <class C, int I, bool LAST>
+__device__ __forceinline__ void inv_round_smem(uint64_t* s, uint32_t tid, uint32_t log_n,
+                                               uint32_t sig_off, uint32_t G, const DevMod& m,
+                                               bool active) {
+  using RG = Round<C, I>;
+  uint64_t x[1 << C::LOGE];
+  const uint32_t b = RG::base(tid);
   if (active) {
-    load_regs<LOGE, R>(x, s, base, lb, beta);
-    const uint32_t hi_bits = K - beta - R;
-    const uint32_t u_hi = (base >> (lb + beta + R)) & ((1u << hi_bits) - 1u);
-    const uint32_t gr = (G << hi_bits) + u_hi;
-    gs_round<LOGE, R, LAST>(x, log_n, sig_off + beta, gr, m.inv, m);
-    store_regs<LOGE, R>(x, s, base, lb, beta);
+    smem_load<RG>(x, s, b);
+    gs_round<RG, LAST>(x, log_n, sig_off + RG::BETA, RG::gr(b, G), m);
+    smem_store<RG>(x, s, b);
   }
 }
 
-// One forward round of width R (runtime) at bit beta, dispatched to the
-// compile-time round.
-template <int LOGE>
-__device__ __forceinline__ void fwd_round(uint64_t* s, uint32_t tid, uint32_t lb, uint32_t K,
-                                          uint32_t R, uint32_t beta, uint32_t s_off, uint32_t G,
-                                          const ulonglong2* tw, uint64_t p, bool active) {
-  switch (R) {
-#define YELL_FWD_CASE(RR)                                                       \
-  case RR:                                                                      \
-    if constexpr (RR <= LOGE)                                                   \
-      fwd_round_smem<LOGE, RR>(s, tid, lb, K, beta, s_off, G, tw, p, active);   \
-    break;
-    YELL_FWD_CASE(1)
-    YELL_FWD_CASE(2)
-    YELL_FWD_CASE(3)
-    YELL_FWD_CASE(4)
-#undef YELL_FWD_CASE
-    default: break;
-  }
-}
-
-template <int LOGE>
-__device__ __forceinline__ void inv_round(uint64_t* s, uint32_t tid, uint32_t lb, uint32_t K,
-                                          uint32_t R, uint32_t beta, uint32_t log_n,
-                                          uint32_t sig_off, uint32_t G, const DevMod& m,
-                                          bool active, bool last) {
-  switch (R) {
-#define YELL_INV_CASE(RR)                                                                   \
-  case RR:                                                                                  \
-    if constexpr (RR <= LOGE) {                                                             \
-      if (last)                                                                             \
-        inv_round_smem<LOGE, RR, true>(s, tid, lb, K, beta, log_n, sig_off, G, m, active);  \
-      else                                                                                  \
-        inv_round_smem<LOGE, RR, false>(s, tid, lb, K, beta, log_n, sig_off, G, m, active); \
-    }                                                                                       \
-    break;
-    YELL_INV_CASE(1)
-    YELL_INV_CASE(2)
-    YELL_INV_CASE(3)
-    YELL_INV_CASE(4)
-#undef YELL_INV_CASE
-    default: break;
-  }
-}
-
-// All rounds of a forward transform over the tile (syncs between rounds).
-// G is this thread's sub-transform group number at stage s_off; tw, p and
-// active may differ per thread (per limb).  A thread's sub-transform is the
-// same in every round: its tile bits above lb + K are tid >> (lb + K - LOGE).
-template <int LOGE>
-__device__ __forceinline__ void fwd_tile(uint64_t* s, uint32_t tid, uint32_t lb, uint32_t K,
-                                         uint32_t s_off, uint32_t G, const ulonglong2* tw,
-                                         uint64_t p, bool active) {
-  const RoundPlan pl = make_plan(K, LOGE, false);
-  for (uint32_t r = 0; r < pl.n; ++r) {
-    uint32_t R, beta;
-    pl.geom(r, R, beta);
-    fwd_round<LOGE>(s, tid, lb, K, R, beta, s_off, G, tw, p, active);
+// Forward rounds [I, I1) through shared memory, a barrier after each.
+template <class C, int I, int I1>
+__device__ __forceinline__ void fwd_rounds(uint64_t* s, uint32_t tid, uint32_t s_off, uint32_t G,
+                                           const ulonglong2* tw, uint64_t p, bool active) {
+  if constexpr (I < I1) {
+    fwd_round_smem<C, I>(s, tid, s_off, G, tw, p, active);
     __syncthreads();
+    fwd_rounds<C, I + 1, I1>(s, tid, s_off, G, tw, p, active);
   }
 }
 
-// All rounds of an inverse transform over the tile.  With has_last, the
-// final sub-stage is the scaled last layer (only when the tile's transform
-// contains the global top bit).
-template <int LOGE>
-__device__ __forceinline__ void inv_tile(uint64_t* s, uint32_t tid, uint32_t lb, uint32_t K,
-                                         uint32_t log_n, uint32_t sig_off, uint32_t G,
-                                         const DevMod& m, bool active, bool has_last) {
-  const RoundPlan pl = make_plan(K, LOGE, true);
-  for (uint32_t r = 0; r < pl.n; ++r) {
-    uint32_t R, beta;
-    pl.geom(r, R, beta);
-    inv_round<LOGE>(s, tid, lb, K, R, beta, log_n, sig_off, G, m, active,
-                    has_last && (r + 1 == pl.n));
+// Inverse rounds from top-index I down to I1 (exclusive), bottom-up order.
+// The round at top-index 0 carries the scaled last layer when HAS_LAST.
+template <class C, int I, int I1, bool HAS_LAST>
+__device__ __forceinline__ void inv_rounds(uint64_t* s, uint32_t tid, uint32_t log_n, uint32_t sig_off,
+                                           uint32_t G, const DevMod& m, bool active) {
+  if constexpr (I > I1) {
+    inv_round_smem<C, I, HAS_LAST && I == 0>(s, tid, log_n, sig_off, G, m, active);
     __syncthreads();
+    inv_rounds<C, I - 1, I1, HAS_LAST>(s, tid, log_n, sig_off, G, m, active);
   }
 }
 
