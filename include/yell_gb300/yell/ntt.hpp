@@ -1,0 +1,57 @@
+// Drop-in for yell/ntt.hpp (include/yell/ntt.hpp:6-66): yell::ntt<N>'s static
+// calls, each one a GPU call through the yell_gb300 C ABI on host memory.
+// Failures (which the reference only asserts on) throw yell::gpu_error.
+#pragma once
+#include <cstddef>
+#include <stdexcept>
+#include <string>
+#include "yell/params.hpp"
+#include "yell_gb300.h"
+
+namespace yell {
+
+struct gpu_error : std::runtime_error {
+  int status;
+  gpu_error(int st, const char* fn)
+      : std::runtime_error(std::string(fn) + ": " + yell_status_string(st) + " (" + yell_last_error() + ")"),
+        status(st) {}
+};
+
+inline void check_status(int st, const char* fn) {
+  if (st != YELL_OK) throw gpu_error(st, fn);
+}
+
+template <size_t N>
+struct static_log2 {
+  static_assert(N >= 2 && (N & (N - 1)) == 0, "degree must be a power of two");
+  static constexpr uint32_t value = 1 + static_log2<N / 2>::value;
+};
+template <>
+struct static_log2<1> {
+  static constexpr uint32_t value = 0;
+};
+
+template <size_t degree_>
+class ntt {
+  using T = params::value_type;
+  static constexpr uint32_t log_n = static_log2<degree_>::value;
+
+ public:
+  static constexpr size_t degree = degree_;
+  // ntt.hpp:50: builds the table of modulus cm (on the GPU, kept for the process).
+  static void init_table(size_t cm) { check_status(yell_init_table(log_n, (uint32_t)cm), "init_table"); }
+  // ntt.hpp:53-56
+  static void init_ntt_tables(size_t K) {
+    check_status(yell_init_ntt_tables(log_n, (uint32_t)K), "init_ntt_tables");
+  }
+  // ntt.hpp:59: in place, bit-reversed output in [0, p).
+  static void forward(T* op, size_t cm) { check_status(yell_ntt_forward(op, log_n, (uint32_t)cm), "forward"); }
+  // ntt.hpp:62: in place, output in [0, 4p).
+  static void forward_lazy(T* op, size_t cm) {
+    check_status(yell_ntt_forward_lazy(op, log_n, (uint32_t)cm), "forward_lazy");
+  }
+  // ntt.hpp:65: in place, natural-order output in [0, p).
+  static void backward(T* op, size_t cm) { check_status(yell_ntt_backward(op, log_n, (uint32_t)cm), "backward"); }
+};
+
+}  // namespace yell

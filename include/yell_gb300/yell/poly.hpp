@@ -1,0 +1,145 @@
+// Drop-in for yell/poly.hpp (include/yell/poly.hpp:43-171 and
+// include/yell/details/poly.hpp) without the samplers and GMP lifting:
+// yell::poly<N> keeps one host allocation per limb (raw_data() is the same
+// uint64_t** the reference exposes) and every NTT and arithmetic member runs
+// on the GPU through the yell_gb300 C ABI.
+#pragma once
+#include <cassert>
+#include <cstdlib>
+#include <cstring>
+#include <stdexcept>
+#include <utility>
+#include <vector>
+#include "yell/ntt.hpp"
+#include "yell/ops.hpp"
+#include "yell/params.hpp"
+
+namespace yell {
+
+template <size_t degree_>
+class poly {
+  static_assert(degree_ < params::kMaxPolyDegree, "");
+  size_t nmoduli;
+  std::vector<params::value_type*> _data;
+  static constexpr uint32_t log_n = static_log2<degree_>::value;
+
+  static params::value_type* alloc_limb() {
+    void* p = nullptr;
+    if (posix_memalign(&p, 64, degree_ * sizeof(params::value_type)) != 0) throw std::bad_alloc();
+    std::memset(p, 0, degree_ * sizeof(params::value_type));
+    return static_cast<params::value_type*>(p);
+  }
+
+ public:
+  using value_type = params::value_type;
+  using gt_value_type = params::gt_value_type;
+  using signed_type = params::signed_type;
+  using pointer_type = value_type*;
+  using const_pointer_type = value_type const*;
+  using iterator = pointer_type;
+  using const_iterator = const_pointer_type;
+  static constexpr size_t degree = degree_;
+  static constexpr size_t logn = log_n;
+
+  explicit poly(size_t nmoduli_) : nmoduli(nmoduli_) {
+    assert(nmoduli <= params::kMaxNbModuli);
+    for (size_t cm = 0; cm < nmoduli; ++cm) _data.push_back(alloc_limb());
+  }
+  ~poly() {
+    for (auto& p : _data) std::free(p);
+  }
+  poly(poly const& oth) : poly(oth.nmoduli) {
+    for (size_t cm = 0; cm < nmoduli; ++cm) std::memcpy(_data[cm], oth._data[cm], degree_ * sizeof(value_type));
+  }
+  poly(poly&& oth) : nmoduli(0) { swap(*this, oth); }
+  poly& operator=(poly const& oth) {
+    resize_moduli_count(oth.moduli_count());
+    for (size_t cm = 0; cm < nmoduli; ++cm) std::memcpy(_data[cm], oth._data[cm], degree_ * sizeof(value_type));
+    return *this;
+  }
+
+  iterator ptr_at(size_t cm) { return _data.at(cm); }
+  iterator ptr_end(size_t cm) { return ptr_at(cm) + degree; }
+  const_iterator cptr_at(size_t cm) const { return _data.at(cm); }
+  const_iterator cptr_end(size_t cm) const { return cptr_at(cm) + degree; }
+
+  bool operator==(poly const& oth) const {
+    if (nmoduli != oth.nmoduli) return false;
+    for (size_t cm = 0; cm < nmoduli; ++cm)
+      if (std::memcmp(_data[cm], oth._data[cm], degree_ * sizeof(value_type)) != 0) return false;
+    return true;
+  }
+  bool operator!=(poly const& oth) const { return !(*this == oth); }
+
+  // details/poly.hpp:118-132: *this += op0 * op1 (ops::muladd per word).
+  poly& add_product_of(const poly& op0, const poly& op1) {
+    assert(nmoduli == op0.nmoduli && nmoduli == op1.nmoduli);
+    check_status(yell_poly_add_product_of(_data.data(), op0._data.data(), op1._data.data(),
+                                          (uint32_t)nmoduli, log_n),
+                 "add_product_of");
+    return *this;
+  }
+  // details/poly.hpp:151-157
+  void negate() { check_status(yell_poly_negate(_data.data(), (uint32_t)nmoduli, log_n), "negate"); }
+
+  // details/poly.hpp:90-109
+  void resize_moduli_count(size_t new_nmoduli) {
+    assert(new_nmoduli <= params::kMaxNbModuli);
+    while (_data.size() < new_nmoduli) _data.push_back(alloc_limb());
+    while (_data.size() > new_nmoduli) {
+      std::free(_data.back());
+      _data.pop_back();
+    }
+    nmoduli = new_nmoduli;
+  }
+
+  value_type const& operator()(size_t cm, size_t i) const { return _data[cm][i]; }
+  value_type& operator()(size_t cm, size_t i) { return _data[cm][i]; }
+
+  // details/poly.hpp:170-186, one GPU call over all limbs each.
+  void forward() { check_status(yell_poly_forward(_data.data(), (uint32_t)nmoduli, log_n), "forward"); }
+  void forward_lazy() {
+    check_status(yell_poly_forward_lazy(_data.data(), (uint32_t)nmoduli, log_n), "forward_lazy");
+  }
+  void backward() { check_status(yell_poly_backward(_data.data(), (uint32_t)nmoduli, log_n), "backward"); }
+
+  value_type get_modulus(size_t cm) { return params::P[cm]; }
+  params::value_type** raw_data() { return _data.data(); }
+  params::value_type* const* raw_data() const { return _data.data(); }
+  friend void swap(poly& a, poly& b) {
+    std::swap(a._data, b._data);
+    std::swap(a.nmoduli, b.nmoduli);
+  }
+  void clear() {
+    for (size_t cm = 0; cm < nmoduli; ++cm) std::memset(_data[cm], 0, degree_ * sizeof(value_type));
+  }
+  size_t moduli_count() const { return nmoduli; }
+};
+
+namespace detail {
+template <size_t N, int (*FN)(uint64_t* const*, const uint64_t* const*, const uint64_t* const*, uint32_t,
+                              uint32_t)>
+poly<N> binary_op(poly<N> const& a, poly<N> const& b, const char* name) {
+  const size_t L = a.moduli_count() < b.moduli_count() ? a.moduli_count() : b.moduli_count();
+  poly<N> r(L);
+  check_status(FN(r.raw_data(), a.raw_data(), b.raw_data(), (uint32_t)L, poly<N>::logn), name);
+  return r;
+}
+template <size_t N, int (*FN)(uint64_t* const*, const uint64_t* const*, const uint64_t* const*, uint32_t,
+                              uint32_t)>
+poly<N>& self_op(poly<N>& a, poly<N> const& b, const char* name) {
+  const size_t L = a.moduli_count() < b.moduli_count() ? a.moduli_count() : b.moduli_count();
+  check_status(FN(a.raw_data(), a.raw_data(), b.raw_data(), (uint32_t)L, poly<N>::logn), name);
+  return a;
+}
+}  // namespace detail
+
+// include/yell/poly.hpp:163-168 (the YELL_BINARY_OPERATOR loops of ops.hpp:7-41).
+template <size_t N> poly<N> operator*(poly<N> const& a, poly<N> const& b) { return detail::binary_op<N, yell_poly_mulmod>(a, b, "operator*"); }
+template <size_t N> poly<N> operator+(poly<N> const& a, poly<N> const& b) { return detail::binary_op<N, yell_poly_addmod>(a, b, "operator+"); }
+template <size_t N> poly<N> operator-(poly<N> const& a, poly<N> const& b) { return detail::binary_op<N, yell_poly_submod>(a, b, "operator-"); }
+template <size_t N> poly<N>& operator*=(poly<N>& a, poly<N> const& b) { return detail::self_op<N, yell_poly_mulmod>(a, b, "operator*="); }
+template <size_t N> poly<N>& operator+=(poly<N>& a, poly<N> const& b) { return detail::self_op<N, yell_poly_addmod>(a, b, "operator+="); }
+template <size_t N> poly<N>& operator-=(poly<N>& a, poly<N> const& b) { return detail::self_op<N, yell_poly_submod>(a, b, "operator-="); }
+
+}  // namespace yell

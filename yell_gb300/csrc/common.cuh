@@ -42,6 +42,14 @@ struct LimbSet {
   __device__ __forceinline__ uint32_t cm(uint32_t k) const {
     return cms ? cms[k] : cm0 + k % L;
   }
+  // Launch order -> limb index.  Contiguous batches of whole polys are
+  // visited modulus-major (limb l of every poly, then limb l + 1), so the
+  // twiddle table of one prime stays resident in L2 while it is in use.
+  __device__ __forceinline__ uint32_t ordered(uint32_t i) const {
+    if (ptrs || L <= 1 || count % L != 0) return i;
+    const uint32_t polys = count / L;
+    return (i % polys) * L + i / polys;
+  }
 };
 
 struct ConstLimbSet {

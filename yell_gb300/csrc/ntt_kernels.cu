@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(C::THREADS) k_col_pass(ConstLimbSet src, LimbS
   constexpr uint32_t log_n = K + LOGB;
   constexpr int TPL = LOGB - LB;  // log2(tiles per limb)
   const uint32_t tid = threadIdx.x;
-  const uint32_t limb = blockIdx.x >> TPL;
+  const uint32_t limb = dst.ordered(blockIdx.x >> TPL);
   const uint32_t col0 = (blockIdx.x & ((1u << TPL) - 1u)) << LB;
   const uint64_t* in = src.limb(limb, log_n) + col0;
   uint64_t* out = dst.limb(limb, log_n) + col0;
@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(C::THREADS) k_row_pass(LimbSet ls, const DevMo
   constexpr uint32_t log_n = K + K1;
   constexpr int TPL = log_n - kTileLog;
   const uint32_t tid = threadIdx.x;
-  const uint32_t limb = blockIdx.x >> TPL;
+  const uint32_t limb = ls.ordered(blockIdx.x >> TPL);
   const uint32_t off = (blockIdx.x & ((1u << TPL) - 1u)) << kTileLog;
   uint64_t* data = ls.limb(limb, log_n) + off;
   const DevMod m = load_mod(mods, ls.cm(limb));
@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(C::THREADS, 2) k_polymul_rows(LimbSet ca, Cons
   uint64_t* sa = smem;
   uint64_t* sb = smem + tile_smem_words(1u << kTileLog);
   const uint32_t tid = threadIdx.x;
-  const uint32_t limb = blockIdx.x >> TPL;
+  const uint32_t limb = ca.ordered(blockIdx.x >> TPL);
   const uint32_t off = (blockIdx.x & ((1u << TPL) - 1u)) << kTileLog;
   uint64_t* pa = ca.limb(limb, log_n) + off;
   const uint64_t* pb = sbuf.limb(limb, log_n) + off;
