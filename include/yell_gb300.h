@@ -158,6 +158,25 @@ int yell_dev_polymul(uint64_t* d_c, const uint64_t* d_a, const uint64_t* d_b, ui
 /* Waits for all work the library queued on its own stream of this device. */
 int yell_synchronize(void);
 
+/* Fused polymul that allocates nothing (no counterpart in the reference).
+ * For callers that cannot allocate device memory: a process whose HBM is
+ * owned by a fixed budget or a pooled allocator that forbids allocations
+ * outside the pool, or a latency-critical caller that cannot afford
+ * cudaMalloc/cudaFree synchronising the device.  Same arguments and results
+ * as yell_dev_polymul, but the scratch of the two-pass degrees (2^14 and up)
+ * is a fixed 16 MiB device array inside the library (2^21 words: at most
+ * 2^21 / N limbs = pairs * L per call, e.g. 32 limbs at N = 2^16); larger
+ * calls return YELL_ERR_INVALID_ARGUMENT.  The twiddle tables must already be
+ * resident (yell_init_ntt_tables_range), since building them allocates.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  All calls share the one array: calls
+ * whose GPU work overlaps (other streams, other host threads) race on it, so
+ * order them on one stream.  The array needs no clearing: each call writes
+ * the scratch it reads. */
+int yell_dev_polymul_noalloc(uint64_t* d_c, const uint64_t* d_a, const uint64_t* d_b,
+                             uint32_t pairs, uint32_t L, uint32_t log_n, uint32_t cm0,
+                             void* stream);
+
 /* ---- launch profiling (no counterpart in the reference) -----------------
  * Between start and stop every kernel the library launches is bracketed by
  * CUDA events on its stream; stop waits for them and totals the device time

@@ -1,0 +1,67 @@
+"""yell_dev_polymul_noalloc: the fused polymul for callers that cannot
+allocate device memory (HBM owned by a fixed budget or a pooled allocator,
+or a latency-critical path that cannot let cudaMalloc/cudaFree synchronise
+the device).  Its scratch is a fixed 16 MiB array inside the library.
+
+Checked through the C ABI against yell_dev_polymul (the allocating entry
+point with caller scratch) on two calls in a row; results must be identical
+word for word.  This file is collected last so that a run stopping at the
+first failure has already run every other test; it sets up its own state,
+so it also passes alone in a fresh process."""
+import numpy as np
+import pytest
+
+import yell_gb300 as y
+from yell_gb300 import _capi
+from yell_gb300.inputs import uniform_polys
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a).view(np.int64).copy()).cuda()
+
+
+@pytest.mark.parametrize("log_n,pairs,L,cm0", [(16, 1, 32, 0), (14, 4, 8, 3), (12, 3, 5, 1)])
+def test_noalloc_matches_allocating_polymul_twice(cuda, log_n, pairs, L, cm0):
+    torch = cuda
+    lib = y.load()
+    y.init_ntt_tables(log_n, L, cm0)  # building tables allocates: done up front
+    ps = y.primes(L, cm0)
+    for call in range(2):
+        a = uniform_polys(900 + 10 * call + log_n, pairs, L, log_n, ps)
+        b = uniform_polys(950 + 10 * call + log_n, pairs, L, log_n, ps)
+        da, db = _dev(torch, a), _dev(torch, b)
+        want = torch.empty(a.size, dtype=torch.int64, device="cuda")
+        sw = y.polymul_scratch_words(pairs, L, log_n)
+        scratch = torch.empty(max(sw, 2), dtype=torch.int64, device="cuda")
+        y.dev_polymul(want, da, db, pairs, L, log_n, cm0, scratch=scratch if sw else None)
+        got = torch.full((a.size,), -1, dtype=torch.int64, device="cuda")
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
+        st = lib.yell_dev_polymul_noalloc(got.data_ptr(), da.data_ptr(), db.data_ptr(), pairs, L,
+                                          log_n, cm0, None)
+        assert st == _capi.YELL_OK, lib.yell_last_error()
+        assert lib.yell_synchronize() == _capi.YELL_OK
+        if call == 1:
+            # the array already exists; the second call must not take device memory
+            assert torch.cuda.mem_get_info()[0] == free_before
+        assert torch.equal(got, want), f"call {call} differs from yell_dev_polymul"
+
+
+def test_noalloc_rejects_oversize_and_missing_tables(cuda):
+    torch = cuda
+    lib = y.load()
+    log_n = 16
+    y.init_ntt_tables(log_n, 33)
+    n = 33 << log_n  # 33 limbs of 2^16 need 33 * 2^16 > 2^21 scratch words
+    buf = [torch.empty(n, dtype=torch.int64, device="cuda") for _ in range(3)]
+    st = lib.yell_dev_polymul_noalloc(buf[0].data_ptr(), buf[1].data_ptr(), buf[2].data_ptr(), 1, 33,
+                                      log_n, 0, None)
+    assert st == _capi.YELL_ERR_INVALID_ARGUMENT
+    assert b"fixed scratch" in lib.yell_last_error()
+    # tables never built for these moduli at this degree
+    st = lib.yell_dev_polymul_noalloc(buf[0].data_ptr(), buf[1].data_ptr(), buf[2].data_ptr(), 1, 2,
+                                      15, 990, None)
+    assert st == _capi.YELL_ERR_INVALID_ARGUMENT
+    assert b"not resident" in lib.yell_last_error()

@@ -79,6 +79,7 @@ SIGNATURES = {
     "yell_profile_stop": (_int, []),
     "yell_profile_count": (_int, []),
     "yell_profile_get": (_int, [_int, ctypes.c_char_p, _sz, _vp, _vp]),
+    "yell_dev_polymul_noalloc": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),
 }
 
 _lib = None

@@ -184,6 +184,15 @@ const DevMod* DeviceContext::mods_if_ready(uint32_t log_n) const {
   return d_mods_[log_n];
 }
 
+const DevMod* DeviceContext::tables_ready(uint32_t log_n, uint32_t cm0, uint32_t L) const {
+  std::lock_guard<std::mutex> g(tables_mu_);
+  const std::vector<uint8_t>& built = built_[log_n];
+  if (built.empty() || !d_mods_[log_n]) return nullptr;
+  for (uint32_t i = 0; i < L; ++i)
+    if (built[cm0 + i] != 1) return nullptr;
+  return d_mods_[log_n];
+}
+
 int DeviceContext::ensure_tables(uint32_t log_n, uint32_t cm0, uint32_t L, const DevMod** mods) {
   std::vector<uint32_t> cms(L);
   for (uint32_t i = 0; i < L; ++i) cms[i] = cm0 + i;

@@ -67,6 +67,9 @@ class DeviceContext {
   int ensure_tables(uint32_t log_n, uint32_t cm0, uint32_t L, const DevMod** mods);
   int ensure_tables_list(uint32_t log_n, const uint32_t* cms, uint32_t n, const DevMod** mods);
   const DevMod* mods_if_ready(uint32_t log_n) const;
+  // DevMod array of this degree if the tables of moduli cm0 .. cm0+L-1 are
+  // all resident, else nullptr.  Makes no CUDA call and allocates nothing.
+  const DevMod* tables_ready(uint32_t log_n, uint32_t cm0, uint32_t L) const;
 
   // Device buffer of at least `words` words owned by the context; grows on
   // demand.  The caller holds `lock` for as long as it uses the buffer.
