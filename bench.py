@@ -335,6 +335,11 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
     per_call_value = world * per_step / (pc_ms * 1e-3)
     del ta, tb
 
+    # ---- uneven batch (512 polymuls, log2 N in 10..16, L in 1..16) ----------
+    uneven = None
+    if not args.no_uneven:
+        uneven = run_uneven(torch, y, stream, barrier, max_over_ranks, world)
+
     # ---- end to end through the host-memory C ABI call --------------------
     pa = y.PinnedBuffer(a.shape)
     pb = y.PinnedBuffer(b.shape)
@@ -387,12 +392,58 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
                          "path": "one launch per reference call: forward(a), forward(b), "
                                  "mulmod, backward per limb"},
             "batched_vs_per_call": value / per_call_value,
+            "uneven_batch": uneven,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+def run_uneven(torch, y, stream, barrier, max_over_ranks, world):
+    """512 polymuls of mixed degree and limb count (seed 4): one batched call
+    (bucketed, CUDA graph per batch shape) against 512 plain per-call calls."""
+    from yell_gb300.workloads import mix_limb_ntts, mix_operands, uneven_mix
+
+    mix = uneven_mix(4, 512)
+    ops = mix_operands(mix, y.primes(16), 4)
+    items, singles = [], []
+    for (log_n, L), (a, b) in zip(mix, ops):
+        da = torch.from_numpy(a.view(np.int64)).cuda()
+        db = torch.from_numpy(b.view(np.int64)).cuda()
+        dc = torch.empty_like(da)
+        items.append((dc, da, db, log_n, L, 0))
+        sw = y.polymul_scratch_words(1, L, log_n)
+        singles.append(torch.empty(sw, dtype=torch.int64, device="cuda") if sw else None)
+    for log_n in range(10, 17):
+        y.init_ntt_tables(log_n, 16)
+    limb_ntts = mix_limb_ntts(mix)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def batched():
+        y.dev_polymul_batch(items, stream=stream)
+
+    def per_call():
+        for (dc, da, db, log_n, L, cm0), sc in zip(items, singles):
+            y.dev_polymul(dc, da, db, 1, L, log_n, cm0, scratch=sc, stream=stream)
+
+    out = {"workload": "512 polymuls, log2 N uniform in 10..16, L uniform in 1..16 (seed 4)",
+           "limb_ntts": limb_ntts}
+    for name, fn, steps in (("batched", batched, 10), ("per_call", per_call, 3)):
+        for _ in range(2):
+            fn()
+        barrier()
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = max_over_ranks(e0.elapsed_time(e1)) / steps
+        out[name] = {"value": world * limb_ntts / (ms * 1e-3), "unit": UNIT, "ms_per_batch": ms}
+    out["batched_vs_per_call"] = out["batched"]["value"] / out["per_call"]["value"]
+    return out
 
 
 def read_ncu_traffic(kernel: str):
@@ -416,6 +467,7 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch comparison")
     ap.add_argument("--device-only", action="store_true",
                     help="time only the device-resident batch (for profiler captures)")
     ap.add_argument("--pairs", type=int, default=PAIRS,

@@ -155,6 +155,25 @@ size_t yell_polymul_scratch_words(uint32_t pairs, uint32_t L, uint32_t log_n);
 int yell_dev_polymul(uint64_t* d_c, const uint64_t* d_a, const uint64_t* d_b, uint32_t pairs,
                      uint32_t L, uint32_t log_n, uint32_t cm0, uint64_t* d_scratch,
                      size_t scratch_words, void* stream);
+/* ---- batched polymul of uneven sizes (no counterpart in the reference) ----
+ * Each entry is one polymul c = a * b of its own degree and limb count: a, b,
+ * c are (L, N) device arrays, limb l using prime cm0 + l.  Entries are
+ * bucketed by degree; each bucket runs as one launch sequence over all its
+ * limbs, buckets run concurrently, and the whole batch is a CUDA graph cached
+ * per batch shape (the sequence of (degree, total limbs) buckets), so a batch
+ * of a shape seen before costs one list upload and one graph launch.  Outputs
+ * of different entries must not overlap.  Asynchronous on `stream`. */
+typedef struct yell_polymul_desc {
+  uint64_t* c;
+  const uint64_t* a;
+  const uint64_t* b;
+  uint32_t log_n;
+  uint32_t L;
+  uint32_t cm0;
+  uint32_t reserved;
+} yell_polymul_desc;
+int yell_dev_polymul_batch(const yell_polymul_desc* descs, uint32_t n, void* stream);
+
 /* Waits for all work the library queued on its own stream of this device. */
 int yell_synchronize(void);
 

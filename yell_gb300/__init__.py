@@ -240,6 +240,14 @@ def dev_polymul(c, a, b, pairs: int, L: int, log_n: int, cm0: int = 0, scratch=N
          _stream(stream))
 
 
+def dev_polymul_batch(items, stream=None) -> None:
+    """Uneven batch: items are (c, a, b, log_n, L, cm0) with (L, N) CUDA tensors."""
+    descs = (_capi.PolymulDesc * len(items))()
+    for i, (c, a, b, log_n, L, cm0) in enumerate(items):
+        descs[i] = _capi.PolymulDesc(_dptr(c), _dptr(a), _dptr(b), log_n, L, cm0, 0)
+    call("yell_dev_polymul_batch", ctypes.addressof(descs), len(items), _stream(stream))
+
+
 def synchronize() -> None:
     call("yell_synchronize")
 

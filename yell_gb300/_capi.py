@@ -29,6 +29,13 @@ YELL_FORWARD, YELL_FORWARD_LAZY, YELL_BACKWARD = 0, 1, 2
 YELL_OP_MULMOD, YELL_OP_ADDMOD, YELL_OP_SUBMOD, YELL_OP_MULADD, YELL_OP_NEGATE = 0, 1, 2, 3, 4
 
 
+class PolymulDesc(ctypes.Structure):
+    """struct yell_polymul_desc"""
+    _fields_ = [("c", ctypes.c_void_p), ("a", ctypes.c_void_p), ("b", ctypes.c_void_p),
+                ("log_n", ctypes.c_uint32), ("L", ctypes.c_uint32), ("cm0", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
 class YellError(RuntimeError):
     def __init__(self, status: int, fn: str, detail: str):
         self.status = status
@@ -80,6 +87,7 @@ SIGNATURES = {
     "yell_profile_count": (_int, []),
     "yell_profile_get": (_int, [_int, ctypes.c_char_p, _sz, _vp, _vp]),
     "yell_dev_polymul_noalloc": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),
+    "yell_dev_polymul_batch": (_int, [_vp, _u32, _vp]),
 }
 
 _lib = None

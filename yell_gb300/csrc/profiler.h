@@ -32,7 +32,9 @@ int profile_get(int i, std::string* name, uint64_t* launches, double* total_ms);
 class LaunchScope {
  public:
   LaunchScope(const char* name, cudaStream_t st) : name_(name), st_(st) {
-    if (g_profiling.load(std::memory_order_relaxed)) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (g_profiling.load(std::memory_order_relaxed) &&
+        cudaStreamIsCapturing(st_, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
       start_ = profile_event();
       stop_ = profile_event();
       if (start_ && stop_) cudaEventRecord(start_, st_);
