@@ -336,9 +336,13 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
     del ta, tb
 
     # ---- uneven batch (512 polymuls, log2 N in 10..16, L in 1..16) ----------
-    uneven = None
+    uneven = serving = None
     if not args.no_uneven:
         uneven = run_uneven(torch, y, stream, barrier, max_over_ranks, world)
+        if not args.no_serve:
+            serving = run_serving(torch, y, uneven, args.serve_seconds)
+        uneven.pop("_items")
+        uneven.pop("_mix")
 
     # ---- end to end through the host-memory C ABI call --------------------
     pa = y.PinnedBuffer(a.shape)
@@ -393,6 +397,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
                                  "mulmod, backward per limb"},
             "batched_vs_per_call": value / per_call_value,
             "uneven_batch": uneven,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -443,6 +448,39 @@ def run_uneven(torch, y, stream, barrier, max_over_ranks, world):
         ms = max_over_ranks(e0.elapsed_time(e1)) / steps
         out[name] = {"value": world * limb_ntts / (ms * 1e-3), "unit": UNIT, "ms_per_batch": ms}
     out["batched_vs_per_call"] = out["batched"]["value"] / out["per_call"]["value"]
+    out["_items"] = items
+    out["_mix"] = mix
+    return out
+
+
+def run_serving(torch, y, uneven, duration_s: float):
+    """Poisson arrivals of polymul requests drawn from the uneven mix, offered
+    at 10%..120% of the measured batched peak, against the continuous-batching
+    server (120 GiB HBM budget) and against a per-call server (one request per
+    launch sequence); device-resident operands."""
+    from yell_gb300.serve import Server
+
+    items, mix = uneven["_items"], uneven["_mix"]
+    templates = [(da, db, log_n, L, cm0) for (dc, da, db, log_n, L, cm0) in items]
+    peak_rps = len(mix) / (uneven["batched"]["ms_per_batch"] * 1e-3)
+    loads = (0.1, 0.4, 0.8, 1.0, 1.2)
+    out = {"workload": "Poisson arrivals from the uneven mix (seed 5), device-resident operands",
+           "batched_peak_rps": peak_rps, "duration_s_per_point": duration_s}
+    for name, max_batch, dur in (("continuous_batching", 1024, duration_s),
+                                 ("per_call", 1, min(duration_s, 0.25))):
+        points = []
+        with Server(hbm_budget_bytes=0, max_inflight=4, max_batch=max_batch) as srv:
+            srv.load_test(templates, 0.1 * peak_rps, 0.05, seed=1)  # warm-up
+            for f in loads:
+                st = srv.load_test(templates, f * peak_rps, dur, seed=5)
+                points.append({"load": f, "offered_rps": f * peak_rps,
+                               "achieved_rps": st["requests_per_s"],
+                               "limb_ntts_per_s": st["limb_ntts_per_s"], "p50_us": st["p50_us"],
+                               "p99_us": st["p99_us"], "max_us": st["max_us"],
+                               "requests": st["completed"], "batches": st["batches"]})
+            out["hbm_budget_bytes"] = st["hbm_budget"]
+        out[name] = points
+    out["p99_us_at_80pct"] = [p["p99_us"] for p in out["continuous_batching"] if p["load"] == 0.8][0]
     return out
 
 
@@ -468,6 +506,8 @@ def main() -> int:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch comparison")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving sweep")
+    ap.add_argument("--serve-seconds", type=float, default=0.5, help="seconds per serving load point")
     ap.add_argument("--device-only", action="store_true",
                     help="time only the device-resident batch (for profiler captures)")
     ap.add_argument("--pairs", type=int, default=PAIRS,

@@ -174,6 +174,64 @@ typedef struct yell_polymul_desc {
 } yell_polymul_desc;
 int yell_dev_polymul_batch(const yell_polymul_desc* descs, uint32_t n, void* stream);
 
+/* ---- serving loop (no counterpart in the reference) ------------------------
+ * Continuous batching of polymul requests of mixed size.  A scheduler thread
+ * owns max_inflight stream slots; whenever one is free it admits queued
+ * requests in arrival order while an HBM budget (a device arena allocated at
+ * create time) can hold their buffers, and launches everything admitted as
+ * one batch, so requests arriving while other batches run overlap with them
+ * on the device.  Host-memory requests are copied in and out by the server;
+ * YELL_REQ_DEVICE requests use caller-owned device buffers (only scratch, and
+ * the output with YELL_REQ_DISCARD_OUTPUT, come from the budget). */
+typedef struct yell_server yell_server;
+typedef struct yell_server_config {
+  uint64_t hbm_budget_bytes;       /* arena size; 0 = 120 GiB capped by free memory */
+  uint32_t max_inflight;           /* concurrent batches (stream slots); 0 = 4 */
+  uint32_t max_batch;              /* requests per batch; 0 = 1024; 1 = per-call serving */
+  uint32_t inject_alloc_failures;  /* test hook: refuse this many admissions (OOM) */
+  uint32_t reserved;
+} yell_server_config;
+enum yell_request_flags {
+  YELL_REQ_HOST = 0,           /* a, b, c are host arrays of L*N words */
+  YELL_REQ_DEVICE = 1,         /* a, b, c are device arrays (16-byte aligned) */
+  YELL_REQ_DISCARD_OUTPUT = 2  /* compute into a server buffer and drop it (load tests) */
+};
+typedef struct yell_polymul_request {
+  const uint64_t* a;
+  const uint64_t* b;
+  uint64_t* c;
+  uint32_t log_n;
+  uint32_t L;
+  uint32_t cm0;
+  uint32_t flags;
+} yell_polymul_request;
+typedef struct yell_request_result {
+  int status;
+  double queue_us;    /* submit -> admitted */
+  double latency_us;  /* submit -> completion observed */
+} yell_request_result;
+typedef struct yell_server_stats {
+  uint64_t submitted, completed, rejected, cancelled, failed, batches, queued;
+  uint64_t hbm_budget, hbm_in_use, hbm_peak;
+  double p50_us, p99_us, mean_us, max_us;
+  double limb_ntts, limb_ntts_per_s, requests_per_s, window_s;
+} yell_server_stats;
+int yell_server_create(const yell_server_config* cfg, yell_server** out);
+int yell_server_destroy(yell_server* s);
+/* Validates and queues; YELL_ERR_BUDGET if the request can never fit. */
+int yell_server_submit(yell_server* s, const yell_polymul_request* r, uint64_t* id);
+/* Bounded wait: YELL_ERR_TIMEOUT after timeout_s; the request's own status otherwise. */
+int yell_server_wait(yell_server* s, uint64_t id, double timeout_s, yell_request_result* out);
+/* Cancels a request that has not been admitted yet. */
+int yell_server_cancel(yell_server* s, uint64_t id);
+/* Holds (1) or releases (0) admission; queued requests stay queued. */
+int yell_server_pause(yell_server* s, int paused);
+int yell_server_get_stats(yell_server* s, int reset, yell_server_stats* out);
+/* Poisson arrivals at offered_rps for duration_s drawn round-robin from the
+ * templates (outputs discarded), then a bounded drain; fills `out`. */
+int yell_server_load_test(yell_server* s, const yell_polymul_request* templates, uint32_t n,
+                          double offered_rps, double duration_s, uint64_t seed, yell_server_stats* out);
+
 /* Waits for all work the library queued on its own stream of this device. */
 int yell_synchronize(void);
 

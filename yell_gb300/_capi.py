@@ -88,6 +88,14 @@ SIGNATURES = {
     "yell_profile_get": (_int, [_int, ctypes.c_char_p, _sz, _vp, _vp]),
     "yell_dev_polymul_noalloc": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),
     "yell_dev_polymul_batch": (_int, [_vp, _u32, _vp]),
+    "yell_server_create": (_int, [_vp, _vp]),
+    "yell_server_destroy": (_int, [_vp]),
+    "yell_server_submit": (_int, [_vp, _vp, _vp]),
+    "yell_server_wait": (_int, [_vp, _u64, ctypes.c_double, _vp]),
+    "yell_server_cancel": (_int, [_vp, _u64]),
+    "yell_server_pause": (_int, [_vp, _int]),
+    "yell_server_get_stats": (_int, [_vp, _int, _vp]),
+    "yell_server_load_test": (_int, [_vp, _vp, _u32, ctypes.c_double, ctypes.c_double, _u64, _vp]),
 }
 
 _lib = None

@@ -31,10 +31,12 @@ cudaError_t launch_ntt(const LimbSet& ls, uint32_t log_n, const DevMod* mods, Nt
                        const NttShape& shape, cudaStream_t st);
 
 // c = INTT(NTT(a) * NTT(b)) per limb.  scratch: one operand's worth of words
-// (count << log_n) when log_n takes the two-pass path, else unused.
+// (count << log_n) when log_n takes the two-pass path, else unused; or, when
+// scratch_ptrs is given, a device list of one N-word scratch limb per limb.
 cudaError_t launch_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
                            uint32_t log_n, const DevMod* mods, uint64_t* scratch,
-                           const NttShape& shape, cudaStream_t st);
+                           const NttShape& shape, cudaStream_t st,
+                           uint64_t* const* scratch_ptrs = nullptr);
 
 // Element-wise op over `count` limbs of N words:
 //   mulmod/addmod/submod: dst = op(a, b);  muladd: dst = barrett(a*b + dst);

@@ -588,14 +588,15 @@ cudaError_t launch_whole_polymul(const LimbSet& c, const ConstLimbSet& a, const 
 
 template <int LOGN>
 cudaError_t launch_two_pass_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
-                                    const DevMod* mods, uint64_t* scratch, cudaStream_t st) {
+                                    const DevMod* mods, uint64_t* scratch, cudaStream_t st,
+                                    uint64_t* const* scratch_ptrs) {
   constexpr int K1 = k1_of(LOGN), LOGB = LOGN - K1;
   using CC = ColCfg<LOGN>;
   using RC = RowCfg<LOGN>;
   const uint32_t tiles = c.count << (LOGN - kTileLog);
   LimbSet sl = c;
-  sl.base = scratch;
-  sl.ptrs = nullptr;
+  sl.base = scratch_ptrs ? nullptr : scratch;
+  sl.ptrs = scratch_ptrs;
   {
     LaunchScope ps("polymul_col_fwd_a", st);
     k_col_pass<CC, LOGB, false><<<tiles, CC::THREADS, kTileSmemBytes, st>>>(a, c, mods);
@@ -656,11 +657,12 @@ cudaError_t ntt_dispatch(const LimbSet& ls, const DevMod* mods, NttDir dir, cuda
 
 template <int LOGN>
 cudaError_t polymul_dispatch(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
-                             const DevMod* mods, uint64_t* scratch, cudaStream_t st) {
+                             const DevMod* mods, uint64_t* scratch, cudaStream_t st,
+                             uint64_t* const* scratch_ptrs) {
   if constexpr (LOGN <= 13)
     return launch_whole_polymul<LOGN>(c, a, b, mods, st);
   else
-    return launch_two_pass_polymul<LOGN>(c, a, b, mods, scratch, st);
+    return launch_two_pass_polymul<LOGN>(c, a, b, mods, scratch, st, scratch_ptrs);
 }
 
 }  // namespace
@@ -708,10 +710,10 @@ cudaError_t launch_ntt(const LimbSet& ls, uint32_t log_n, const DevMod* mods, Nt
 
 cudaError_t launch_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
                            uint32_t log_n, const DevMod* mods, uint64_t* scratch,
-                           const NttShape&, cudaStream_t st) {
+                           const NttShape&, cudaStream_t st, uint64_t* const* scratch_ptrs) {
   if (c.count == 0) return cudaSuccess;
-  if (log_n > 13 && scratch == nullptr) return cudaErrorInvalidValue;
-#define YELL_PM_CALL(L) polymul_dispatch<L>(c, a, b, mods, scratch, st)
+  if (log_n > 13 && scratch == nullptr && scratch_ptrs == nullptr) return cudaErrorInvalidValue;
+#define YELL_PM_CALL(L) polymul_dispatch<L>(c, a, b, mods, scratch, st, scratch_ptrs)
   YELL_DEGREE_SWITCH(log_n, YELL_PM_CALL)
 #undef YELL_PM_CALL
 }
