@@ -44,8 +44,7 @@ WORKLOAD = f"fused polymul N=2^{LOG_N}, L={L} (P[0..{L - 1}]), {PAIRS} pairs"
 # Algorithmic bytes of one launch of each pipeline kernel per limb (pair):
 # reads + writes of the words it must move (twiddles excluded).
 ALGO_BYTES_PER_LIMB = {
-    "polymul_col_fwd_a": 16 * N,   # read a, write NTT-pass-1(a)
-    "polymul_col_fwd_b": 16 * N,   # read b, write NTT-pass-1(b)
+    "polymul_col_fwd": 32 * N,     # read a and b, write their NTT pass-1 outputs
     "polymul_rows": 24 * N,        # read both pass-1 outputs, write pass-1 of the INTT
     "polymul_col_inv": 16 * N,     # read, write the product
     "polymul_whole": 24 * N,
@@ -246,6 +245,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
     scratch = torch.empty(y.polymul_scratch_words(pairs, L, LOG_N), dtype=torch.int64,
                           device="cuda")
     y.init_ntt_tables(LOG_N, L)
+    # autotune the launch variant of this degree at this size (same words for every variant)
+    tuned_variant, _ = y.autotune(LOG_N, L, pairs)
     stream = torch.cuda.Stream()
 
     def step():
@@ -301,6 +302,22 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
                 "pipeline": {"algorithmic_bytes_per_step": 24 * N * L * pairs,
                              "achieved": 24 * N * L * pairs / (ms_per_step * 1e-3) / 1e9,
                              "frac": 24 * N * L * pairs / (ms_per_step * 1e-3) / 1e9 / hbm}}
+    # ---- integer roofline: butterflies against the calibrated ceiling -----
+    ct_rate, gs_rate = y.calibrate_butterflies()
+    ceiling = (2 * ct_rate + gs_rate) / 3  # two forward NTTs per inverse
+    bfly_step = 3 * L * pairs * (N // 2) * LOG_N
+    rows_bfly = 3 * L * pairs * (N // 2) * (LOG_N - 8)  # forward rows of a and b, inverse rows
+    integer_roofline = {
+        "bound": "imad (64-bit modmul from 32-bit IMAD)",
+        "ceiling_ct_bfly_per_s": ct_rate, "ceiling_gs_bfly_per_s": gs_rate,
+        "pipeline_bfly_per_s": bfly_step / (ms_per_step * 1e-3),
+        "pipeline_frac": bfly_step / (ms_per_step * 1e-3) / ceiling,
+        "rows_kernel_bfly_per_s": rows_bfly / (kernels["polymul_rows"][1] / kernels["polymul_rows"][0] * 1e-3)
+        if "polymul_rows" in kernels else None,
+        "note": "ceiling = register-only CT/GS butterflies on every SM (yell_calibrate_butterflies)"}
+    if integer_roofline["rows_kernel_bfly_per_s"]:
+        integer_roofline["rows_kernel_frac"] = integer_roofline["rows_kernel_bfly_per_s"] / ceiling
+    roofline["integer"] = integer_roofline
     if args.device_only:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT,
@@ -388,6 +405,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
             "data": "synthetic: splitmix64 seed 3 (+1000 per rank), B discrete Gaussian sigma 3.2",
             "config": {"workload": WORKLOAD, "log_n": LOG_N, "L": L, "pairs": PAIRS,
                        "parallelism": f"replicas x{world}",
+                       "launch_variant": y.variants(LOG_N)[tuned_variant],
                        "l2": "inputs larger than L2 (768 MiB operands+result per step)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches,
@@ -423,6 +441,7 @@ def run_uneven(torch, y, stream, barrier, max_over_ranks, world):
         singles.append(torch.empty(sw, dtype=torch.int64, device="cuda") if sw else None)
     for log_n in range(10, 17):
         y.init_ntt_tables(log_n, 16)
+        y.autotune(log_n, 8, 4)
     limb_ntts = mix_limb_ntts(mix)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)

@@ -232,6 +232,26 @@ int yell_server_get_stats(yell_server* s, int reset, yell_server_stats* out);
 int yell_server_load_test(yell_server* s, const yell_polymul_request* templates, uint32_t n,
                           double offered_rps, double duration_s, uint64_t seed, yell_server_stats* out);
 
+/* ---- launch variants and the autotuner (no counterpart in the reference) --
+ * Every degree has one or more launch variants that apply exactly the same
+ * butterflies (same output words) with a different split of the work: limbs
+ * per CTA for whole-limb degrees, column/row split k1 for 2^14 and up.
+ * yell_autotune times the fused polymul of every variant of log_n on
+ * synthetic data of the given size on the current device and selects the
+ * fastest; with YELL_GB300_TUNE_FILE set the choice is saved there and
+ * reloaded when the library first uses the device. */
+int yell_variant_count(uint32_t log_n, uint32_t* count);
+int yell_variant_name(uint32_t log_n, uint32_t variant, char* buf, size_t len);
+int yell_set_variant(uint32_t log_n, uint32_t variant);
+int yell_get_variant(uint32_t log_n, uint32_t* variant);
+int yell_autotune(uint32_t log_n, uint32_t L, uint32_t pairs, uint32_t* best, double* best_ms);
+
+/* Integer roofline (no counterpart in the reference): runs the production CT
+ * and GS butterflies on register-resident words with no memory traffic on
+ * every SM of the current device and returns butterflies per second, the
+ * ceiling the 64-bit modular arithmetic allows at the current clock. */
+int yell_calibrate_butterflies(double* ct_per_s, double* gs_per_s);
+
 /* Waits for all work the library queued on its own stream of this device. */
 int yell_synchronize(void);
 

@@ -248,6 +248,42 @@ def dev_polymul_batch(items, stream=None) -> None:
     call("yell_dev_polymul_batch", ctypes.addressof(descs), len(items), _stream(stream))
 
 
+def variants(log_n: int) -> list[str]:
+    """Names of the launch variants of a degree (index = variant number)."""
+    n = ctypes.c_uint32()
+    call("yell_variant_count", log_n, ctypes.addressof(n))
+    out = []
+    for v in range(n.value):
+        buf = ctypes.create_string_buffer(128)
+        call("yell_variant_name", log_n, v, buf, 128)
+        out.append(buf.value.decode())
+    return out
+
+
+def set_variant(log_n: int, v: int) -> None:
+    call("yell_set_variant", log_n, v)
+
+
+def get_variant(log_n: int) -> int:
+    v = ctypes.c_uint32()
+    call("yell_get_variant", log_n, ctypes.addressof(v))
+    return v.value
+
+
+def autotune(log_n: int, L: int, pairs: int) -> tuple[int, float]:
+    """Times every variant of the fused polymul at this size; selects the fastest."""
+    best, ms = ctypes.c_uint32(), ctypes.c_double()
+    call("yell_autotune", log_n, L, pairs, ctypes.addressof(best), ctypes.addressof(ms))
+    return best.value, ms.value
+
+
+def calibrate_butterflies() -> tuple[float, float]:
+    """Register-only butterfly rate of this GPU: (CT per s, GS per s)."""
+    ct, gs = ctypes.c_double(), ctypes.c_double()
+    call("yell_calibrate_butterflies", ctypes.addressof(ct), ctypes.addressof(gs))
+    return ct.value, gs.value
+
+
 def synchronize() -> None:
     call("yell_synchronize")
 

@@ -88,6 +88,12 @@ SIGNATURES = {
     "yell_profile_get": (_int, [_int, ctypes.c_char_p, _sz, _vp, _vp]),
     "yell_dev_polymul_noalloc": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),
     "yell_dev_polymul_batch": (_int, [_vp, _u32, _vp]),
+    "yell_calibrate_butterflies": (_int, [_vp, _vp]),
+    "yell_variant_count": (_int, [_u32, _vp]),
+    "yell_variant_name": (_int, [_u32, _u32, ctypes.c_char_p, _sz]),
+    "yell_set_variant": (_int, [_u32, _u32]),
+    "yell_get_variant": (_int, [_u32, _vp]),
+    "yell_autotune": (_int, [_u32, _u32, _u32, _vp, _vp]),
     "yell_server_create": (_int, [_vp, _vp]),
     "yell_server_destroy": (_int, [_vp]),
     "yell_server_submit": (_int, [_vp, _vp, _vp]),

@@ -1,4 +1,4 @@
-// NTT, fused polymul and element-wise kernels for sm_103a.
+// NTT and fused polymul kernels for sm_103a (templates; see ntt_variants.h).
 //
 // Paths (per degree N = 2^log_n):
 //   * whole-limb: N <= 2^13.  One CTA holds whole limbs in shared memory
@@ -19,14 +19,19 @@
 // cover contiguous words (the top round of a row tile, every round of a
 // column tile); the other ends are staged through shared memory so that the
 // HBM accesses stay coalesced.
+#pragma once
 #include <utility>
 
 #include "kernels.h"
 #include "ntt_tile.cuh"
 #include "profiler.h"
+#include "ntt_variants.h"
+#include <cstdio>
 
 namespace yell_gb300 {
 
+// Everything below has internal linkage: each translation unit that includes
+// this header instantiates the kernels of its own degrees and variants.
 namespace {
 
 constexpr int kTileLog = 12;  // 4096 words per two-pass tile
@@ -406,6 +411,49 @@ __global__ void __launch_bounds__(C::THREADS) k_polymul_whole(LimbSet c, ConstLi
   }
 }
 
+// Forward column pass of both polymul operands in one CTA: each thread
+// applies the same butterflies to a's and b's words at the same positions,
+// so every twiddle load serves two butterflies.  a -> ca, b -> cb.
+template <class C, int LOGB>
+__global__ void __launch_bounds__(C::THREADS, 2) k_col_pass2(ConstLimbSet a, ConstLimbSet b, LimbSet ca,
+                                                             LimbSet cb, const DevMod* __restrict__ mods) {
+  extern __shared__ __align__(16) uint64_t smem[];
+  constexpr int K = C::K, LB = C::LB, NR = C::NR;
+  constexpr uint32_t log_n = K + LOGB;
+  constexpr int TPL = LOGB - LB;
+  uint64_t* sa = smem;
+  uint64_t* sb = smem + tile_smem_words(1u << kTileLog);
+  const uint32_t tid = threadIdx.x;
+  const uint32_t limb = ca.ordered(blockIdx.x >> TPL);
+  const uint32_t col0 = (blockIdx.x & ((1u << TPL) - 1u)) << LB;
+  const DevMod m = load_mod(mods, ca.cm(limb));
+  const uint64_t np = 0 - m.p, p2 = m.p << 1;
+  constexpr int E = 1 << C::LOGE;
+  uint64_t xa[E], xb[E];
+  using R0 = Round<C, 0>;
+  const uint32_t b0 = R0::base(tid);
+  gload_cols<R0, LOGB>(xa, a.limb(limb, log_n) + col0, b0);
+  gload_cols<R0, LOGB>(xb, b.limb(limb, log_n) + col0, b0);
+  ct_stages2<R0::R, R0::E, 0>(xa, xb, m.fwd, R0::HI, R0::gr(b0, 0), np, p2);
+  if constexpr (NR == 1) {
+    gstore_cols<R0, LOGB>(xa, ca.limb(limb, log_n) + col0, b0);
+    gstore_cols<R0, LOGB>(xb, cb.limb(limb, log_n) + col0, b0);
+  } else {
+    smem_store<R0>(xa, sa, b0);
+    smem_store<R0>(xb, sb, b0);
+    __syncthreads();
+    fwd_rounds<C, 1, NR - 1>(sa, tid, 0, 0, m.fwd, m.p, true);
+    fwd_rounds<C, 1, NR - 1>(sb, tid, 0, 0, m.fwd, m.p, true);
+    using RL = Round<C, NR - 1>;
+    const uint32_t bl = RL::base(tid);
+    smem_load<RL>(xa, sa, bl);
+    smem_load<RL>(xb, sb, bl);
+    ct_stages2<RL::R, RL::E, 0>(xa, xb, m.fwd, RL::HI, RL::gr(bl, 0), np, p2);
+    gstore_cols<RL, LOGB>(xa, ca.limb(limb, log_n) + col0, bl);
+    gstore_cols<RL, LOGB>(xb, cb.limb(limb, log_n) + col0, bl);
+  }
+}
+
 // Two-pass fused row step: ca holds a's column-pass output and receives the
 // row-pass output of the product; sbuf holds b's column-pass output.
 template <class C, int K1>
@@ -450,93 +498,31 @@ __global__ void __launch_bounds__(C::THREADS, 2) k_polymul_rows(LimbSet ca, Cons
 }
 
 // ===========================================================================
-// Element-wise ops, two words per thread with 128-bit accesses.
+// Launch templates.  A variant is (degree, tile size T) for whole-limb
+// degrees and (degree, column stages K1) for two-pass degrees.
 // ===========================================================================
-template <int OP>
-__global__ void __launch_bounds__(256) k_elementwise(LimbSet dst, ConstLimbSet a, ConstLimbSet b,
-                                                     uint32_t log_n, const DevMod* __restrict__ mods) {
-  const size_t pairs = ((size_t)dst.count << log_n) >> 1;
-  const uint32_t nmask = (1u << log_n) - 1u;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < pairs;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const size_t v = i * 2;
-    const uint32_t limb = (uint32_t)(v >> log_n);
-    const uint32_t off = (uint32_t)v & nmask;
-    const uint32_t cm = dst.cm(limb);
-    const uint64_t p = __ldg(&mods[cm].p);
-    const ulonglong2 x = ld_pair(a.limb(limb, log_n) + off);
-    uint64_t* d = dst.limb(limb, log_n) + off;
-    uint64_t r0, r1;
-    if (OP == (int)EwOp::kNegate) {
-      r0 = p - x.x;
-      r1 = p - x.y;
-    } else {
-      const ulonglong2 y = ld_pair(b.limb(limb, log_n) + off);
-      if (OP == (int)EwOp::kAddmod) {
-        r0 = addmod(x.x, y.x, p);
-        r1 = addmod(x.y, y.y, p);
-      } else if (OP == (int)EwOp::kSubmod) {
-        r0 = submod(x.x, y.x, p);
-        r1 = submod(x.y, y.y, p);
-      } else {
-        const uint64_t pn = __ldg(&mods[cm].pn);
-        if (OP == (int)EwOp::kMulmod) {
-          r0 = mulmod_barrett(x.x, y.x, p, pn);
-          r1 = mulmod_barrett(x.y, y.y, p, pn);
-        } else {
-          const ulonglong2 acc = *reinterpret_cast<const ulonglong2*>(d);
-          r0 = muladd_barrett(acc.x, x.x, y.x, p, pn);
-          r1 = muladd_barrett(acc.y, x.y, y.y, p, pn);
-        }
-      }
-    }
-    st_pair(d, r0, r1);
-  }
-}
-
-// ===========================================================================
-// Host-side dispatch.
-// ===========================================================================
-int g_num_sms = 0;
-
-int num_sms() {
-  if (g_num_sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (g_num_sms <= 0) g_num_sms = 1;
-  }
-  return g_num_sms;
-}
-
 template <typename KernelT>
 cudaError_t set_smem(KernelT kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-// Whole-limb tile: 2^max(log_n, 12) words; 16 words per thread (8 at N = 8).
-template <int LOGN>
-using WholeCfg = TileCfg<(LOGN > 12 ? LOGN : 12), LOGN, 0, (LOGN >= 4 ? 4 : 3)>;
+// Whole-limb tile: 2^T words (T >= log_n); 16 words per thread (8 at N = 8).
+template <int LOGN, int T>
+using WholeCfg = TileCfg<T, LOGN, 0, (LOGN >= 4 ? 4 : 3)>;
+template <int LOGN, int K1>
+using ColCfg = TileCfg<kTileLog, K1, kTileLog - K1, 4>;
+template <int LOGN, int K1>
+using RowCfg = TileCfg<kTileLog, LOGN - K1, 0, 4>;
 
-// Two-pass split: k1 column stages, log_n - k1 row stages.
-constexpr int k1_of(int log_n) { return log_n <= 15 ? 7 : 8; }
-template <int LOGN>
-using ColCfg = TileCfg<kTileLog, k1_of(LOGN), kTileLog - k1_of(LOGN), 4>;
-template <int LOGN>
-using RowCfg = TileCfg<kTileLog, LOGN - k1_of(LOGN), 0, 4>;
+constexpr size_t tile_bytes(int T) { return tile_smem_words(1u << T) * sizeof(uint64_t); }
+constexpr size_t kTileSmemBytes = tile_bytes(kTileLog);
 
-template <int LOGN>
-size_t whole_smem_bytes() {
-  return tile_smem_words(1u << WholeCfg<LOGN>::T) * sizeof(uint64_t);
-}
-constexpr size_t kTileSmemBytes = tile_smem_words(1u << kTileLog) * sizeof(uint64_t);
-
-template <int LOGN>
+template <int LOGN, int T>
 cudaError_t launch_whole_ntt(const LimbSet& ls, const DevMod* mods, NttDir dir, cudaStream_t st) {
-  using C = WholeCfg<LOGN>;
-  const uint32_t per = 1u << (C::T - LOGN);
+  using C = WholeCfg<LOGN, T>;
+  const uint32_t per = 1u << (T - LOGN);
   const uint32_t grid = (ls.count + per - 1) / per;
-  const size_t smem = whole_smem_bytes<LOGN>();
+  const size_t smem = tile_bytes(T);
   LaunchScope ps(dir == NttDir::kBackward ? "ntt_whole_inv" : "ntt_whole_fwd", st);
   switch (dir) {
     case NttDir::kForward: k_ntt_whole<C, 0><<<grid, C::THREADS, smem, st>>>(ls, mods); break;
@@ -547,11 +533,34 @@ cudaError_t launch_whole_ntt(const LimbSet& ls, const DevMod* mods, NttDir dir, 
   return cudaGetLastError();
 }
 
-template <int LOGN>
+template <int LOGN, int T>
+cudaError_t launch_whole_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
+                                 const DevMod* mods, uint64_t*, uint64_t* const*, cudaStream_t st) {
+  using C = WholeCfg<LOGN, T>;
+  const uint32_t per = 1u << (T - LOGN);
+  const uint32_t grid = (c.count + per - 1) / per;
+  LaunchScope ps("polymul_whole", st);
+  k_polymul_whole<C><<<grid, C::THREADS, 2 * tile_bytes(T), st>>>(c, a, b, mods);
+  g_kernel_launches += 1;
+  return cudaGetLastError();
+}
+
+template <int LOGN, int T>
+cudaError_t set_attrs_whole() {
+  using C = WholeCfg<LOGN, T>;
+  const size_t s = tile_bytes(T);
+  cudaError_t e;
+  if ((e = set_smem(k_ntt_whole<C, 0>, s)) != cudaSuccess) return e;
+  if ((e = set_smem(k_ntt_whole<C, 1>, s)) != cudaSuccess) return e;
+  if ((e = set_smem(k_ntt_whole<C, 2>, s)) != cudaSuccess) return e;
+  return set_smem(k_polymul_whole<C>, 2 * s);
+}
+
+template <int LOGN, int K1>
 cudaError_t launch_two_pass_ntt(const LimbSet& ls, const DevMod* mods, NttDir dir, cudaStream_t st) {
-  constexpr int K1 = k1_of(LOGN), LOGB = LOGN - K1;
-  using CC = ColCfg<LOGN>;
-  using RC = RowCfg<LOGN>;
+  constexpr int LOGB = LOGN - K1;
+  using CC = ColCfg<LOGN, K1>;
+  using RC = RowCfg<LOGN, K1>;
   const uint32_t tiles = ls.count << (LOGN - kTileLog);
   const ConstLimbSet cls = as_const(ls);
   if (dir == NttDir::kBackward) {
@@ -574,36 +583,20 @@ cudaError_t launch_two_pass_ntt(const LimbSet& ls, const DevMod* mods, NttDir di
   return cudaGetLastError();
 }
 
-template <int LOGN>
-cudaError_t launch_whole_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
-                                 const DevMod* mods, cudaStream_t st) {
-  using C = WholeCfg<LOGN>;
-  const uint32_t per = 1u << (C::T - LOGN);
-  const uint32_t grid = (c.count + per - 1) / per;
-  LaunchScope ps("polymul_whole", st);
-  k_polymul_whole<C><<<grid, C::THREADS, 2 * whole_smem_bytes<LOGN>(), st>>>(c, a, b, mods);
-  g_kernel_launches += 1;
-  return cudaGetLastError();
-}
-
-template <int LOGN>
+template <int LOGN, int K1>
 cudaError_t launch_two_pass_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
-                                    const DevMod* mods, uint64_t* scratch, cudaStream_t st,
-                                    uint64_t* const* scratch_ptrs) {
-  constexpr int K1 = k1_of(LOGN), LOGB = LOGN - K1;
-  using CC = ColCfg<LOGN>;
-  using RC = RowCfg<LOGN>;
+                                    const DevMod* mods, uint64_t* scratch, uint64_t* const* scratch_ptrs,
+                                    cudaStream_t st) {
+  constexpr int LOGB = LOGN - K1;
+  using CC = ColCfg<LOGN, K1>;
+  using RC = RowCfg<LOGN, K1>;
   const uint32_t tiles = c.count << (LOGN - kTileLog);
   LimbSet sl = c;
   sl.base = scratch_ptrs ? nullptr : scratch;
   sl.ptrs = scratch_ptrs;
   {
-    LaunchScope ps("polymul_col_fwd_a", st);
-    k_col_pass<CC, LOGB, false><<<tiles, CC::THREADS, kTileSmemBytes, st>>>(a, c, mods);
-  }
-  {
-    LaunchScope ps("polymul_col_fwd_b", st);
-    k_col_pass<CC, LOGB, false><<<tiles, CC::THREADS, kTileSmemBytes, st>>>(b, sl, mods);
+    LaunchScope ps("polymul_col_fwd", st);
+    k_col_pass2<CC, LOGB><<<tiles, CC::THREADS, 2 * kTileSmemBytes, st>>>(a, b, c, sl, mods);
   }
   {
     LaunchScope ps("polymul_rows", st);
@@ -613,129 +606,48 @@ cudaError_t launch_two_pass_polymul(const LimbSet& c, const ConstLimbSet& a, con
     LaunchScope ps("polymul_col_inv", st);
     k_col_pass<CC, LOGB, true><<<tiles, CC::THREADS, kTileSmemBytes, st>>>(as_const(c), c, mods);
   }
-  g_kernel_launches += 4;
+  g_kernel_launches += 3;
   return cudaGetLastError();
 }
 
-template <int LOGN>
-cudaError_t set_attrs_for() {
+template <int LOGN, int K1>
+cudaError_t set_attrs_two_pass() {
+  constexpr int LOGB = LOGN - K1;
+  using CC = ColCfg<LOGN, K1>;
+  using RC = RowCfg<LOGN, K1>;
   cudaError_t e;
-  if constexpr (LOGN <= 13) {
-    using C = WholeCfg<LOGN>;
-    const size_t s = whole_smem_bytes<LOGN>();
-    if ((e = set_smem(k_ntt_whole<C, 0>, s)) != cudaSuccess) return e;
-    if ((e = set_smem(k_ntt_whole<C, 1>, s)) != cudaSuccess) return e;
-    if ((e = set_smem(k_ntt_whole<C, 2>, s)) != cudaSuccess) return e;
-    if ((e = set_smem(k_polymul_whole<C>, 2 * s)) != cudaSuccess) return e;
-  } else {
-    constexpr int K1 = k1_of(LOGN), LOGB = LOGN - K1;
-    using CC = ColCfg<LOGN>;
-    using RC = RowCfg<LOGN>;
-    if ((e = set_smem(k_col_pass<CC, LOGB, false>, kTileSmemBytes)) != cudaSuccess) return e;
-    if ((e = set_smem(k_col_pass<CC, LOGB, true>, kTileSmemBytes)) != cudaSuccess) return e;
-    if ((e = set_smem(k_row_pass<RC, K1, false>, kTileSmemBytes)) != cudaSuccess) return e;
-    if ((e = set_smem(k_row_pass<RC, K1, true>, kTileSmemBytes)) != cudaSuccess) return e;
-    if ((e = set_smem(k_polymul_rows<RC, K1>, 2 * kTileSmemBytes)) != cudaSuccess) return e;
-  }
-  return cudaSuccess;
+  if ((e = set_smem(k_col_pass<CC, LOGB, false>, kTileSmemBytes)) != cudaSuccess) return e;
+  if ((e = set_smem(k_col_pass<CC, LOGB, true>, kTileSmemBytes)) != cudaSuccess) return e;
+  if ((e = set_smem(k_row_pass<RC, K1, false>, kTileSmemBytes)) != cudaSuccess) return e;
+  if ((e = set_smem(k_row_pass<RC, K1, true>, kTileSmemBytes)) != cudaSuccess) return e;
+  if ((e = set_smem(k_col_pass2<CC, LOGB>, 2 * kTileSmemBytes)) != cudaSuccess) return e;
+  return set_smem(k_polymul_rows<RC, K1>, 2 * kTileSmemBytes);
 }
 
-template <int... LOGNS>
-cudaError_t set_all_attrs(std::integer_sequence<int, LOGNS...>) {
-  cudaError_t e = cudaSuccess;
-  ((e = (e == cudaSuccess ? set_attrs_for<LOGNS>() : e)), ...);
-  return e;
+template <int LOGN, int T>
+Variant whole_variant() {
+  Variant v;
+  std::snprintf(v.name, sizeof(v.name), "whole-limb tile 2^%d (%d threads, %d limbs/CTA)", T,
+                1 << (T - (LOGN >= 4 ? 4 : 3)), 1 << (T - LOGN));
+  v.ntt = &launch_whole_ntt<LOGN, T>;
+  v.polymul = &launch_whole_polymul<LOGN, T>;
+  v.set_attrs = &set_attrs_whole<LOGN, T>;
+  v.ntt_launches = 1;
+  v.polymul_launches = 1;
+  return v;
 }
 
-template <int LOGN>
-cudaError_t ntt_dispatch(const LimbSet& ls, const DevMod* mods, NttDir dir, cudaStream_t st) {
-  if constexpr (LOGN <= 13)
-    return launch_whole_ntt<LOGN>(ls, mods, dir, st);
-  else
-    return launch_two_pass_ntt<LOGN>(ls, mods, dir, st);
-}
-
-template <int LOGN>
-cudaError_t polymul_dispatch(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
-                             const DevMod* mods, uint64_t* scratch, cudaStream_t st,
-                             uint64_t* const* scratch_ptrs) {
-  if constexpr (LOGN <= 13)
-    return launch_whole_polymul<LOGN>(c, a, b, mods, st);
-  else
-    return launch_two_pass_polymul<LOGN>(c, a, b, mods, scratch, st, scratch_ptrs);
+template <int LOGN, int K1>
+Variant two_pass_variant() {
+  Variant v;
+  std::snprintf(v.name, sizeof(v.name), "two-pass k1=%d (columns of 2^%d, rows of 2^%d)", K1, K1, LOGN - K1);
+  v.ntt = &launch_two_pass_ntt<LOGN, K1>;
+  v.polymul = &launch_two_pass_polymul<LOGN, K1>;
+  v.set_attrs = &set_attrs_two_pass<LOGN, K1>;
+  v.ntt_launches = 2;
+  v.polymul_launches = 3;
+  return v;
 }
 
 }  // namespace
-
-uint32_t default_k1(uint32_t log_n) { return (uint32_t)k1_of((int)log_n); }
-
-cudaError_t init_kernel_attributes() {
-  return set_all_attrs(std::integer_sequence<int, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17>{});
-}
-
-uint32_t ntt_launch_count(uint32_t log_n, const NttShape&) { return log_n <= 13 ? 1u : 2u; }
-uint32_t polymul_launch_count(uint32_t log_n, const NttShape&) { return log_n <= 13 ? 1u : 4u; }
-
-size_t polymul_scratch_words(uint32_t count, uint32_t log_n, const NttShape&) {
-  return log_n <= 13 ? 0 : ((size_t)count << log_n);
-}
-
-#define YELL_DEGREE_SWITCH(LOGN, CALL) \
-  switch (LOGN) {                      \
-    case 3: return CALL(3);            \
-    case 4: return CALL(4);            \
-    case 5: return CALL(5);            \
-    case 6: return CALL(6);            \
-    case 7: return CALL(7);            \
-    case 8: return CALL(8);            \
-    case 9: return CALL(9);            \
-    case 10: return CALL(10);          \
-    case 11: return CALL(11);          \
-    case 12: return CALL(12);          \
-    case 13: return CALL(13);          \
-    case 14: return CALL(14);          \
-    case 15: return CALL(15);          \
-    case 16: return CALL(16);          \
-    case 17: return CALL(17);          \
-    default: return cudaErrorInvalidValue; \
-  }
-
-cudaError_t launch_ntt(const LimbSet& ls, uint32_t log_n, const DevMod* mods, NttDir dir,
-                       const NttShape&, cudaStream_t st) {
-  if (ls.count == 0) return cudaSuccess;
-#define YELL_NTT_CALL(L) ntt_dispatch<L>(ls, mods, dir, st)
-  YELL_DEGREE_SWITCH(log_n, YELL_NTT_CALL)
-#undef YELL_NTT_CALL
-}
-
-cudaError_t launch_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
-                           uint32_t log_n, const DevMod* mods, uint64_t* scratch,
-                           const NttShape&, cudaStream_t st, uint64_t* const* scratch_ptrs) {
-  if (c.count == 0) return cudaSuccess;
-  if (log_n > 13 && scratch == nullptr && scratch_ptrs == nullptr) return cudaErrorInvalidValue;
-#define YELL_PM_CALL(L) polymul_dispatch<L>(c, a, b, mods, scratch, st, scratch_ptrs)
-  YELL_DEGREE_SWITCH(log_n, YELL_PM_CALL)
-#undef YELL_PM_CALL
-}
-
-cudaError_t launch_elementwise(EwOp op, const LimbSet& dst, const ConstLimbSet& a,
-                               const ConstLimbSet& b, uint32_t log_n, const DevMod* mods,
-                               cudaStream_t st) {
-  if (dst.count == 0) return cudaSuccess;
-  const size_t pairs = ((size_t)dst.count << log_n) >> 1;
-  const size_t want = (pairs + 255) / 256;
-  const size_t cap = (size_t)num_sms() * 8;
-  const uint32_t grid = (uint32_t)(want < cap ? want : cap);
-  LaunchScope ps("elementwise", st);
-  switch (op) {
-    case EwOp::kMulmod: k_elementwise<0><<<grid, 256, 0, st>>>(dst, a, b, log_n, mods); break;
-    case EwOp::kAddmod: k_elementwise<1><<<grid, 256, 0, st>>>(dst, a, b, log_n, mods); break;
-    case EwOp::kSubmod: k_elementwise<2><<<grid, 256, 0, st>>>(dst, a, b, log_n, mods); break;
-    case EwOp::kMuladd: k_elementwise<3><<<grid, 256, 0, st>>>(dst, a, b, log_n, mods); break;
-    case EwOp::kNegate: k_elementwise<4><<<grid, 256, 0, st>>>(dst, a, b, log_n, mods); break;
-  }
-  g_kernel_launches += 1;
-  return cudaGetLastError();
-}
-
 }  // namespace yell_gb300

@@ -153,6 +153,7 @@ int DeviceContext::init() {
   }
   e = init_kernel_attributes();
   if (e != cudaSuccess) return fail_cuda(e, "cudaFuncSetAttribute");
+  load_tuning(device_);
   return kOk;
 }
 

@@ -42,6 +42,9 @@ int fail_cuda(cudaError_t e, const char* what);
 const char* last_error();
 void clear_error();
 
+// Applies persisted autotuner choices for a device (YELL_GB300_TUNE_FILE).
+void load_tuning(int device);
+
 // Argument checks shared by the entry points.
 int check_degree(uint32_t log_n);
 int check_moduli(uint32_t cm0, uint32_t L);
