@@ -246,7 +246,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
                           device="cuda")
     y.init_ntt_tables(LOG_N, L)
     # autotune the launch variant of this degree at this size (same words for every variant)
-    tuned_variant, _ = y.autotune(LOG_N, L, pairs)
+    if args.no_autotune:
+        tuned_variant = y.get_variant(LOG_N)
+    else:
+        tuned_variant, _ = y.autotune(LOG_N, L, pairs)
     stream = torch.cuda.Stream()
 
     def step():
@@ -355,7 +358,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
     # ---- uneven batch (512 polymuls, log2 N in 10..16, L in 1..16) ----------
     uneven = serving = None
     if not args.no_uneven:
-        uneven = run_uneven(torch, y, stream, barrier, max_over_ranks, world)
+        uneven = run_uneven(torch, y, stream, barrier, max_over_ranks, world, args.no_autotune)
         if not args.no_serve:
             serving = run_serving(torch, y, uneven, args.serve_seconds)
         uneven.pop("_items")
@@ -424,7 +427,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
     return 0
 
 
-def run_uneven(torch, y, stream, barrier, max_over_ranks, world):
+def run_uneven(torch, y, stream, barrier, max_over_ranks, world, no_autotune=False):
     """512 polymuls of mixed degree and limb count (seed 4): one batched call
     (bucketed, CUDA graph per batch shape) against 512 plain per-call calls."""
     from yell_gb300.workloads import mix_limb_ntts, mix_operands, uneven_mix
@@ -441,7 +444,8 @@ def run_uneven(torch, y, stream, barrier, max_over_ranks, world):
         singles.append(torch.empty(sw, dtype=torch.int64, device="cuda") if sw else None)
     for log_n in range(10, 17):
         y.init_ntt_tables(log_n, 16)
-        y.autotune(log_n, 8, 4)
+        if not no_autotune:
+            y.autotune(log_n, 8, 4)
     limb_ntts = mix_limb_ntts(mix)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -526,6 +530,8 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch comparison")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving sweep")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the selected launch variants (default or YELL_GB300_TUNE_FILE)")
     ap.add_argument("--serve-seconds", type=float, default=0.5, help="seconds per serving load point")
     ap.add_argument("--device-only", action="store_true",
                     help="time only the device-resident batch (for profiler captures)")

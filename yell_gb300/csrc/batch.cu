@@ -80,14 +80,20 @@ int BatchExecutor::reserve_scratch(size_t words) {
   return kOk;
 }
 
+int BatchExecutor::reserve_limbs(size_t limbs) {
+  const int st = reserve_lists(limbs * (4 * 8 + 4) + kDegrees * 16);
+  return st != kOk ? st : reserve_scratch(2);
+}
+
 cudaError_t BatchExecutor::launch_buckets(const std::vector<Bucket>& buckets, cudaStream_t s,
-                                          bool scratch_lists) {
-  cudaError_t le = cudaEventRecord(fork_, s);
+                                          bool scratch_lists, bool fork) {
+  fork = fork && buckets.size() > 1;
+  cudaError_t le = fork ? cudaEventRecord(fork_, s) : cudaSuccess;
   for (size_t i = 0; i < buckets.size() && le == cudaSuccess; ++i) {
     const Bucket& b = buckets[i];
     const int k = (int)(b.log_n - kMinLogN);
-    cudaStream_t side = side_[k];
-    le = cudaStreamWaitEvent(side, fork_, 0);
+    cudaStream_t side = fork ? side_[k] : s;
+    if (fork) le = cudaStreamWaitEvent(side, fork_, 0);
     if (le != cudaSuccess) break;
     LimbSet c;
     c.base = nullptr;
@@ -104,14 +110,14 @@ cudaError_t BatchExecutor::launch_buckets(const std::vector<Bucket>& buckets, cu
     uint64_t* const* sptrs =
         scratch_lists ? reinterpret_cast<uint64_t* const*>(d_lists_ + b.s_off) : nullptr;
     le = launch_polymul(c, a, bb, b.log_n, b.mods, d_scratch_ + b.scratch_off, NttShape{}, side, sptrs);
-    if (le == cudaSuccess) le = cudaEventRecord(join_[k], side);
-    if (le == cudaSuccess) le = cudaStreamWaitEvent(s, join_[k], 0);
+    if (fork && le == cudaSuccess) le = cudaEventRecord(join_[k], side);
+    if (fork && le == cudaSuccess) le = cudaStreamWaitEvent(s, join_[k], 0);
   }
   return le;
 }
 
 int BatchExecutor::run(DeviceContext* ctx, const yell_polymul_desc* descs, uint64_t* const* desc_scratch,
-                       uint32_t n, cudaStream_t s, bool use_graph) {
+                       uint32_t n, cudaStream_t s, bool use_graph, bool fork) {
   // ---- buckets and their list layout -----------------------------------
   std::array<std::vector<uint32_t>, kDegrees> members;
   for (uint32_t i = 0; i < n; ++i) members[descs[i].log_n - kMinLogN].push_back(i);
@@ -172,19 +178,19 @@ int BatchExecutor::run(DeviceContext* ctx, const yell_polymul_desc* descs, uint6
   const bool scratch_lists = desc_scratch != nullptr;
   if (!use_graph) {
     const uint64_t l0 = g_kernel_launches.load();
-    e = launch_buckets(buckets, s, scratch_lists);
+    e = launch_buckets(buckets, s, scratch_lists, fork);
     last_launches_ = g_kernel_launches.load() - l0;
     if (e != cudaSuccess) return fail_cuda(e, "batch launch");
     return kOk;
   }
-  std::string sig = std::to_string(generation_) + (scratch_lists ? "s" : "o");
+  std::string sig = std::to_string(generation_) + (scratch_lists ? "s" : "o") + (fork ? "f" : "q");
   for (const Bucket& b : buckets) sig += ";" + std::to_string(b.log_n) + ":" + std::to_string(b.limbs);
   auto it = graphs_.find(sig);
   if (it == graphs_.end()) {
     const uint64_t launches0 = g_kernel_launches.load();
     e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return fail_cuda(e, "batch capture begin");
-    const cudaError_t le = launch_buckets(buckets, s, scratch_lists);
+    const cudaError_t le = launch_buckets(buckets, s, scratch_lists, fork);
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(s, &graph);
     if (le != cudaSuccess) {

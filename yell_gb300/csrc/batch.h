@@ -27,8 +27,15 @@ class BatchExecutor {
   // else the executor's own grow-on-demand scratch.  With use_graph the
   // launch sequence is captured once per batch shape and replayed.  The
   // caller has made sure every entry's tables are resident (ensure_tables).
+  // With fork, buckets run on per-degree side streams joined back into s;
+  // without, they run one after another on s (cheaper to issue for small
+  // batches whose concurrency comes from several slots in flight).
   int run(DeviceContext* ctx, const yell_polymul_desc* descs, uint64_t* const* desc_scratch,
-          uint32_t n, cudaStream_t s, bool use_graph);
+          uint32_t n, cudaStream_t s, bool use_graph, bool fork = true);
+
+  // Grows the list buffers to hold `limbs` limbs now (so later runs do not
+  // reallocate, which would synchronise the device).
+  int reserve_limbs(size_t limbs);
 
   // Kernel launches made by the last run() (replays included).
   uint64_t last_launches() const { return last_launches_; }
@@ -49,7 +56,8 @@ class BatchExecutor {
   int reserve_lists(size_t bytes);
   int reserve_scratch(size_t words);
   void drop_graphs();
-  cudaError_t launch_buckets(const std::vector<Bucket>& buckets, cudaStream_t s, bool scratch_lists);
+  cudaError_t launch_buckets(const std::vector<Bucket>& buckets, cudaStream_t s, bool scratch_lists,
+                             bool fork);
 
   uint8_t* d_lists_ = nullptr;
   uint8_t* h_lists_ = nullptr;

@@ -237,9 +237,11 @@ void yell_host_free(void* p) {
   if (p) cudaFreeHost(p);
 }
 
-// Pipelined host polymul: chunks of whole pairs cycle through kPipeSlots
-// streams, each with its own device buffers (a, b, c, scratch), so the copy
-// engines move chunk k+1 in and chunk k-1 out while chunk k computes.
+// Pipelined host polymul: chunks of whole pairs move through three streams
+// (H2D, compute, D2H) using kPipeSlots device buffer sets in turn, so the
+// copy engines move chunk k+1 in and chunk k-1 out while chunk k computes.
+// Reusing a slot waits (on the GPU) for the compute that read its operands
+// and for the copy-out that read its product.
 int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_t pairs,
                       uint32_t L, uint32_t log_n, uint32_t cm0) {
   if (!c || !a || !b) return fail(kInvalidArgument, "null pointer");
@@ -251,8 +253,8 @@ int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_
   const DevMod* mods;
   YELL_TRY(ctx->ensure_tables(log_n, cm0, L, &mods));
   const size_t pair_words = ((size_t)L) << log_n;
-  // ~32 MiB of operands per chunk, at least one pair.
-  const size_t target = (32ull << 20) / 8;
+  // ~64 MiB of operands per chunk, at least one pair.
+  const size_t target = (64ull << 20) / 8;
   uint32_t cp = (uint32_t)std::max<size_t>(1, target / (2 * pair_words));
   if (cp > pairs) cp = pairs;
   const size_t cw = cp * pair_words;
@@ -262,25 +264,33 @@ int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_
     std::lock_guard<std::mutex> gb(ctx->pipe_buf[s].lock);
     YELL_TRY(ctx->pipe_buf[s].reserve(3 * cw + sw));
   }
-  uint32_t slot = 0;
-  for (uint32_t p0 = 0; p0 < pairs; p0 += cp, slot = (slot + 1) % DeviceContext::kPipeSlots) {
+  cudaStream_t h2d = ctx->pipe_stream[0], comp = ctx->pipe_stream[1], d2h = ctx->pipe_stream[2];
+  uint32_t k = 0;
+  for (uint32_t p0 = 0; p0 < pairs; p0 += cp, ++k) {
+    const int s = (int)(k % DeviceContext::kPipeSlots);
+    const bool reuse = k >= (uint32_t)DeviceContext::kPipeSlots;
     const uint32_t np = std::min(cp, pairs - p0);
     const size_t w = np * pair_words;
-    cudaStream_t st = ctx->pipe_stream[slot];
-    uint64_t* da = ctx->pipe_buf[slot].ptr;
+    uint64_t* da = ctx->pipe_buf[s].ptr;
     uint64_t* db = da + cw;
     uint64_t* dc = db + cw;
     uint64_t* ds = dc + cw;
-    YELL_CUDA(cudaMemcpyAsync(da, a + p0 * pair_words, w * 8, cudaMemcpyHostToDevice, st), "H2D a");
-    YELL_CUDA(cudaMemcpyAsync(db, b + p0 * pair_words, w * 8, cudaMemcpyHostToDevice, st), "H2D b");
+    if (reuse) YELL_CUDA(cudaStreamWaitEvent(h2d, ctx->pipe_comp[s], 0), "pipe order");
+    YELL_CUDA(cudaMemcpyAsync(da, a + p0 * pair_words, w * 8, cudaMemcpyHostToDevice, h2d), "H2D a");
+    YELL_CUDA(cudaMemcpyAsync(db, b + p0 * pair_words, w * 8, cudaMemcpyHostToDevice, h2d), "H2D b");
+    YELL_CUDA(cudaEventRecord(ctx->pipe_h2d[s], h2d), "pipe event");
+    YELL_CUDA(cudaStreamWaitEvent(comp, ctx->pipe_h2d[s], 0), "pipe order");
+    if (reuse) YELL_CUDA(cudaStreamWaitEvent(comp, ctx->pipe_d2h[s], 0), "pipe order");
     YELL_CUDA(launch_polymul(contiguous(dc, np * L, L, cm0), const_contiguous(da, np * L, L, cm0),
                              const_contiguous(db, np * L, L, cm0), log_n, mods, sw ? ds : nullptr,
-                             ctx->shape, st),
+                             ctx->shape, comp),
               "launch polymul");
-    YELL_CUDA(cudaMemcpyAsync(c + p0 * pair_words, dc, w * 8, cudaMemcpyDeviceToHost, st), "D2H c");
+    YELL_CUDA(cudaEventRecord(ctx->pipe_comp[s], comp), "pipe event");
+    YELL_CUDA(cudaStreamWaitEvent(d2h, ctx->pipe_comp[s], 0), "pipe order");
+    YELL_CUDA(cudaMemcpyAsync(c + p0 * pair_words, dc, w * 8, cudaMemcpyDeviceToHost, d2h), "D2H c");
+    YELL_CUDA(cudaEventRecord(ctx->pipe_d2h[s], d2h), "pipe event");
   }
-  for (int s = 0; s < DeviceContext::kPipeSlots; ++s)
-    YELL_CUDA(cudaStreamSynchronize(ctx->pipe_stream[s]), "synchronize");
+  for (int i = 0; i < 3; ++i) YELL_CUDA(cudaStreamSynchronize(ctx->pipe_stream[i]), "synchronize");
   return kOk;
 }
 

@@ -147,9 +147,16 @@ DeviceContext::DeviceContext(int device) : device_(device) {}
 int DeviceContext::init() {
   cudaError_t e = cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking);
   if (e != cudaSuccess) return fail_cuda(e, "cudaStreamCreate");
-  for (int i = 0; i < kPipeSlots; ++i) {
+  for (int i = 0; i < 3; ++i) {
     e = cudaStreamCreateWithFlags(&pipe_stream[i], cudaStreamNonBlocking);
     if (e != cudaSuccess) return fail_cuda(e, "cudaStreamCreate(pipe)");
+  }
+  for (int i = 0; i < kPipeSlots; ++i) {
+    cudaEvent_t* evs[] = {&pipe_h2d[i], &pipe_comp[i], &pipe_d2h[i]};
+    for (cudaEvent_t* ev : evs) {
+      e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+      if (e != cudaSuccess) return fail_cuda(e, "cudaEventCreate(pipe)");
+    }
   }
   e = init_kernel_attributes();
   if (e != cudaSuccess) return fail_cuda(e, "cudaFuncSetAttribute");

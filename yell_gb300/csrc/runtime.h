@@ -86,10 +86,13 @@ class DeviceContext {
   Buffer scratch;   // polymul scratch for device-resident calls
   Buffer staging;   // host-pointer drop-ins: operands / results
 
-  // Pipelined host polymul slots (streams + buffers), under `pipe_lock`.
+  // Pipelined host polymul, under `pipe_lock`: one stream each for H2D,
+  // compute and D2H; kPipeSlots device buffer sets cycled by the chunks, with
+  // per-slot events ordering reuse of a slot's buffers.
   std::mutex pipe_lock;
   static constexpr int kPipeSlots = 3;
-  cudaStream_t pipe_stream[kPipeSlots] = {};
+  cudaStream_t pipe_stream[3] = {};  // 0: H2D, 1: compute, 2: D2H
+  cudaEvent_t pipe_h2d[kPipeSlots] = {}, pipe_comp[kPipeSlots] = {}, pipe_d2h[kPipeSlots] = {};
   Buffer pipe_buf[kPipeSlots];
 
   NttShape shape;  // launch shape (autotuner may adjust)

@@ -155,6 +155,7 @@ int yell_server::init(const yell_server_config* c) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming);
     if (e != cudaSuccess) return fail_cuda(e, "server slot");
     st = s->exec.init();
+    if (st == kOk) st = s->exec.reserve_limbs((size_t)cfg.max_batch * 64);  // no growth in steady state
     if (st != kOk) return st;
     slots.push_back(std::move(s));
   }
@@ -257,7 +258,7 @@ int yell_server::launch(Slot& s, std::vector<ReqPtr>& batch) {
     scratch[i] = r.d_s;
   }
   if (e != cudaSuccess) return fail_cuda(e, "server H2D");
-  const int st = s.exec.run(ctx, descs.data(), scratch.data(), (uint32_t)n, s.stream, false);
+  const int st = s.exec.run(ctx, descs.data(), scratch.data(), (uint32_t)n, s.stream, false, false);
   if (st != kOk) return st;
   for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
     Request& r = *batch[i];
