@@ -232,6 +232,41 @@ int yell_server_get_stats(yell_server* s, int reset, yell_server_stats* out);
 int yell_server_load_test(yell_server* s, const yell_polymul_request* templates, uint32_t n,
                           double offered_rps, double duration_s, uint64_t seed, yell_server_stats* out);
 
+/* ---- seeded device samplers: replace poly<N>::set(uniform / ZO_dist / hwt_dist /
+ * gaussian) (include/yell/details/poly.hpp:195-330) -------------------------
+ * Fill `count` polys (count, L, N) on the device.  The reference's samplers
+ * are unseeded; these draw random word k of a stream as
+ * splitmix64(seed + (k + 1) * 0x9E3779B97F4A7C15) and turn words into
+ * coefficients with the reference's rule for each distribution (uniform: mask
+ * to 2^(floor(log2 p)+1) then subtract p once; ZO: one byte r per coefficient,
+ * r <= rho ? (r & 2 ? -1 : 1) : 0; HWT: exactly h coefficients +-1; gaussian:
+ * a centred integer |e| <= tail by a cumulative table, times `amplifier` as
+ * in the reference's gaussian{prng, amp}; tail <= 1024, tail*amplifier < 2^61).  ZO, HWT and gaussian
+ * coefficients are the same integers in every limb, mapped e < 0 ? p + e : e. */
+int yell_dev_sample_uniform(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
+                            uint64_t seed, void* stream);
+int yell_dev_sample_zo(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
+                       uint32_t rho, uint64_t seed, void* stream);
+int yell_dev_sample_hwt(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
+                        uint32_t h, uint64_t seed, void* stream);
+int yell_dev_sample_gaussian(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
+                             double sigma, uint32_t tail, uint64_t amplifier, uint64_t seed, void* stream);
+
+/* ---- RNS -> big-integer lifting: replaces gmp::poly2mpz
+ * (include/yell/gmp.hpp:42-70, tables lib/gmp.cpp:6-51) ----------------------
+ * Coefficient i of a poly with residues r_j mod q_j (moduli cm0 .. cm0+L-1,
+ * L <= 400) lifts to the unique x in [0, Q), Q = prod q_j, x = r_j mod q_j:
+ * the value poly2mpz returns for residues below their moduli (the form
+ * backward() leaves).  x is written as W little-endian 64-bit words
+ * (W = yell_crt_words(L, cm0); mpz_import(z, W, -1, 8, 0, 0, words) makes the
+ * mpz_t), coefficient-major: words [i*W, (i+1)*W) of the output. */
+int yell_crt_words(uint32_t L, uint32_t cm0, uint32_t* words);
+/* d_in: count polys (count, L, N); d_out: count * N * W words. */
+int yell_dev_crt_lift(uint64_t* d_out, const uint64_t* d_in, uint32_t count, uint32_t L, uint32_t log_n,
+                      uint32_t cm0, void* stream);
+/* Host drop-in for poly2mpz over moduli 0 .. L-1: limbs[j] -> out (N * W words). */
+int yell_poly_to_bigint(uint64_t* out, const uint64_t* const* limbs, uint32_t L, uint32_t log_n);
+
 /* ---- launch variants and the autotuner (no counterpart in the reference) --
  * Every degree has one or more launch variants that apply exactly the same
  * butterflies (same output words) with a different split of the work: limbs

@@ -9,6 +9,10 @@ Two CPU implementations are exposed through ctypes:
 * ``port``: ``liboracle.so``, the plain-C restatement in ``yell_oracle.c`` of
   the reference algorithm (fionser/YELL ``lib/ntt.cpp``, ``lib/ops.cpp``,
   ``include/yell/details/ntt.hpp``), built by ``oracle/Makefile``.
+  ``samplers_oracle.c`` restates the reference's sampler rules
+  (``include/yell/details/poly.hpp:195-330``) over the seeded counter stream.
+* ``crt.py``: pure-Python big-integer restatement of ``gmp::poly2mpz``
+  (``include/yell/gmp.hpp:42-70``, ``lib/gmp.cpp:6-51``).
 * ``ref``: ``_ref/libyellref.so``, the reference's own sources compiled
   unmodified with ``ref_harness.cpp``; present only where the reference
   checkout was available to build it (``ref_available()``).
@@ -60,6 +64,11 @@ def _bind(lib, prefix: str):
             "negacyclic_schoolbook": (ctypes.c_int, [_U64P, _U64P, _U64P, u32, u32]),
             "polymul": (ctypes.c_int, [_U64P, _U64P, _U64P, u32, u32, u32]),
             "polymul_batch": (ctypes.c_double, [_U64P, _U64P, _U64P, u32, u32, u32, u32, u32]),
+            "sample_uniform": (None, [_U64P, u32, u32, u32, u32, u64]),
+            "sample_zo": (None, [_U64P, u32, u32, u32, u32, u32, u64]),
+            "sample_hwt": (ctypes.c_int, [_U64P, u32, u32, u32, u32, u32, u64]),
+            "gaussian_cdt": (u32, [ctypes.c_double, u32, _U64P]),
+            "sample_gaussian": (None, [_U64P, u32, u32, u32, u32, _U64P, u32, u32, u64, u64]),
         })
     else:
         sig["polymul_batch"] = (ctypes.c_double, [_U64P, _U64P, _U64P, u32, u32, u32, u32])
@@ -240,3 +249,35 @@ class Oracle:
         if t < 0:
             raise ValueError("polymul_batch: bad arguments")
         return c, float(t)
+
+    # --- samplers (port only) ------------------------------------------------
+    def _polys(self, count, L, log_n):
+        return np.zeros((count, L, 1 << log_n), dtype=np.uint64)
+
+    def sample_uniform(self, count, L, log_n, cm0=0, seed=0):
+        out = self._polys(count, L, log_n)
+        self.lib.orc_sample_uniform(_ptr(out), count, L, log_n, cm0, seed)
+        return out
+
+    def sample_zo(self, count, L, log_n, cm0=0, rho=0x7F, seed=0):
+        out = self._polys(count, L, log_n)
+        self.lib.orc_sample_zo(_ptr(out), count, L, log_n, cm0, rho, seed)
+        return out
+
+    def sample_hwt(self, count, L, log_n, h, cm0=0, seed=0):
+        out = self._polys(count, L, log_n)
+        if self.lib.orc_sample_hwt(_ptr(out), count, L, log_n, cm0, h, seed) != 0:
+            raise ValueError("sample_hwt: bad arguments")
+        return out
+
+    def gaussian_cdt(self, sigma, tail):
+        out = np.zeros(2 * tail + 1, dtype=np.uint64)
+        m = self.lib.orc_gaussian_cdt(sigma, tail, _ptr(out))
+        return out[:m]
+
+    def sample_gaussian(self, count, L, log_n, cm0=0, sigma=3.2, tail=19, amplifier=1, seed=0):
+        cdt = self.gaussian_cdt(sigma, tail)
+        out = self._polys(count, L, log_n)
+        self.lib.orc_sample_gaussian(_ptr(out), count, L, log_n, cm0, _ptr(cdt), len(cdt), tail,
+                                     amplifier, seed)
+        return out

@@ -24,7 +24,8 @@ __all__ = [
     "poly_forward", "poly_forward_lazy", "poly_backward", "poly_mulmod", "poly_addmod",
     "poly_submod", "poly_add_product_of", "poly_negate", "polymul_host", "dev_ntt",
     "dev_ntt_limbs", "dev_elementwise", "dev_polymul", "polymul_scratch_words", "kernel_launches",
-    "Poly", "PinnedBuffer",
+    "Poly", "PinnedBuffer", "sample_uniform", "sample_zo", "sample_hwt", "sample_gaussian",
+    "crt_words", "dev_crt_lift", "poly_to_bigint", "words_to_ints",
 ]
 
 
@@ -246,6 +247,52 @@ def dev_polymul_batch(items, stream=None) -> None:
     for i, (c, a, b, log_n, L, cm0) in enumerate(items):
         descs[i] = _capi.PolymulDesc(_dptr(c), _dptr(a), _dptr(b), log_n, L, cm0, 0)
     call("yell_dev_polymul_batch", ctypes.addressof(descs), len(items), _stream(stream))
+
+
+def sample_uniform(t, count: int, L: int, log_n: int, cm0: int = 0, seed: int = 0, stream=None):
+    call("yell_dev_sample_uniform", _dptr(t), count, L, log_n, cm0, seed, _stream(stream))
+
+
+def sample_zo(t, count: int, L: int, log_n: int, cm0: int = 0, rho: int = 0x7F, seed: int = 0,
+              stream=None):
+    call("yell_dev_sample_zo", _dptr(t), count, L, log_n, cm0, rho, seed, _stream(stream))
+
+
+def sample_hwt(t, count: int, L: int, log_n: int, h: int, cm0: int = 0, seed: int = 0, stream=None):
+    call("yell_dev_sample_hwt", _dptr(t), count, L, log_n, cm0, h, seed, _stream(stream))
+
+
+def sample_gaussian(t, count: int, L: int, log_n: int, cm0: int = 0, sigma: float = 3.2,
+                    tail: int = 19, amplifier: int = 1, seed: int = 0, stream=None):
+    call("yell_dev_sample_gaussian", _dptr(t), count, L, log_n, cm0, sigma, tail, amplifier, seed,
+         _stream(stream))
+
+
+def crt_words(L: int, cm0: int = 0) -> int:
+    """64-bit words of prod q_j over moduli cm0 .. cm0+L-1 (words per lifted coefficient)."""
+    w = ctypes.c_uint32()
+    call("yell_crt_words", L, cm0, ctypes.byref(w))
+    return int(w.value)
+
+
+def dev_crt_lift(out, t, count: int, L: int, log_n: int, cm0: int = 0, stream=None) -> None:
+    """Lift count (L, N) polys to integers in [0, Q): out holds count * N * crt_words(L) words."""
+    call("yell_dev_crt_lift", _dptr(out), _dptr(t), count, L, log_n, cm0, _stream(stream))
+
+
+def poly_to_bigint(limbs) -> np.ndarray:
+    """gmp::poly2mpz over moduli 0 .. L-1: (N, W) little-endian words per coefficient."""
+    ls = _limbs(limbs)
+    log_n = _log_n_of(ls)
+    out = np.zeros(((1 << log_n), crt_words(len(ls))), dtype=np.uint64)
+    call("yell_poly_to_bigint", _addr(out), _ptr_array(ls), len(ls), log_n)
+    return out
+
+
+def words_to_ints(words: np.ndarray) -> list[int]:
+    """(..., W) little-endian words -> flat list of Python integers."""
+    w = np.ascontiguousarray(words, dtype=np.uint64).reshape(-1, words.shape[-1])
+    return [int.from_bytes(row.tobytes(), "little") for row in w]
 
 
 def variants(log_n: int) -> list[str]:

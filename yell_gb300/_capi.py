@@ -89,6 +89,13 @@ SIGNATURES = {
     "yell_dev_polymul_noalloc": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),
     "yell_dev_polymul_batch": (_int, [_vp, _u32, _vp]),
     "yell_calibrate_butterflies": (_int, [_vp, _vp]),
+    "yell_crt_words": (_int, [_u32, _u32, _vp]),
+    "yell_dev_crt_lift": (_int, [_vp, _vp, _u32, _u32, _u32, _u32, _vp]),
+    "yell_poly_to_bigint": (_int, [_vp, _vp, _u32, _u32]),
+    "yell_dev_sample_uniform": (_int, [_vp, _u32, _u32, _u32, _u32, _u64, _vp]),
+    "yell_dev_sample_zo": (_int, [_vp, _u32, _u32, _u32, _u32, _u32, _u64, _vp]),
+    "yell_dev_sample_hwt": (_int, [_vp, _u32, _u32, _u32, _u32, _u32, _u64, _vp]),
+    "yell_dev_sample_gaussian": (_int, [_vp, _u32, _u32, _u32, _u32, ctypes.c_double, _u32, _u64, _u64, _vp]),
     "yell_variant_count": (_int, [_u32, _vp]),
     "yell_variant_name": (_int, [_u32, _u32, ctypes.c_char_p, _sz]),
     "yell_set_variant": (_int, [_u32, _u32]),

@@ -1,0 +1,300 @@
+// Seeded device samplers for RNS polynomials (poly<N>::set(...) of the
+// reference, include/yell/details/poly.hpp:195-330).
+//
+// The reference draws from an unseeded stream (Salsa20 keyed from
+// /dev/urandom).  Here every random word is splitmix64 of a counter, so a
+// sample is a pure function of (seed, position) and can be regenerated on the
+// host; the transformation of random words into coefficients follows the
+// reference's algorithm for each distribution:
+//   uniform  (poly.hpp:200-229): per limb, w & (2^(floor(log2 p)+1) - 1), minus p
+//            once if still >= p; independent words for every limb.
+//   ZO(rho)  (poly.hpp:262-275): one random byte r per coefficient, shared by all
+//            limbs: r <= rho ? (r & 2 ? p - 1 : 1) : 0.
+//   HWT(h)   (poly.hpp:282-325): exactly h coefficients set to +-1 (same positions
+//            and signs in every limb), the positions uniform among all h-subsets;
+//            sign bit 1 of a random word: set -> +1, clear -> p - 1.
+//   gaussian (poly.hpp:238-258): a centred integer e per coefficient, shared by all
+//            limbs, times an amplifier, mapped e < 0 ? p + e : e.  e comes from a
+//            cumulative table of 64-bit thresholds (search of one random word), not
+//            the reference's FastGaussianNoise lookup tables: the same truncated
+//            distribution exp(-e^2 / 2 sigma^2) on |e| <= tail, a different algorithm.
+// Random word k of a stream with seed s is splitmix64(s + (k + 1) * 0x9E3779B97F4A7C15).
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "profiler.h"
+#include "runtime.h"
+#include "yell_gb300.h"
+
+using namespace yell_gb300;
+
+namespace {
+
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__host__ __device__ __forceinline__ uint64_t rand_word(uint64_t seed, uint64_t k) {
+  return mix64(seed + (k + 1) * 0x9E3779B97F4A7C15ull);
+}
+
+// Derived stream seeds for the parts of one sampler.
+constexpr uint64_t kSeedPositions = 0x5ca1ab1e0ddba11ull;
+constexpr uint64_t kSeedSigns = 0x0b5e55edc0ffee5ull;
+
+__global__ void k_sample_uniform(uint64_t* out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
+                                 const DevMod* __restrict__ mods, uint64_t seed) {
+  const size_t total = ((size_t)count * L) << log_n;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t l = (uint32_t)((k >> log_n) % L);
+    const uint64_t p = __ldg(&mods[cm0 + l].p);
+    const uint64_t mask = (2ull << (63 - __clzll(p))) - 1ull;  // 2^(floor(log2 p) + 1) - 1
+    uint64_t v = rand_word(seed, k) & mask;
+    if (v >= p) v -= p;
+    out[k] = v;
+  }
+}
+
+// mode 0: ZO with threshold rho; mode 1: gaussian through the cumulative table.
+__global__ void k_sample_shared_int(uint64_t* out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
+                                    const DevMod* __restrict__ mods, uint64_t seed, int mode, uint32_t rho,
+                                    const uint64_t* __restrict__ cdt, uint32_t cdt_len, int32_t tail,
+                                    uint64_t amplifier) {
+  const size_t coeffs = (size_t)count << log_n;
+  const uint32_t nmask = (1u << log_n) - 1u;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < coeffs; k += (size_t)gridDim.x * blockDim.x) {
+    const uint64_t r = rand_word(seed, k);
+    int64_t e;
+    if (mode == 0) {
+      const uint32_t byte = (uint32_t)(r & 0xFF);
+      e = byte <= rho ? ((byte & 2) ? -1 : 1) : 0;
+    } else {
+      // first index with r < cdt[idx] (upper bound), clamped to the table
+      uint32_t lo = 0, hi = cdt_len;
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (r < __ldg(&cdt[mid])) hi = mid;
+        else lo = mid + 1;
+      }
+      if (lo >= cdt_len) lo = cdt_len - 1;
+      e = ((int64_t)lo - tail) * (int64_t)amplifier;
+    }
+    const size_t poly = k >> log_n;
+    const uint32_t i = (uint32_t)k & nmask;
+    for (uint32_t l = 0; l < L; ++l) {
+      const uint64_t p = __ldg(&mods[cm0 + l].p);
+      out[(((poly * L) + l) << log_n) + i] = e < 0 ? p + (uint64_t)e : (uint64_t)e;
+    }
+  }
+}
+
+// HWT: the h positions with the smallest random keys (a uniformly random
+// h-subset); found by an 8-bit-digit radix select over the 64-bit keys in one
+// CTA per poly, keys recomputed from the counter in every pass.
+constexpr int kHwtThreads = 512;
+
+__global__ void __launch_bounds__(kHwtThreads) k_sample_hwt(uint64_t* out, uint32_t L, uint32_t log_n, uint32_t cm0,
+                                                           const DevMod* __restrict__ mods, uint64_t seed, uint32_t h) {
+  __shared__ uint32_t hist[256];
+  __shared__ uint64_t prefix_s;
+  __shared__ uint32_t need_s;
+  const uint32_t n = 1u << log_n;
+  const uint64_t poly = blockIdx.x;
+  const uint64_t kbase = poly << log_n;
+  const uint64_t kseed = seed ^ kSeedPositions;
+  uint64_t prefix = 0;  // selected high digits of the threshold key
+  uint32_t need = h;    // how many keys below the threshold are still to take
+  for (int shift = 56; shift >= 0; shift -= 8) {
+    for (uint32_t t = threadIdx.x; t < 256; t += blockDim.x) hist[t] = 0;
+    __syncthreads();
+    const uint64_t hi_mask = shift == 56 ? 0ull : (~0ull << (shift + 8));
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const uint64_t key = rand_word(kseed, kbase + i);
+      if ((key & hi_mask) == prefix) atomicAdd(&hist[(key >> shift) & 0xFF], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t acc = 0, d = 0;
+      for (; d < 256; ++d) {
+        if (acc + hist[d] >= need) break;
+        acc += hist[d];
+      }
+      prefix_s = prefix | ((uint64_t)d << shift);
+      need_s = need - acc;
+    }
+    __syncthreads();
+    prefix = prefix_s;
+    need = need_s;
+    __syncthreads();
+  }
+  // prefix is now the key of rank h (1-based): take keys < prefix, plus `need`
+  // keys equal to it (64-bit keys of distinct counters: ties do not occur in
+  // practice, and the first ones by index are taken if they do).
+  const uint64_t sseed = seed ^ kSeedSigns;
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const uint64_t key = rand_word(kseed, kbase + i);
+    bool take = key < prefix;
+    if (key == prefix) {
+      // rank among equal keys by index (rare path)
+      uint32_t before = 0;
+      for (uint32_t j = 0; j < i; ++j) before += rand_word(kseed, kbase + j) == prefix;
+      take = before < need;
+    }
+    const bool plus = (rand_word(sseed, kbase + i) & 2) != 0;
+    for (uint32_t l = 0; l < L; ++l) {
+      const uint64_t p = __ldg(&mods[cm0 + l].p);
+      out[(((poly * L) + l) << log_n) + i] = take ? (plus ? 1ull : p - 1) : 0ull;
+    }
+  }
+}
+
+int grid_for(size_t items) {
+  const size_t g = (items + 255) / 256;
+  return (int)(g < 152 * 16 ? (g ? g : 1) : 152 * 16);
+}
+
+// Cumulative table of P(e) ~ exp(-e^2 / 2 sigma^2) on |e| <= tail, scaled to
+// 64-bit thresholds (the last one is 2^64 - 1).
+std::vector<uint64_t> gaussian_cdt(double sigma, int tail) {
+  std::vector<long double> w;
+  long double sum = 0;
+  for (int e = -tail; e <= tail; ++e) {
+    const long double v = std::exp(-(long double)e * e / (2.0L * sigma * sigma));
+    w.push_back(v);
+    sum += v;
+  }
+  std::vector<uint64_t> cdt;
+  long double acc = 0;
+  for (size_t i = 0; i < w.size(); ++i) {
+    acc += w[i];
+    long double t = std::floor(acc / sum * 18446744073709551616.0L);
+    cdt.push_back(t >= 18446744073709551615.0L ? ~0ull : (uint64_t)t);
+  }
+  cdt.back() = ~0ull;
+  return cdt;
+}
+
+constexpr uint32_t kMaxGaussianTail = 1024;
+
+// Device copies of the cumulative tables, one per (device, sigma, tail), built
+// on first use and kept for the life of the process (a few KB each).
+int gaussian_table(int device, double sigma, uint32_t tail, const uint64_t** out, uint32_t* len) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, uint64_t, uint32_t>, std::pair<uint64_t*, uint32_t>> tables;
+  uint64_t sigma_bits;
+  std::memcpy(&sigma_bits, &sigma, sizeof sigma_bits);
+  const auto key = std::make_tuple(device, sigma_bits, tail);
+  std::lock_guard<std::mutex> g(mu);
+  auto it = tables.find(key);
+  if (it == tables.end()) {
+    const std::vector<uint64_t> cdt = gaussian_cdt(sigma, (int)tail);
+    uint64_t* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, cdt.size() * sizeof(uint64_t));
+    if (e != cudaSuccess) return fail_cuda(e, "cudaMalloc(gaussian table)");
+    e = cudaMemcpy(d, cdt.data(), cdt.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(d);
+      return fail_cuda(e, "upload gaussian table");
+    }
+    it = tables.emplace(key, std::make_pair(d, (uint32_t)cdt.size())).first;
+  }
+  *out = it->second.first;
+  *len = it->second.second;
+  return kOk;
+}
+
+struct SamplerArgs {
+  DeviceContext* ctx = nullptr;
+  const DevMod* mods = nullptr;
+  cudaStream_t st = nullptr;
+};
+
+int prepare(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0, void* stream,
+            SamplerArgs* a) {
+  if (!d_out || count == 0) return fail(kInvalidArgument, "null output or zero count");
+  int st = check_degree(log_n);
+  if (st != kOk) return st;
+  st = check_moduli(cm0, L);
+  if (st != kOk) return st;
+  a->ctx = DeviceContext::current(&st);
+  if (!a->ctx) return st;
+  st = a->ctx->ensure_tables(log_n, cm0, L, &a->mods);
+  if (st != kOk) return st;
+  a->st = stream ? static_cast<cudaStream_t>(stream) : a->ctx->stream();
+  return kOk;
+}
+
+}  // namespace
+
+extern "C" {
+
+int yell_dev_sample_uniform(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
+                            uint64_t seed, void* stream) {
+  SamplerArgs a;
+  int st = prepare(d_out, count, L, log_n, cm0, stream, &a);
+  if (st != kOk) return st;
+  LaunchScope ps("sample_uniform", a.st);
+  k_sample_uniform<<<grid_for(((size_t)count * L) << log_n), 256, 0, a.st>>>(d_out, count, L, log_n, cm0,
+                                                                            a.mods, seed);
+  g_kernel_launches += 1;
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? kOk : fail_cuda(e, "sample_uniform");
+}
+
+int yell_dev_sample_zo(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
+                       uint32_t rho, uint64_t seed, void* stream) {
+  if (rho > 255) return fail(kInvalidArgument, "rho must be a byte (0..255)");
+  SamplerArgs a;
+  int st = prepare(d_out, count, L, log_n, cm0, stream, &a);
+  if (st != kOk) return st;
+  LaunchScope ps("sample_zo", a.st);
+  k_sample_shared_int<<<grid_for((size_t)count << log_n), 256, 0, a.st>>>(d_out, count, L, log_n, cm0, a.mods,
+                                                                         seed, 0, rho, nullptr, 0, 0, 1);
+  g_kernel_launches += 1;
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? kOk : fail_cuda(e, "sample_zo");
+}
+
+int yell_dev_sample_hwt(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
+                        uint32_t h, uint64_t seed, void* stream) {
+  if (h == 0 || h > (1u << log_n)) return fail(kInvalidArgument, "hamming weight must be in [1, N]");
+  SamplerArgs a;
+  int st = prepare(d_out, count, L, log_n, cm0, stream, &a);
+  if (st != kOk) return st;
+  LaunchScope ps("sample_hwt", a.st);
+  k_sample_hwt<<<count, kHwtThreads, 0, a.st>>>(d_out, L, log_n, cm0, a.mods, seed, h);
+  g_kernel_launches += 1;
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? kOk : fail_cuda(e, "sample_hwt");
+}
+
+int yell_dev_sample_gaussian(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
+                             double sigma, uint32_t tail, uint64_t amplifier, uint64_t seed, void* stream) {
+  if (!(sigma > 0) || !(sigma < 1e6) || tail == 0 || tail > kMaxGaussianTail)
+    return fail(kInvalidArgument, "need 0 < sigma < 1e6 and 0 < tail <= 1024");
+  if (amplifier == 0 || (unsigned __int128)tail * amplifier >= (1ull << 61))
+    return fail(kInvalidArgument, "tail * amplifier must be below 2^61 (below every modulus)");
+  SamplerArgs a;
+  int st = prepare(d_out, count, L, log_n, cm0, stream, &a);
+  if (st != kOk) return st;
+  const uint64_t* cdt = nullptr;
+  uint32_t len = 0;
+  st = gaussian_table(a.ctx->device(), sigma, tail, &cdt, &len);
+  if (st != kOk) return st;
+  LaunchScope ps("sample_gaussian", a.st);
+  k_sample_shared_int<<<grid_for((size_t)count << log_n), 256, 0, a.st>>>(
+      d_out, count, L, log_n, cm0, a.mods, seed, 1, 0, cdt, len, (int32_t)tail, amplifier);
+  g_kernel_launches += 1;
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? kOk : fail_cuda(e, "sample_gaussian");
+}
+
+}  // extern "C"
