@@ -232,6 +232,37 @@ int yell_server_get_stats(yell_server* s, int reset, yell_server_stats* out);
 int yell_server_load_test(yell_server* s, const yell_polymul_request* templates, uint32_t n,
                           double offered_rps, double duration_s, uint64_t seed, yell_server_stats* out);
 
+/* ---- device-resident poly handles (the device-side poly<N>) -------------
+ * A handle owns one poly in HBM: L limbs of N words, limb l under prime
+ * cm0 + l (the reference's poly<N>(nmoduli) uses cm0 = 0;
+ * include/yell/poly.hpp:43-121).  upload / download take L host limb
+ * pointers like raw_data() and are synchronous; every other call is ordered
+ * on the device's library stream.  Handles in one call must agree in N, L and
+ * cm0. */
+typedef struct yell_dev_poly yell_dev_poly;
+int yell_dev_poly_alloc(uint32_t L, uint32_t log_n, uint32_t cm0, yell_dev_poly** out);
+int yell_dev_poly_free(yell_dev_poly* p);
+int yell_dev_poly_info(const yell_dev_poly* p, uint64_t** d_data, uint32_t* L, uint32_t* log_n, uint32_t* cm0);
+int yell_dev_poly_upload(yell_dev_poly* p, const uint64_t* const* limbs);
+int yell_dev_poly_download(const yell_dev_poly* p, uint64_t* const* limbs);
+/* poly<N>::forward / forward_lazy / backward (details/poly.hpp:170-186) */
+int yell_dev_poly_ntt(yell_dev_poly* p, int direction);
+/* dst = a op b with op a yell_elementwise_op: operator* + - and their
+ * assigning forms (dst may be a), add_product_of (MULADD), negate (b NULL) */
+int yell_dev_poly_op(int op, yell_dev_poly* dst, const yell_dev_poly* a, const yell_dev_poly* b);
+/* c = a * b in Z_Q[X]/(X^N + 1): forward, mulmod, backward fused; c is not a or b */
+int yell_dev_poly_mul(yell_dev_poly* c, const yell_dev_poly* a, const yell_dev_poly* b);
+/* Asynchronous batch of n products c[i] = a[i] * b[i] of any mix of sizes
+ * (run as yell_dev_polymul_batch); the ticket completes with the batch.
+ * yell_batch_wait returns YELL_ERR_TIMEOUT after timeout_s (the ticket stays
+ * valid) and frees the ticket otherwise; yell_batch_release drops a ticket
+ * without waiting. */
+typedef struct yell_batch yell_batch;
+int yell_batch_submit(yell_dev_poly* const* c, const yell_dev_poly* const* a, const yell_dev_poly* const* b,
+                      uint32_t n, yell_batch** ticket);
+int yell_batch_wait(yell_batch* t, double timeout_s);
+int yell_batch_release(yell_batch* t);
+
 /* ---- seeded device samplers: replace poly<N>::set(uniform / ZO_dist / hwt_dist /
  * gaussian) (include/yell/details/poly.hpp:195-330) -------------------------
  * Fill `count` polys (count, L, N) on the device.  The reference's samplers

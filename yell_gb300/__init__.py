@@ -25,7 +25,8 @@ __all__ = [
     "poly_submod", "poly_add_product_of", "poly_negate", "polymul_host", "dev_ntt",
     "dev_ntt_limbs", "dev_elementwise", "dev_polymul", "polymul_scratch_words", "kernel_launches",
     "Poly", "PinnedBuffer", "sample_uniform", "sample_zo", "sample_hwt", "sample_gaussian",
-    "crt_words", "dev_crt_lift", "poly_to_bigint", "words_to_ints",
+    "crt_words", "dev_crt_lift", "poly_to_bigint", "words_to_ints", "DevPoly", "BatchTicket",
+    "batch_submit",
 ]
 
 
@@ -427,3 +428,110 @@ class Poly:
 
     def array(self) -> np.ndarray:
         return np.stack(self.limbs)
+
+
+class DevPoly:
+    """A poly kept in HBM (yell_dev_poly handle): L limbs of N words, limb l
+    under prime cm0 + l.  upload/download move host limbs synchronously; the
+    other methods queue work on the device's library stream."""
+
+    def __init__(self, log_n: int, L: int, cm0: int = 0, limbs=None):
+        h = ctypes.c_void_p()
+        call("yell_dev_poly_alloc", L, log_n, cm0, ctypes.byref(h))
+        self._h = h
+        self.log_n, self.L, self.cm0 = log_n, L, cm0
+        if limbs is not None:
+            self.upload(limbs)
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        if self._h is None:
+            raise YellError(1, "DevPoly", "poly handle already freed")
+        return self._h
+
+    def data_ptr(self) -> int:
+        d = ctypes.c_void_p()
+        call("yell_dev_poly_info", self.handle, ctypes.byref(d), None, None, None)
+        return int(d.value)
+
+    def upload(self, limbs) -> "DevPoly":
+        ls = [_u64(x) for x in limbs]
+        if len(ls) != self.L or any(x.size != 1 << self.log_n for x in ls):
+            raise ValueError("limb count or size does not match the handle")
+        call("yell_dev_poly_upload", self.handle, _ptr_array(ls))
+        return self
+
+    def download(self) -> np.ndarray:
+        out = np.zeros((self.L, 1 << self.log_n), dtype=np.uint64)
+        call("yell_dev_poly_download", self.handle, _ptr_array(list(out)))
+        return out
+
+    def forward(self) -> "DevPoly":
+        call("yell_dev_poly_ntt", self.handle, YELL_FORWARD)
+        return self
+
+    def forward_lazy(self) -> "DevPoly":
+        call("yell_dev_poly_ntt", self.handle, YELL_FORWARD_LAZY)
+        return self
+
+    def backward(self) -> "DevPoly":
+        call("yell_dev_poly_ntt", self.handle, YELL_BACKWARD)
+        return self
+
+    def op(self, code: int, a: "DevPoly", b: "DevPoly | None" = None) -> "DevPoly":
+        """self = a op b (YELL_OP_*); MULADD accumulates into self."""
+        call("yell_dev_poly_op", code, self.handle, a.handle, b.handle if b is not None else None)
+        return self
+
+    def add_product_of(self, a: "DevPoly", b: "DevPoly") -> "DevPoly":
+        return self.op(YELL_OP_MULADD, a, b)
+
+    def negate(self) -> "DevPoly":
+        return self.op(YELL_OP_NEGATE, self)
+
+    def mul(self, a: "DevPoly", b: "DevPoly") -> "DevPoly":
+        """self = a * b (negacyclic product of coefficient-domain polys)."""
+        call("yell_dev_poly_mul", self.handle, a.handle, b.handle)
+        return self
+
+    def free(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            call("yell_dev_poly_free", self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class BatchTicket:
+    """Completion of an asynchronous yell_batch_submit."""
+
+    def __init__(self, c, a, b):
+        n = len(c)
+        arr = ctypes.c_void_p * n
+        t = ctypes.c_void_p()
+        call("yell_batch_submit", arr(*[x.handle for x in c]), arr(*[x.handle for x in a]),
+             arr(*[x.handle for x in b]), n, ctypes.byref(t))
+        self._t = t
+        self._keep = (c, a, b)  # the handles outlive the batch
+
+    def wait(self, timeout_s: float = 60.0) -> None:
+        if self._t is None:
+            return
+        call("yell_batch_wait", self._t, timeout_s)
+        self._t = None
+        self._keep = None
+
+    def __del__(self):
+        if getattr(self, "_t", None) is not None:
+            try:
+                load().yell_batch_release(self._t)
+            except Exception:
+                pass
+
+
+def batch_submit(c, a, b) -> BatchTicket:
+    return BatchTicket(list(c), list(a), list(b))

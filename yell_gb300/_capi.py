@@ -89,6 +89,17 @@ SIGNATURES = {
     "yell_dev_polymul_noalloc": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),
     "yell_dev_polymul_batch": (_int, [_vp, _u32, _vp]),
     "yell_calibrate_butterflies": (_int, [_vp, _vp]),
+    "yell_dev_poly_alloc": (_int, [_u32, _u32, _u32, _vp]),
+    "yell_dev_poly_free": (_int, [_vp]),
+    "yell_dev_poly_info": (_int, [_vp, _vp, _vp, _vp, _vp]),
+    "yell_dev_poly_upload": (_int, [_vp, _vp]),
+    "yell_dev_poly_download": (_int, [_vp, _vp]),
+    "yell_dev_poly_ntt": (_int, [_vp, ctypes.c_int]),
+    "yell_dev_poly_op": (_int, [ctypes.c_int, _vp, _vp, _vp]),
+    "yell_dev_poly_mul": (_int, [_vp, _vp, _vp]),
+    "yell_batch_submit": (_int, [_vp, _vp, _vp, _u32, _vp]),
+    "yell_batch_wait": (_int, [_vp, ctypes.c_double]),
+    "yell_batch_release": (_int, [_vp]),
     "yell_crt_words": (_int, [_u32, _u32, _vp]),
     "yell_dev_crt_lift": (_int, [_vp, _vp, _u32, _u32, _u32, _u32, _vp]),
     "yell_poly_to_bigint": (_int, [_vp, _vp, _u32, _u32]),
