@@ -232,6 +232,30 @@ int yell_server_get_stats(yell_server* s, int reset, yell_server_stats* out);
 int yell_server_load_test(yell_server* s, const yell_polymul_request* templates, uint32_t n,
                           double offered_rps, double duration_s, uint64_t seed, yell_server_stats* out);
 
+/* ---- 32-bit moduli mode: the reference built with -DYELL_USE_32BITS_MODULI
+ * (include/yell/params.hpp:2-6, params_32.hpp:15-34): 291 30-bit primes
+ * p = 1 mod 2^16, uint32 words, uint64 products, N = 2^3 .. 2^15.  Same call
+ * meanings as the 64-bit functions above with uint32_t words; modulus
+ * indices address the 32-bit prime table. ---------------------------------- */
+uint32_t yell32_max_moduli(void);      /* kMaxNbModuli = 291 */
+uint32_t yell32_max_log_degree(void);  /* log2 kMaxPolyDegree = 15 */
+uint32_t yell32_prime(uint32_t cm);          /* params::P[cm] */
+uint32_t yell32_prime_pn(uint32_t cm);       /* params::Pn[cm] */
+uint32_t yell32_primitive_root(uint32_t cm); /* params::primitive_roots[cm], order 2^16 */
+int yell32_ntt_tables(uint32_t log_n, uint32_t cm, uint32_t* out4n, uint32_t* scalars4);
+int yell32_init_ntt_tables(uint32_t log_n, uint32_t cm0, uint32_t L);
+/* ntt<N>::forward / forward_lazy / backward (include/yell/ntt.hpp:59-65) */
+int yell32_ntt_forward(uint32_t* op, uint32_t log_n, uint32_t cm);
+int yell32_ntt_forward_lazy(uint32_t* op, uint32_t log_n, uint32_t cm);
+int yell32_ntt_backward(uint32_t* op, uint32_t log_n, uint32_t cm);
+/* device batches laid out (count, L, N) uint32, 16-byte aligned */
+int yell32_dev_ntt(uint32_t* d_polys, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
+                   int direction, void* stream);
+int yell32_dev_polymul(uint32_t* d_c, const uint32_t* d_a, const uint32_t* d_b, uint32_t pairs,
+                       uint32_t L, uint32_t log_n, uint32_t cm0, void* stream);
+int yell32_dev_elementwise(int op, uint32_t* d_dst, const uint32_t* d_a, const uint32_t* d_b,
+                           uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0, void* stream);
+
 /* ---- device-resident poly handles (the device-side poly<N>) -------------
  * A handle owns one poly in HBM: L limbs of N words, limb l under prime
  * cm0 + l (the reference's poly<N>(nmoduli) uses cm0 = 0;

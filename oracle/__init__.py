@@ -11,8 +11,12 @@ Two CPU implementations are exposed through ctypes:
   ``include/yell/details/ntt.hpp``), built by ``oracle/Makefile``.
   ``samplers_oracle.c`` restates the reference's sampler rules
   (``include/yell/details/poly.hpp:195-330``) over the seeded counter stream.
+  ``yell_oracle32.c`` restates the reference's 32-bit moduli mode
+  (``-DYELL_USE_32BITS_MODULI``, ``include/yell/params_32.hpp``).
 * ``crt.py``: pure-Python big-integer restatement of ``gmp::poly2mpz``
   (``include/yell/gmp.hpp:42-70``, ``lib/gmp.cpp:6-51``).
+* ``Oracle32``: the 32-bit mode, ``port`` from ``liboracle.so`` or ``ref``
+  from ``_ref/libyellref32.so`` (the reference's sources compiled in that mode).
 * ``ref``: ``_ref/libyellref.so``, the reference's own sources compiled
   unmodified with ``ref_harness.cpp``; present only where the reference
   checkout was available to build it (``ref_available()``).
@@ -27,6 +31,7 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _U64P = ctypes.POINTER(ctypes.c_uint64)
+_U32P = ctypes.POINTER(ctypes.c_uint32)
 _port = None
 _ref = None
 
@@ -65,6 +70,20 @@ def _bind(lib, prefix: str):
             "polymul": (ctypes.c_int, [_U64P, _U64P, _U64P, u32, u32, u32]),
             "polymul_batch": (ctypes.c_double, [_U64P, _U64P, _U64P, u32, u32, u32, u32, u32]),
             "sample_uniform": (None, [_U64P, u32, u32, u32, u32, u64]),
+            "32_prime": (u32, [u32]),
+            "32_pn": (u32, [u32]),
+            "32_primitive_root": (u32, [u32]),
+            "32_ntt_tables": (ctypes.c_int, [u32, u32, _U32P, _U32P]),
+            "32_forward": (ctypes.c_int, [_U32P, u32, u32]),
+            "32_forward_lazy": (ctypes.c_int, [_U32P, u32, u32]),
+            "32_backward": (ctypes.c_int, [_U32P, u32, u32]),
+            "32_barrett": (u32, [u64, u32]),
+            "32_mulmod_n": (None, [_U32P, _U32P, _U32P, sz, u32]),
+            "32_addmod_n": (None, [_U32P, _U32P, _U32P, sz, u32]),
+            "32_submod_n": (None, [_U32P, _U32P, _U32P, sz, u32]),
+            "32_muladd_n": (None, [_U32P, _U32P, _U32P, sz, u32]),
+            "32_negate_n": (None, [_U32P, sz, u32]),
+            "32_polymul": (ctypes.c_int, [_U32P, _U32P, _U32P, u32, u32, u32]),
             "sample_zo": (None, [_U64P, u32, u32, u32, u32, u32, u64]),
             "sample_hwt": (ctypes.c_int, [_U64P, u32, u32, u32, u32, u32, u64]),
             "gaussian_cdt": (u32, [ctypes.c_double, u32, _U64P]),
@@ -73,7 +92,8 @@ def _bind(lib, prefix: str):
     else:
         sig["polymul_batch"] = (ctypes.c_double, [_U64P, _U64P, _U64P, u32, u32, u32, u32])
     for name, (res, args) in sig.items():
-        fn = getattr(lib, prefix + name)
+        # "32_x" entries are the 32-bit mode's orc32_x functions
+        fn = getattr(lib, (prefix[:-1] + name) if name.startswith("32_") else prefix + name)
         fn.restype = res
         fn.argtypes = args
     return lib
@@ -281,3 +301,135 @@ class Oracle:
         self.lib.orc_sample_gaussian(_ptr(out), count, L, log_n, cm0, _ptr(cdt), len(cdt), tail,
                                      amplifier, seed)
         return out
+
+
+def ref32_available() -> bool:
+    return os.path.exists(os.path.join(_HERE, "_ref", "libyellref32.so"))
+
+
+def _ptr32(a: np.ndarray):
+    assert a.dtype == np.uint32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_U32P)
+
+
+_ref32 = None
+
+
+def _load_ref32():
+    global _ref32
+    if _ref32 is None:
+        lib = ctypes.CDLL(os.path.join(_HERE, "_ref", "libyellref32.so"))
+        u32, u64, sz = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_size_t
+        sig = {
+            "prime": (u32, [u32]), "pn": (u32, [u32]), "primitive_root": (u32, [u32]),
+            "ntt_tables": (ctypes.c_int, [u32, u32, _U32P, _U32P]),
+            "forward": (ctypes.c_int, [_U32P, u32, u32]),
+            "forward_lazy": (ctypes.c_int, [_U32P, u32, u32]),
+            "backward": (ctypes.c_int, [_U32P, u32, u32]),
+            "barrett": (u32, [u64, u32]),
+            "mulmod_n": (None, [_U32P, _U32P, _U32P, sz, u32]),
+            "addmod_n": (None, [_U32P, _U32P, _U32P, sz, u32]),
+            "submod_n": (None, [_U32P, _U32P, _U32P, sz, u32]),
+            "muladd_n": (None, [_U32P, _U32P, _U32P, sz, u32]),
+            "polymul_batch": (ctypes.c_double, [_U32P, _U32P, _U32P, u32, u32, u32, u32]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, "ref32_" + name)
+            fn.restype = res
+            fn.argtypes = args
+        _ref32 = lib
+    return _ref32
+
+
+class Oracle32:
+    """32-bit moduli mode; ``which`` is "port" (yell_oracle32.c) or "ref"."""
+
+    def __init__(self, which: str = "port"):
+        self.which = which
+        if which == "port":
+            self.lib, self.pre = _load_port(), "orc32_"
+        else:
+            self.lib, self.pre = _load_ref32(), "ref32_"
+
+    def _f(self, name):
+        return getattr(self.lib, self.pre + name)
+
+    def prime(self, cm):
+        return int(self._f("prime")(cm))
+
+    def pn(self, cm):
+        return int(self._f("pn")(cm))
+
+    def primitive_root(self, cm):
+        return int(self._f("primitive_root")(cm))
+
+    def _ntt(self, name, x, log_n, cm):
+        a = np.ascontiguousarray(x, dtype=np.uint32).copy()
+        if self._f(name)(_ptr32(a), log_n, cm) != 0:
+            raise ValueError(f"{name}: bad arguments")
+        return a
+
+    def forward(self, x, log_n, cm):
+        return self._ntt("forward", x, log_n, cm)
+
+    def forward_lazy(self, x, log_n, cm):
+        return self._ntt("forward_lazy", x, log_n, cm)
+
+    def backward(self, x, log_n, cm):
+        return self._ntt("backward", x, log_n, cm)
+
+    def tables(self, log_n, cm):
+        n = 1 << log_n
+        out = np.zeros(4 * n, dtype=np.uint32)
+        sc = np.zeros(4, dtype=np.uint32)
+        if self._f("ntt_tables")(log_n, cm, _ptr32(out), _ptr32(sc)) != 0:
+            raise ValueError("ntt_tables: bad arguments")
+        return out.reshape(4, n), sc
+
+    def barrett(self, x, cm):
+        return int(self._f("barrett")(x, cm))
+
+    def _ew(self, name, a, b, cm):
+        a = np.ascontiguousarray(a, dtype=np.uint32)
+        b = np.ascontiguousarray(b, dtype=np.uint32)
+        d = np.zeros_like(a)
+        self._f(name)(_ptr32(d), _ptr32(a), _ptr32(b), a.size, cm)
+        return d
+
+    def mulmod(self, a, b, cm):
+        return self._ew("mulmod_n", a, b, cm)
+
+    def addmod(self, a, b, cm):
+        return self._ew("addmod_n", a, b, cm)
+
+    def submod(self, a, b, cm):
+        return self._ew("submod_n", a, b, cm)
+
+    def muladd(self, rop, a, b, cm):
+        r = np.ascontiguousarray(rop, dtype=np.uint32).copy()
+        a = np.ascontiguousarray(a, dtype=np.uint32)
+        b = np.ascontiguousarray(b, dtype=np.uint32)
+        self._f("muladd_n")(_ptr32(r), _ptr32(a), _ptr32(b), r.size, cm)
+        return r
+
+    def negate(self, a, cm):
+        assert self.which == "port"
+        r = np.ascontiguousarray(a, dtype=np.uint32).copy()
+        self.lib.orc32_negate_n(_ptr32(r), r.size, cm)
+        return r
+
+    def polymul(self, a, b, log_n, cm0=0):
+        """(L, N) polys, limb l under cm0 + l."""
+        n = 1 << log_n
+        a = np.ascontiguousarray(a, dtype=np.uint32).reshape(-1, n)
+        b = np.ascontiguousarray(b, dtype=np.uint32).reshape(-1, n)
+        if self.which == "port":
+            c = np.zeros_like(a)
+            if self.lib.orc32_polymul(_ptr32(c), _ptr32(a), _ptr32(b), a.shape[0], log_n, cm0) != 0:
+                raise ValueError("polymul: bad arguments")
+            return c
+        out = []
+        for l in range(a.shape[0]):
+            fa, fb = self.forward(a[l], log_n, cm0 + l), self.forward(b[l], log_n, cm0 + l)
+            out.append(self.backward(self.mulmod(fa, fb, cm0 + l), log_n, cm0 + l))
+        return np.stack(out)

@@ -13,7 +13,7 @@ import ctypes
 
 import numpy as np
 
-from . import _capi
+from . import _capi, moduli32
 from ._capi import (YELL_BACKWARD, YELL_FORWARD, YELL_FORWARD_LAZY, YELL_OP_ADDMOD,
                     YELL_OP_MULADD, YELL_OP_MULMOD, YELL_OP_NEGATE, YELL_OP_SUBMOD, YellError,
                     call, load)

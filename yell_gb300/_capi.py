@@ -89,6 +89,19 @@ SIGNATURES = {
     "yell_dev_polymul_noalloc": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),
     "yell_dev_polymul_batch": (_int, [_vp, _u32, _vp]),
     "yell_calibrate_butterflies": (_int, [_vp, _vp]),
+    "yell32_max_moduli": (_u32, []),
+    "yell32_max_log_degree": (_u32, []),
+    "yell32_prime": (_u32, [_u32]),
+    "yell32_prime_pn": (_u32, [_u32]),
+    "yell32_primitive_root": (_u32, [_u32]),
+    "yell32_ntt_tables": (_int, [_u32, _u32, _vp, _vp]),
+    "yell32_init_ntt_tables": (_int, [_u32, _u32, _u32]),
+    "yell32_ntt_forward": (_int, [_vp, _u32, _u32]),
+    "yell32_ntt_forward_lazy": (_int, [_vp, _u32, _u32]),
+    "yell32_ntt_backward": (_int, [_vp, _u32, _u32]),
+    "yell32_dev_ntt": (_int, [_vp, _u32, _u32, _u32, _u32, _int, _vp]),
+    "yell32_dev_polymul": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),
+    "yell32_dev_elementwise": (_int, [_int, _vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),
     "yell_dev_poly_alloc": (_int, [_u32, _u32, _u32, _vp]),
     "yell_dev_poly_free": (_int, [_vp]),
     "yell_dev_poly_info": (_int, [_vp, _vp, _vp, _vp, _vp]),

@@ -199,4 +199,89 @@ __device__ __forceinline__ uint64_t submod(uint64_t x, uint64_t y, uint64_t p) {
   return (x >= p) ? x - p : x;
 }
 
+// ---------------------------------------------------------------------------
+// 32-bit moduli mode (include/yell/params_32.hpp: 30-bit primes, uint32
+// words, uint64 products).  The reference runs the same generic code with
+// bit_width = 32; the functions below are those formulas at 32-bit words.
+// ---------------------------------------------------------------------------
+
+// Per-(log_n, cm) constants of a 32-bit modulus; fwd/inv point at N {w, w'}
+// pairs, bit-reversed, w' = floor(w * 2^32 / p).
+struct alignas(16) DevMod32 {
+  const uint2* fwd;
+  const uint2* inv;
+  uint32_t p;
+  uint32_t pn;  // low word of floor(2^64/p) (params_32.hpp Pn)
+  uint32_t inv_n, inv_n_s;
+  uint32_t inv_n_iphi, inv_n_iphi_s;
+};
+
+// u >= m ? u - m : u for 0 < m: u - m wraps above u exactly when u < m.
+__device__ __forceinline__ uint32_t csub(uint32_t u, uint32_t m) { return min(u, u - m); }
+
+// x*w - hi32(x*w')*p (mod 2^32), in [0, 2p); np = 2^32 - p.
+__device__ __forceinline__ uint32_t shoup_lazy(uint32_t x, uint32_t w, uint32_t wp, uint32_t np) {
+  return x * w + __umulhi(x, wp) * np;
+}
+
+__device__ __forceinline__ void ct_bfly(uint32_t& x0, uint32_t& x1, uint32_t w, uint32_t wp, uint32_t np,
+                                        uint32_t p2) {
+  const uint32_t u0 = csub(x0, p2);
+  const uint32_t t = shoup_lazy(x1, w, wp, np);
+  x0 = u0 + t;
+  x1 = u0 - t + p2;
+}
+
+__device__ __forceinline__ void gs_bfly(uint32_t& x0, uint32_t& x1, uint32_t w, uint32_t wp, uint32_t np,
+                                        uint32_t p2) {
+  const uint32_t u0 = x0, u1 = x1;
+  const uint32_t t1 = u0 - u1 + p2;
+  x0 = csub(u0 + u1, p2);
+  x1 = shoup_lazy(t1, w, wp, np);
+}
+
+__device__ __forceinline__ uint32_t mulmod_shoup(uint32_t x, uint32_t y, uint32_t yp, uint32_t p) {
+  return csub(shoup_lazy(x, y, yp, 0u - p), p);
+}
+
+__device__ __forceinline__ void gs_last(uint32_t& x0, uint32_t& x1, const DevMod32& m) {
+  const uint32_t u = x0, v = x1;
+  x0 = mulmod_shoup(u + v, m.inv_n, m.inv_n_s, m.p);
+  x1 = mulmod_shoup(u - v + (m.p << 1), m.inv_n_iphi, m.inv_n_iphi_s, m.p);
+}
+
+__device__ __forceinline__ uint32_t fwd_correct(uint32_t v, uint32_t p, uint32_t p2) {
+  return csub(csub(v, p2), p);
+}
+
+// lib/ops.cpp:5-21 at shift 32, delta 2: q = Pn*(x >> 32) + (x << 2)
+// (mod 2^64); r = lo32(x) - hi32(q)*p (mod 2^32); one correction.
+__device__ __forceinline__ uint32_t barrett64(uint64_t x, uint32_t p, uint32_t pn) {
+  const uint64_t q = (uint64_t)pn * (x >> 32) + (x << 2);
+  return csub((uint32_t)x - (uint32_t)(q >> 32) * p, p);
+}
+
+__device__ __forceinline__ uint32_t mulmod_barrett(uint32_t x, uint32_t y, uint32_t p, uint32_t pn) {
+  return barrett64((uint64_t)x * y, p, pn);
+}
+
+__device__ __forceinline__ uint32_t muladd_barrett(uint32_t rop, uint32_t x, uint32_t y, uint32_t p,
+                                                   uint32_t pn) {
+  return barrett64((uint64_t)x * y + rop, p, pn);
+}
+
+__device__ __forceinline__ uint32_t addmod(uint32_t x, uint32_t y, uint32_t p) { return csub(x + y, p); }
+__device__ __forceinline__ uint32_t submod(uint32_t x, uint32_t y, uint32_t p) { return csub(x + (p - y), p); }
+
+// Twiddle pair type of a word type.
+template <class W> struct PairOf;
+template <> struct PairOf<uint64_t> {
+  using type = ulonglong2;
+  __device__ static __forceinline__ type make(uint64_t a, uint64_t b) { return make_ulonglong2(a, b); }
+};
+template <> struct PairOf<uint32_t> {
+  using type = uint2;
+  __device__ static __forceinline__ type make(uint32_t a, uint32_t b) { return make_uint2(a, b); }
+};
+
 }  // namespace yell_gb300

@@ -1,0 +1,515 @@
+// 32-bit moduli mode of the hot path (the reference built with
+// -DYELL_USE_32BITS_MODULI: include/yell/params_32.hpp, 291 30-bit primes,
+// uint32 words and uint64 products, degrees up to kMaxPolyDegree = 2^15).
+//
+// The kernels reuse the tile engine of the 64-bit path at 32-bit words.  A CTA
+// holds whole limbs in shared memory (2^T words, T = max(log_n, 11), several
+// limbs per CTA below 2^11); every word is read from HBM once and written
+// once.  The fused polymul keeps one operand tile in shared memory at a time:
+// NTT(a) leaves its last forward round in registers and parks the reduced
+// words in the output limb (the same thread reads them back, so they stay in
+// L2), NTT(b) then runs in the same buffer, and the product, inverse rounds
+// and scaled last layer follow.  The butterflies, their order and their
+// twiddle indices are the reference's, so lazy words match it exactly.
+#include <algorithm>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "kernels.h"
+#include "ntt_tile.cuh"
+#include "profiler.h"
+#include "runtime.h"
+#include "yell_gb300.h"
+
+namespace yell_gb300 {
+namespace {
+
+constexpr uint32_t kMaxModuli32 = 291;   // params_32.hpp kMaxNbModuli
+constexpr uint32_t kLogMaxDegree32 = 15; // kMaxPolyDegree = 2^15
+constexpr uint32_t kMinLogN32 = 3;
+
+// ---- prime table -------------------------------------------------------------
+// params_32.hpp:15-34: p = 2^30 - j * 2^16 + 1 for increasing j, kept when
+// prime (the stated 2^14 step, restricted to p = 1 mod 2^16 so that a
+// primitive 2^16-th root exists); Pn = low word of floor(2^64 / p);
+// primitive_roots[cm] = g^((p - 1) / 2^16), g the least primitive root.
+struct Prime32 {
+  uint32_t p, pn, root;
+};
+
+uint32_t pow32(uint64_t b, uint64_t e, uint32_t m) {
+  uint64_t r = 1;
+  b %= m;
+  while (e) {
+    if (e & 1) r = r * b % m;
+    b = b * b % m;
+    e >>= 1;
+  }
+  return (uint32_t)r;
+}
+
+bool is_prime32(uint32_t n) {
+  if (n < 2) return false;
+  for (uint32_t q : {2u, 7u, 61u})
+    if (n % q == 0) return n == q;
+  uint32_t d = n - 1;
+  int s = 0;
+  while (!(d & 1)) d >>= 1, ++s;
+  for (uint32_t a : {2u, 7u, 61u}) {
+    uint64_t x = pow32(a, d, n);
+    if (x == 1 || x == n - 1) continue;
+    bool comp = true;
+    for (int r = 1; r < s && comp; ++r) {
+      x = x * x % n;
+      if (x == n - 1) comp = false;
+    }
+    if (comp) return false;
+  }
+  return true;
+}
+
+uint32_t least_primitive_root32(uint32_t p) {
+  std::vector<uint32_t> f;
+  uint32_t m = p - 1;
+  for (uint32_t q = 2; q * q <= m; ++q)
+    if (m % q == 0) {
+      f.push_back(q);
+      while (m % q == 0) m /= q;
+    }
+  if (m > 1) f.push_back(m);
+  for (uint32_t g = 2;; ++g) {
+    bool ok = true;
+    for (uint32_t q : f) ok = ok && pow32(g, (p - 1) / q, p) != 1;
+    if (ok) return g;
+  }
+}
+
+const std::vector<Prime32>& primes32() {
+  static std::vector<Prime32> table = [] {
+    std::vector<Prime32> t;
+    for (uint32_t j = 1; t.size() < kMaxModuli32; ++j) {
+      const uint32_t p = (1u << 30) - j * (1u << 16) + 1;
+      if (!is_prime32(p)) continue;
+      t.push_back({p, (uint32_t)(~0ull / p), pow32(least_primitive_root32(p), (p - 1) >> 16, p)});
+    }
+    return t;
+  }();
+  return table;
+}
+
+uint32_t shoupify32(uint32_t x, uint32_t p) { return (uint32_t)(((uint64_t)x << 32) / p); }
+
+// details/ntt.hpp:28-77 at 32-bit words: psi = root^(2^(15 - log_n)); phi and
+// invphi powers with Shoup forms, bit-reversed; N^-1 and N^-1 * invphi[1].
+void build_host_tables32(uint32_t log_n, uint32_t cm, uint32_t* out4n, uint32_t* sc4) {
+  const Prime32& pe = primes32()[cm];
+  const uint32_t p = pe.p, n = 1u << log_n;
+  uint32_t psi = pe.root;
+  for (uint32_t i = 0; i < kLogMaxDegree32 - log_n; ++i) psi = (uint32_t)((uint64_t)psi * psi % p);
+  const uint32_t ipsi = pow32(psi, 2ull * n - 1, p);
+  uint32_t a = 1, b = 1;
+  for (uint32_t i = 0; i < n; ++i) {
+    uint32_t r = 0;
+    for (uint32_t k = 0; k < log_n; ++k) r |= ((i >> k) & 1u) << (log_n - 1 - k);
+    out4n[r] = a;
+    out4n[n + r] = shoupify32(a, p);
+    out4n[2 * n + r] = b;
+    out4n[3 * n + r] = shoupify32(b, p);
+    a = (uint32_t)((uint64_t)a * psi % p);
+    b = (uint32_t)((uint64_t)b * ipsi % p);
+  }
+  const uint32_t inv_n = pow32(n % p, p - 2, p);
+  const uint32_t inv_n_iphi = (uint32_t)((uint64_t)inv_n * out4n[2 * n + 1] % p);
+  sc4[0] = inv_n;
+  sc4[1] = shoupify32(inv_n, p);
+  sc4[2] = inv_n_iphi;
+  sc4[3] = shoupify32(inv_n_iphi, p);
+}
+
+// ---- device tables -------------------------------------------------------------
+struct DeviceTables32 {
+  std::mutex mu;
+  DevMod32* mods[kLogMaxDegree32 + 1] = {};
+  std::vector<uint8_t> built[kLogMaxDegree32 + 1];
+};
+
+DeviceTables32& tables_of(int device) {
+  static std::mutex mu;
+  static std::vector<std::unique_ptr<DeviceTables32>> all;
+  std::lock_guard<std::mutex> g(mu);
+  if ((int)all.size() <= device) all.resize(device + 1);
+  if (!all[device]) all[device].reset(new DeviceTables32);
+  return *all[device];
+}
+
+int ensure32(int device, uint32_t log_n, uint32_t cm0, uint32_t L, const DevMod32** out) {
+  DeviceTables32& t = tables_of(device);
+  std::lock_guard<std::mutex> g(t.mu);
+  std::vector<uint8_t>& built = t.built[log_n];
+  if (built.empty()) built.assign(kMaxModuli32, 0);
+  cudaError_t e;
+  if (!t.mods[log_n]) {
+    e = cudaMalloc(&t.mods[log_n], kMaxModuli32 * sizeof(DevMod32));
+    if (e != cudaSuccess) {
+      t.mods[log_n] = nullptr;
+      return fail_cuda(e, "cudaMalloc(DevMod32 table)");
+    }
+    e = cudaMemset(t.mods[log_n], 0, kMaxModuli32 * sizeof(DevMod32));
+    if (e != cudaSuccess) return fail_cuda(e, "cudaMemset(DevMod32 table)");
+  }
+  const uint32_t n = 1u << log_n;
+  std::vector<uint32_t> host(4 * (size_t)n), packed(4 * (size_t)n);
+  for (uint32_t cm = cm0; cm < cm0 + L; ++cm) {
+    if (built[cm]) continue;
+    uint32_t sc[4];
+    build_host_tables32(log_n, cm, host.data(), sc);
+    for (uint32_t k = 0; k < n; ++k) {  // {w, w'} pairs: fwd then inv
+      packed[2 * k] = host[k];
+      packed[2 * k + 1] = host[n + k];
+      packed[2 * (size_t)n + 2 * k] = host[2 * n + k];
+      packed[2 * (size_t)n + 2 * k + 1] = host[3 * n + k];
+    }
+    uint32_t* d = nullptr;
+    e = cudaMalloc(&d, packed.size() * sizeof(uint32_t));
+    if (e != cudaSuccess) return fail_cuda(e, "cudaMalloc(twiddles32)");
+    e = cudaMemcpy(d, packed.data(), packed.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail_cuda(e, "upload twiddles32");
+    DevMod32 m;
+    m.fwd = reinterpret_cast<const uint2*>(d);
+    m.inv = reinterpret_cast<const uint2*>(d + 2 * (size_t)n);
+    m.p = primes32()[cm].p;
+    m.pn = primes32()[cm].pn;
+    m.inv_n = sc[0];
+    m.inv_n_s = sc[1];
+    m.inv_n_iphi = sc[2];
+    m.inv_n_iphi_s = sc[3];
+    e = cudaMemcpy(t.mods[log_n] + cm, &m, sizeof m, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail_cuda(e, "upload DevMod32");
+    built[cm] = 1;
+  }
+  *out = t.mods[log_n];
+  return kOk;
+}
+
+// ---- kernels -------------------------------------------------------------------
+// Tile geometry per degree: whole limbs, 2^LOGE words per thread.
+template <int LOGN>
+struct Cfg32 {
+  static constexpr int T = LOGN > 11 ? LOGN : 11;
+  static constexpr int LOGE = LOGN < 4 ? LOGN : (T == 15 ? 5 : 4);
+  using C = TileCfg<T, LOGN, 0, LOGE>;
+  static constexpr size_t kSmem = tile_smem_words(1u << T) * sizeof(uint32_t);
+};
+
+struct Limbs32 {
+  uint32_t count, L, cm0;
+  __device__ __forceinline__ uint32_t cm(uint32_t k) const { return cm0 + k % L; }
+};
+
+// Tile <- limbs limb0 .. (16-byte global loads, 8-byte shared stores).
+template <class C>
+__device__ __forceinline__ void stage_in32(uint32_t* s, const uint32_t* g, uint32_t limb0, uint32_t count) {
+  for (uint32_t v = threadIdx.x * 4; v < (1u << C::T); v += C::THREADS * 4) {
+    const uint32_t limb = limb0 + (v >> C::K);
+    if (limb < count) {
+      const uint4 d = __ldg(reinterpret_cast<const uint4*>(g + ((size_t)limb << C::K) + (v & ((1u << C::K) - 1u))));
+      *reinterpret_cast<uint2*>(s + sidx(v)) = make_uint2(d.x, d.y);
+      *reinterpret_cast<uint2*>(s + sidx(v + 2)) = make_uint2(d.z, d.w);
+    }
+  }
+}
+
+template <class C>
+__device__ __forceinline__ void stage_out32(const uint32_t* s, uint32_t* g, uint32_t limb0, const Limbs32& ls,
+                                            const DevMod32* __restrict__ mods, bool reduce) {
+  for (uint32_t v = threadIdx.x * 4; v < (1u << C::T); v += C::THREADS * 4) {
+    const uint32_t limb = limb0 + (v >> C::K);
+    if (limb < ls.count) {
+      const uint2 lo = *reinterpret_cast<const uint2*>(s + sidx(v));
+      const uint2 hi = *reinterpret_cast<const uint2*>(s + sidx(v + 2));
+      uint4 d = make_uint4(lo.x, lo.y, hi.x, hi.y);
+      if (reduce) {
+        const uint32_t p = __ldg(&mods[ls.cm(limb)].p), p2 = p << 1;
+        d.x = fwd_correct(d.x, p, p2);
+        d.y = fwd_correct(d.y, p, p2);
+        d.z = fwd_correct(d.z, p, p2);
+        d.w = fwd_correct(d.w, p, p2);
+      }
+      *reinterpret_cast<uint4*>(g + ((size_t)limb << C::K) + (v & ((1u << C::K) - 1u))) = d;
+    }
+  }
+}
+
+// DIR: 0 forward (reduced to [0, p)), 1 forward lazy ([0, 4p)), 2 backward.
+template <class C, int DIR>
+__global__ void __launch_bounds__(C::THREADS) k32_ntt(uint32_t* data, Limbs32 ls, const DevMod32* __restrict__ mods) {
+  extern __shared__ __align__(16) uint32_t smem32[];
+  constexpr int NR = C::NR;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t limb0 = blockIdx.x << (C::T - C::K);
+  const uint32_t my_limb = limb0 + C::sub(tid);
+  const bool active = my_limb < ls.count;
+  const DevMod32 m = load_mod(mods, ls.cm(active ? my_limb : 0));
+  stage_in32<C>(smem32, data, limb0, ls.count);
+  __syncthreads();
+  if constexpr (DIR != 2) {
+    fwd_rounds<C, 0, NR>(smem32, tid, 0, 0, m.fwd, m.p, active);
+  } else {
+    inv_rounds<C, NR - 1, -1, true>(smem32, tid, (uint32_t)C::K, 0, 0, m, active);
+  }
+  stage_out32<C>(smem32, data, limb0, ls, mods, DIR == 0);
+}
+
+// c = INTT(NTT(a) * NTT(b)) per limb; c must not alias a or b.
+template <class C>
+__global__ void __launch_bounds__(C::THREADS) k32_polymul(uint32_t* c, const uint32_t* a, const uint32_t* b,
+                                                          Limbs32 ls, const DevMod32* __restrict__ mods) {
+  extern __shared__ __align__(16) uint32_t smem32[];
+  constexpr int NR = C::NR, E = 1 << C::LOGE;
+  using RB = Round<C, NR - 1>;
+  static_assert(RB::R == C::LOGE && RB::BETA == 0 && RB::EB == 0, "bottom round must own contiguous words");
+  const uint32_t tid = threadIdx.x;
+  const uint32_t limb0 = blockIdx.x << (C::T - C::K);
+  const uint32_t my_limb = limb0 + C::sub(tid);
+  const bool active = my_limb < ls.count;
+  const DevMod32 m = load_mod(mods, ls.cm(active ? my_limb : 0));
+  const uint32_t p = m.p, p2 = p << 1;
+  const uint32_t bb = RB::base(tid);
+  // the thread's E contiguous words of the output tile (in limb my_limb)
+  uint32_t* park = c + ((size_t)my_limb << C::K) + (bb & ((1u << C::K) - 1u));
+  uint32_t x[E];
+  // NTT(a), parked in c
+  stage_in32<C>(smem32, a, limb0, ls.count);
+  __syncthreads();
+  fwd_rounds<C, 0, NR - 1>(smem32, tid, 0, 0, m.fwd, p, active);
+  if (active) {
+    smem_load<RB>(x, smem32, bb);
+    ct_round<RB>(x, m.fwd, (uint32_t)RB::HI, RB::gr(bb, 0), p);
+#pragma unroll
+    for (int i = 0; i < E; i += 4)
+      *reinterpret_cast<uint4*>(park + i) =
+          make_uint4(fwd_correct(x[i], p, p2), fwd_correct(x[i + 1], p, p2), fwd_correct(x[i + 2], p, p2),
+                     fwd_correct(x[i + 3], p, p2));
+  }
+  __syncthreads();
+  // NTT(b), product, inverse
+  stage_in32<C>(smem32, b, limb0, ls.count);
+  __syncthreads();
+  fwd_rounds<C, 0, NR - 1>(smem32, tid, 0, 0, m.fwd, p, active);
+  if (active) {
+    smem_load<RB>(x, smem32, bb);
+    ct_round<RB>(x, m.fwd, (uint32_t)RB::HI, RB::gr(bb, 0), p);
+#pragma unroll
+    for (int i = 0; i < E; i += 4) {
+      const uint4 ah = *reinterpret_cast<const uint4*>(park + i);  // written above by this thread
+      x[i] = mulmod_barrett(ah.x, fwd_correct(x[i], p, p2), p, m.pn);
+      x[i + 1] = mulmod_barrett(ah.y, fwd_correct(x[i + 1], p, p2), p, m.pn);
+      x[i + 2] = mulmod_barrett(ah.z, fwd_correct(x[i + 2], p, p2), p, m.pn);
+      x[i + 3] = mulmod_barrett(ah.w, fwd_correct(x[i + 3], p, p2), p, m.pn);
+    }
+    gs_round<RB, NR == 1>(x, (uint32_t)C::K, (uint32_t)RB::BETA, RB::gr(bb, 0), m);
+    smem_store<RB>(x, smem32, bb);
+  }
+  __syncthreads();
+  inv_rounds<C, NR - 2, -1, true>(smem32, tid, (uint32_t)C::K, 0, 0, m, active);
+  stage_out32<C>(smem32, c, limb0, ls, mods, false);
+}
+
+template <int OP>
+__global__ void k32_elementwise(uint32_t* dst, const uint32_t* a, const uint32_t* b, size_t total, uint32_t log_n,
+                                Limbs32 ls, const DevMod32* __restrict__ mods) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t cm = ls.cm((uint32_t)(k >> log_n));
+    const uint32_t p = __ldg(&mods[cm].p);
+    if constexpr (OP == YELL_OP_MULMOD) dst[k] = mulmod_barrett(a[k], b[k], p, __ldg(&mods[cm].pn));
+    else if constexpr (OP == YELL_OP_ADDMOD) dst[k] = addmod(a[k], b[k], p);
+    else if constexpr (OP == YELL_OP_SUBMOD) dst[k] = submod(a[k], b[k], p);
+    else if constexpr (OP == YELL_OP_MULADD) dst[k] = muladd_barrett(dst[k], a[k], b[k], p, __ldg(&mods[cm].pn));
+    else dst[k] = p - a[k];
+  }
+}
+
+// ---- launch ----------------------------------------------------------------------
+template <int LOGN>
+cudaError_t set_attrs32() {
+  using C = typename Cfg32<LOGN>::C;
+  const int smem = (int)Cfg32<LOGN>::kSmem;
+  cudaError_t e = cudaSuccess;
+  for (auto k : {k32_ntt<C, 0>, k32_ntt<C, 1>, k32_ntt<C, 2>})
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k32_polymul<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  return e;
+}
+
+template <int LOGN>
+cudaError_t launch32(int kind, uint32_t* c, const uint32_t* a, const uint32_t* b, const Limbs32& ls,
+                     const DevMod32* mods, cudaStream_t st) {
+  using CF = Cfg32<LOGN>;
+  using C = typename CF::C;
+  const uint32_t blocks = (ls.count + (1u << (C::T - LOGN)) - 1) >> (C::T - LOGN);
+  if (kind == 0) k32_ntt<C, 0><<<blocks, C::THREADS, CF::kSmem, st>>>(c, ls, mods);
+  else if (kind == 1) k32_ntt<C, 1><<<blocks, C::THREADS, CF::kSmem, st>>>(c, ls, mods);
+  else if (kind == 2) k32_ntt<C, 2><<<blocks, C::THREADS, CF::kSmem, st>>>(c, ls, mods);
+  else k32_polymul<C><<<blocks, C::THREADS, CF::kSmem, st>>>(c, a, b, ls, mods);
+  return cudaGetLastError();
+}
+
+template <int... L>
+cudaError_t dispatch32(std::integer_sequence<int, L...>, uint32_t log_n, int kind, uint32_t* c, const uint32_t* a,
+                       const uint32_t* b, const Limbs32& ls, const DevMod32* mods, cudaStream_t st) {
+  cudaError_t e = cudaErrorInvalidValue;
+  ((log_n == (uint32_t)(L + kMinLogN32) ? (e = launch32<L + kMinLogN32>(kind, c, a, b, ls, mods, st), 0) : 0), ...);
+  return e;
+}
+
+template <int... L>
+cudaError_t attrs32(std::integer_sequence<int, L...>) {
+  cudaError_t e = cudaSuccess;
+  ((e = (e == cudaSuccess ? set_attrs32<L + kMinLogN32>() : e)), ...);
+  return e;
+}
+
+using Degrees32 = std::make_integer_sequence<int, kLogMaxDegree32 - kMinLogN32 + 1>;
+
+int prepare32(uint32_t log_n, uint32_t cm0, uint32_t L, DeviceContext** ctx, const DevMod32** mods) {
+  if (log_n < kMinLogN32 || log_n > kLogMaxDegree32)
+    return fail(kUnsupportedDegree, "32-bit moduli: log_n must be in [3, 15]");
+  if (L == 0 || cm0 >= kMaxModuli32 || L > kMaxModuli32 - cm0)
+    return fail(kInvalidModulus, "32-bit moduli: indices must lie in [0, 291)");
+  int st = kOk;
+  *ctx = DeviceContext::current(&st);
+  if (!*ctx) return st;
+  {
+    static std::mutex mu;
+    static std::vector<int> done;
+    std::lock_guard<std::mutex> g(mu);
+    const int dev = (*ctx)->device();
+    if (std::find(done.begin(), done.end(), dev) == done.end()) {
+      const cudaError_t e = attrs32(Degrees32{});
+      if (e != cudaSuccess) return fail_cuda(e, "32-bit kernel attributes");
+      done.push_back(dev);
+    }
+  }
+  return ensure32((*ctx)->device(), log_n, cm0, L, mods);
+}
+
+int aligned16(const void* p, const char* what) {
+  return reinterpret_cast<uintptr_t>(p) % 16 ? fail(kInvalidArgument, std::string(what) + " is not 16-byte aligned")
+                                             : kOk;
+}
+
+int run32(int kind, uint32_t* c, const uint32_t* a, const uint32_t* b, uint32_t count, uint32_t L, uint32_t log_n,
+          uint32_t cm0, void* stream) {
+  DeviceContext* ctx;
+  const DevMod32* mods;
+  int st = prepare32(log_n, cm0, L, &ctx, &mods);
+  if (st != kOk) return st;
+  if ((st = aligned16(c, "output")) != kOk) return st;
+  if (a && (st = aligned16(a, "a")) != kOk) return st;
+  if (b && (st = aligned16(b, "b")) != kOk) return st;
+  const Limbs32 ls{count * L, L, cm0};
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream();
+  static const char* names[4] = {"ntt32_forward", "ntt32_forward_lazy", "ntt32_backward", "polymul32"};
+  LaunchScope ps(names[kind], s);
+  const cudaError_t e = dispatch32(Degrees32{}, log_n, kind, c, a, b, ls, mods, s);
+  g_kernel_launches += 1;
+  return e == cudaSuccess ? kOk : fail_cuda(e, names[kind]);
+}
+
+// Host-memory single-limb transform through the staging buffer.
+int host_ntt32(int kind, uint32_t* op, uint32_t log_n, uint32_t cm) {
+  if (!op) return fail(kInvalidArgument, "null pointer");
+  DeviceContext* ctx;
+  const DevMod32* mods;
+  int st = prepare32(log_n, cm, 1, &ctx, &mods);
+  if (st != kOk) return st;
+  const size_t n = (size_t)1 << log_n;
+  std::lock_guard<std::mutex> g(ctx->staging.lock);
+  st = ctx->staging.reserve(n);
+  if (st != kOk) return st;
+  uint32_t* d = reinterpret_cast<uint32_t*>(ctx->staging.ptr);
+  cudaStream_t s = ctx->stream();
+  cudaError_t e = cudaMemcpyAsync(d, op, n * 4, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return fail_cuda(e, "H2D");
+  st = run32(kind, d, nullptr, nullptr, 1, 1, log_n, cm, s);
+  if (st != kOk) return st;
+  e = cudaMemcpyAsync(op, d, n * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? kOk : fail_cuda(e, "D2H");
+}
+
+}  // namespace
+}  // namespace yell_gb300
+
+using namespace yell_gb300;
+
+extern "C" {
+
+uint32_t yell32_max_moduli(void) { return kMaxModuli32; }
+uint32_t yell32_max_log_degree(void) { return kLogMaxDegree32; }
+uint32_t yell32_prime(uint32_t cm) { return cm < kMaxModuli32 ? primes32()[cm].p : 0; }
+uint32_t yell32_prime_pn(uint32_t cm) { return cm < kMaxModuli32 ? primes32()[cm].pn : 0; }
+uint32_t yell32_primitive_root(uint32_t cm) { return cm < kMaxModuli32 ? primes32()[cm].root : 0; }
+
+int yell32_ntt_tables(uint32_t log_n, uint32_t cm, uint32_t* out4n, uint32_t* scalars4) {
+  if (!out4n || !scalars4) return fail(kInvalidArgument, "null output");
+  if (log_n < 1 || log_n > kLogMaxDegree32) return fail(kUnsupportedDegree, "log_n must be in [1, 15]");
+  if (cm >= kMaxModuli32) return fail(kInvalidModulus, "modulus index out of range");
+  build_host_tables32(log_n, cm, out4n, scalars4);
+  return kOk;
+}
+
+int yell32_init_ntt_tables(uint32_t log_n, uint32_t cm0, uint32_t L) {
+  DeviceContext* ctx;
+  const DevMod32* mods;
+  return prepare32(log_n, cm0, L, &ctx, &mods);
+}
+
+int yell32_ntt_forward(uint32_t* op, uint32_t log_n, uint32_t cm) { return host_ntt32(0, op, log_n, cm); }
+int yell32_ntt_forward_lazy(uint32_t* op, uint32_t log_n, uint32_t cm) { return host_ntt32(1, op, log_n, cm); }
+int yell32_ntt_backward(uint32_t* op, uint32_t log_n, uint32_t cm) { return host_ntt32(2, op, log_n, cm); }
+
+int yell32_dev_ntt(uint32_t* d_polys, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0, int direction,
+                   void* stream) {
+  if (!d_polys || count == 0) return fail(kInvalidArgument, "null pointer or zero count");
+  if (direction < 0 || direction > 2) return fail(kInvalidArgument, "bad direction");
+  return run32(direction, d_polys, nullptr, nullptr, count, L, log_n, cm0, stream);
+}
+
+int yell32_dev_polymul(uint32_t* d_c, const uint32_t* d_a, const uint32_t* d_b, uint32_t pairs, uint32_t L,
+                       uint32_t log_n, uint32_t cm0, void* stream) {
+  if (!d_c || !d_a || !d_b || pairs == 0) return fail(kInvalidArgument, "null pointer or zero pairs");
+  if (d_c == d_a || d_c == d_b) return fail(kInvalidArgument, "the product may not overwrite an operand");
+  return run32(3, d_c, d_a, d_b, pairs, L, log_n, cm0, stream);
+}
+
+int yell32_dev_elementwise(int op, uint32_t* d_dst, const uint32_t* d_a, const uint32_t* d_b, uint32_t count,
+                           uint32_t L, uint32_t log_n, uint32_t cm0, void* stream) {
+  if (!d_dst || !d_a || (op != YELL_OP_NEGATE && !d_b) || count == 0)
+    return fail(kInvalidArgument, "null pointer or zero count");
+  if (op < YELL_OP_MULMOD || op > YELL_OP_NEGATE) return fail(kInvalidArgument, "bad op");
+  DeviceContext* ctx;
+  const DevMod32* mods;
+  int st = prepare32(log_n, cm0, L, &ctx, &mods);
+  if (st != kOk) return st;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream();
+  const size_t total = ((size_t)count * L) << log_n;
+  const Limbs32 ls{count * L, L, cm0};
+  const int grid = (int)std::min<size_t>((total + 255) / 256, 152 * 16);
+  LaunchScope ps("elementwise32", s);
+  switch (op) {
+    case YELL_OP_MULMOD: k32_elementwise<YELL_OP_MULMOD><<<grid, 256, 0, s>>>(d_dst, d_a, d_b, total, log_n, ls, mods); break;
+    case YELL_OP_ADDMOD: k32_elementwise<YELL_OP_ADDMOD><<<grid, 256, 0, s>>>(d_dst, d_a, d_b, total, log_n, ls, mods); break;
+    case YELL_OP_SUBMOD: k32_elementwise<YELL_OP_SUBMOD><<<grid, 256, 0, s>>>(d_dst, d_a, d_b, total, log_n, ls, mods); break;
+    case YELL_OP_MULADD: k32_elementwise<YELL_OP_MULADD><<<grid, 256, 0, s>>>(d_dst, d_a, d_b, total, log_n, ls, mods); break;
+    default: k32_elementwise<YELL_OP_NEGATE><<<grid, 256, 0, s>>>(d_dst, d_a, d_b, total, log_n, ls, mods); break;
+  }
+  g_kernel_launches += 1;
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? kOk : fail_cuda(e, "elementwise32");
+}
+
+}  // extern "C"

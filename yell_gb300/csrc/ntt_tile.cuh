@@ -87,16 +87,17 @@ struct Round {
 };
 
 // ---- register <-> shared memory ----------------------------------------------
-template <class RG>
-__device__ __forceinline__ void smem_load(uint64_t* x, const uint64_t* s, uint32_t base_v) {
+template <class RG, class W>
+__device__ __forceinline__ void smem_load(W* x, const W* s, uint32_t base_v) {
   constexpr int R = RG::R;
-  const uint64_t* sb = s + sidx(base_v);
+  using PW = typename PairOf<W>::type;
+  const W* sb = s + sidx(base_v);
   if constexpr (RG::PAIRS) {
 #pragma unroll
     for (int m = 0; m < RG::E / 2; ++m)
 #pragma unroll
       for (int j = 0; j < (1 << R); ++j) {
-        const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(sb + sidx(RG::off(2 * m, j)));
+        const PW v = *reinterpret_cast<const PW*>(sb + sidx(RG::off(2 * m, j)));
         x[((2 * m) << R) | j] = v.x;
         x[((2 * m + 1) << R) | j] = v.y;
       }
@@ -108,17 +109,18 @@ __device__ __forceinline__ void smem_load(uint64_t* x, const uint64_t* s, uint32
   }
 }
 
-template <class RG>
-__device__ __forceinline__ void smem_store(const uint64_t* x, uint64_t* s, uint32_t base_v) {
+template <class RG, class W>
+__device__ __forceinline__ void smem_store(const W* x, W* s, uint32_t base_v) {
   constexpr int R = RG::R;
-  uint64_t* sb = s + sidx(base_v);
+  using PW = typename PairOf<W>::type;
+  W* sb = s + sidx(base_v);
   if constexpr (RG::PAIRS) {
 #pragma unroll
     for (int m = 0; m < RG::E / 2; ++m)
 #pragma unroll
       for (int j = 0; j < (1 << R); ++j)
-        *reinterpret_cast<ulonglong2*>(sb + sidx(RG::off(2 * m, j))) =
-            make_ulonglong2(x[((2 * m) << R) | j], x[((2 * m + 1) << R) | j]);
+        *reinterpret_cast<PW*>(sb + sidx(RG::off(2 * m, j))) =
+            PairOf<W>::make(x[((2 * m) << R) | j], x[((2 * m + 1) << R) | j]);
   } else {
 #pragma unroll
     for (int ex = 0; ex < RG::E; ++ex)
@@ -131,17 +133,16 @@ __device__ __forceinline__ void smem_store(const uint64_t* x, uint64_t* s, uint3
 // Forward sub-stage k of a round pairs (j, j + 2^(R-1-k)) with twiddle
 // w[2^(s_first+k) + (gr << k) + (j >> (R-k))].  The twiddles of sub-stage
 // k+1 are requested before sub-stage k computes.
-template <int R, int E, int k>
-__device__ __forceinline__ void ct_stages(uint64_t* x, const ulonglong2* __restrict__ tw,
-                                          uint32_t s_first, uint32_t gr, uint64_t np, uint64_t p2,
-                                          const ulonglong2* wk) {
+template <int R, int E, int k, class W, class PW>
+__device__ __forceinline__ void ct_stages(W* x, const PW* __restrict__ tw, uint32_t s_first, uint32_t gr,
+                                          W np, W p2, const PW* wk) {
   if constexpr (k < R) {
     constexpr int d = 1 << (R - 1 - k);
     constexpr int NJ = 1 << k;
     constexpr int NN = (k + 1 < R) ? (2 << k) : 1;
-    ulonglong2 wn[NN];
+    PW wn[NN];
     if constexpr (k + 1 < R) {
-      const ulonglong2* src = tw + (1u << (s_first + k + 1)) + (gr << (k + 1));
+      const PW* src = tw + (1u << (s_first + k + 1)) + (gr << (k + 1));
 #pragma unroll
       for (int jj = 0; jj < NN; ++jj) wn[jj] = __ldg(src + jj);
     }
@@ -158,26 +159,25 @@ __device__ __forceinline__ void ct_stages(uint64_t* x, const ulonglong2* __restr
   }
 }
 
-template <class RG>
-__device__ __forceinline__ void ct_round(uint64_t* x, const ulonglong2* __restrict__ tw,
-                                         uint32_t s_first, uint32_t gr, uint64_t p) {
-  ulonglong2 w0[1];
+template <class RG, class W, class PW>
+__device__ __forceinline__ void ct_round(W* x, const PW* __restrict__ tw, uint32_t s_first, uint32_t gr, W p) {
+  PW w0[1];
   w0[0] = __ldg(tw + (1u << s_first) + gr);
-  ct_stages<RG::R, RG::E, 0>(x, tw, s_first, gr, 0 - p, p << 1, w0);
+  ct_stages<RG::R, RG::E, 0>(x, tw, s_first, gr, (W)(0 - p), (W)(p << 1), w0);
 }
 
 // The same round applied to two operands that share twiddles (the two
 // inputs of a polymul at the same limb and position).
-template <int R, int E, int k>
-__device__ __forceinline__ void ct_stages2(uint64_t* x, uint64_t* y, const ulonglong2* __restrict__ tw,
-                                           uint32_t s_first, uint32_t gr, uint64_t np, uint64_t p2) {
+template <int R, int E, int k, class W, class PW>
+__device__ __forceinline__ void ct_stages2(W* x, W* y, const PW* __restrict__ tw, uint32_t s_first, uint32_t gr,
+                                           W np, W p2) {
   if constexpr (k < R) {
     constexpr int d = 1 << (R - 1 - k);
     constexpr int NJ = 1 << k;
-    const ulonglong2* src = tw + (1u << (s_first + k)) + (gr << k);
+    const PW* src = tw + (1u << (s_first + k)) + (gr << k);
 #pragma unroll
     for (int jj = 0; jj < NJ; ++jj) {
-      const ulonglong2 w = __ldg(src + jj);
+      const PW w = __ldg(src + jj);
 #pragma unroll
       for (int ex = 0; ex < E; ++ex)
 #pragma unroll
@@ -196,10 +196,9 @@ __device__ __forceinline__ void ct_stages2(uint64_t* x, uint64_t* y, const ulong
 // LAST, the round's final sub-stage is the reference's last layer with the
 // N^-1 scaling fused (include/yell/details/ntt.hpp:220-228).
 // top = log_n - 1 - sigma_first, so sub-stage k uses m = 2^(top - k).
-template <int R, int E, bool LAST, int k>
-__device__ __forceinline__ void gs_stages(uint64_t* x, const ulonglong2* __restrict__ itw,
-                                          uint32_t top, uint32_t gr, const DevMod& m,
-                                          const ulonglong2* wk) {
+template <int R, int E, bool LAST, int k, class W, class PW, class M>
+__device__ __forceinline__ void gs_stages(W* x, const PW* __restrict__ itw, uint32_t top, uint32_t gr,
+                                          const M& m, const PW* wk) {
   if constexpr (k < R) {
     constexpr int d = 1 << k;
     if constexpr (LAST && k == R - 1) {
@@ -211,13 +210,13 @@ __device__ __forceinline__ void gs_stages(uint64_t* x, const ulonglong2* __restr
       constexpr int NJ = 1 << (R - 1 - k);
       constexpr bool NEXT = (k + 1 < R) && !(LAST && k + 2 == R);
       constexpr int NN = NEXT ? (1 << (R - 2 - k)) : 1;
-      ulonglong2 wn[NN];
+      PW wn[NN];
       if constexpr (NEXT) {
-        const ulonglong2* src = itw + (1u << (top - k - 1)) + (gr << (R - 2 - k));
+        const PW* src = itw + (1u << (top - k - 1)) + (gr << (R - 2 - k));
 #pragma unroll
         for (int jj = 0; jj < NN; ++jj) wn[jj] = __ldg(src + jj);
       }
-      const uint64_t np = 0 - m.p, p2 = m.p << 1;
+      const W np = (W)(0 - m.p), p2 = (W)(m.p << 1);
 #pragma unroll
       for (int jj = 0; jj < NJ; ++jj)
 #pragma unroll
@@ -232,16 +231,16 @@ __device__ __forceinline__ void gs_stages(uint64_t* x, const ulonglong2* __restr
   }
 }
 
-template <class RG, bool LAST>
-__device__ __forceinline__ void gs_round(uint64_t* x, uint32_t log_n, uint32_t sigma_first,
-                                         uint32_t gr, const DevMod& m) {
+template <class RG, bool LAST, class W, class M>
+__device__ __forceinline__ void gs_round(W* x, uint32_t log_n, uint32_t sigma_first, uint32_t gr, const M& m) {
   constexpr int R = RG::R;
+  using PW = typename PairOf<W>::type;
   const uint32_t top = log_n - 1 - sigma_first;
   constexpr bool ONLY_LAST = LAST && R == 1;
   constexpr int N0 = ONLY_LAST ? 1 : (1 << (R - 1));
-  ulonglong2 w0[N0];
+  PW w0[N0];
   if constexpr (!ONLY_LAST) {
-    const ulonglong2* src = m.inv + (1u << top) + (gr << (R - 1));
+    const PW* src = m.inv + (1u << top) + (gr << (R - 1));
 #pragma unroll
     for (int jj = 0; jj < N0; ++jj) w0[jj] = __ldg(src + jj);
   }
@@ -264,14 +263,31 @@ __device__ __forceinline__ DevMod load_mod(const DevMod* __restrict__ mods, uint
   return m;
 }
 
+__device__ __forceinline__ DevMod32 load_mod(const DevMod32* __restrict__ mods, uint32_t cm) {
+  DevMod32 m;
+  const ulonglong2* src = reinterpret_cast<const ulonglong2*>(mods + cm);
+  const ulonglong2 a = __ldg(src);
+  const uint4 b = __ldg(reinterpret_cast<const uint4*>(src + 1));
+  const uint2 c = __ldg(reinterpret_cast<const uint2*>(src + 2));
+  m.fwd = reinterpret_cast<const uint2*>(a.x);
+  m.inv = reinterpret_cast<const uint2*>(a.y);
+  m.p = b.x;
+  m.pn = b.y;
+  m.inv_n = b.z;
+  m.inv_n_s = b.w;
+  m.inv_n_iphi = c.x;
+  m.inv_n_iphi_s = c.y;
+  return m;
+}
+
 // ---- whole rounds through shared memory ---------------------------------------
 // Forward round I: load from s, CT stages, store to s.  s_off: absolute stage
 // of the transform's top u bit; G: the thread's sub-transform group number.
-template <class C, int I>
-__device__ __forceinline__ void fwd_round_smem(uint64_t* s, uint32_t tid, uint32_t s_off, uint32_t G,
-                                               const ulonglong2* tw, uint64_t p, bool active) {
+template <class C, int I, class W, class PW>
+__device__ __forceinline__ void fwd_round_smem(W* s, uint32_t tid, uint32_t s_off, uint32_t G, const PW* tw, W p,
+                                               bool active) {
   using RG = Round<C, I>;
-  uint64_t x[1 << C::LOGE];
+  W x[1 << C::LOGE];
   const uint32_t b = RG::base(tid);
   if (active) {
     smem_load<RG>(x, s, b);
@@ -282,12 +298,11 @@ __device__ __forceinline__ void fwd_round_smem(uint64_t* s, uint32_t tid, uint32
 
 // Inverse round at top-index I: sig_off is the absolute inverse stage of the
 // transform's u-bit 0.
-template <class C, int I, bool LAST>
-__device__ __forceinline__ void inv_round_smem(uint64_t* s, uint32_t tid, uint32_t log_n,
-                                               uint32_t sig_off, uint32_t G, const DevMod& m,
-                                               bool active) {
+template <class C, int I, bool LAST, class W, class M>
+__device__ __forceinline__ void inv_round_smem(W* s, uint32_t tid, uint32_t log_n, uint32_t sig_off, uint32_t G,
+                                               const M& m, bool active) {
   using RG = Round<C, I>;
-  uint64_t x[1 << C::LOGE];
+  W x[1 << C::LOGE];
   const uint32_t b = RG::base(tid);
   if (active) {
     smem_load<RG>(x, s, b);
@@ -297,9 +312,9 @@ __device__ __forceinline__ void inv_round_smem(uint64_t* s, uint32_t tid, uint32
 }
 
 // Forward rounds [I, I1) through shared memory, a barrier after each.
-template <class C, int I, int I1>
-__device__ __forceinline__ void fwd_rounds(uint64_t* s, uint32_t tid, uint32_t s_off, uint32_t G,
-                                           const ulonglong2* tw, uint64_t p, bool active) {
+template <class C, int I, int I1, class W, class PW>
+__device__ __forceinline__ void fwd_rounds(W* s, uint32_t tid, uint32_t s_off, uint32_t G, const PW* tw, W p,
+                                           bool active) {
   if constexpr (I < I1) {
     fwd_round_smem<C, I>(s, tid, s_off, G, tw, p, active);
     __syncthreads();
@@ -309,9 +324,9 @@ __device__ __forceinline__ void fwd_rounds(uint64_t* s, uint32_t tid, uint32_t s
 
 // Inverse rounds from top-index I down to I1 (exclusive), bottom-up order.
 // The round at top-index 0 carries the scaled last layer when HAS_LAST.
-template <class C, int I, int I1, bool HAS_LAST>
-__device__ __forceinline__ void inv_rounds(uint64_t* s, uint32_t tid, uint32_t log_n, uint32_t sig_off,
-                                           uint32_t G, const DevMod& m, bool active) {
+template <class C, int I, int I1, bool HAS_LAST, class W, class M>
+__device__ __forceinline__ void inv_rounds(W* s, uint32_t tid, uint32_t log_n, uint32_t sig_off, uint32_t G,
+                                           const M& m, bool active) {
   if constexpr (I > I1) {
     inv_round_smem<C, I, HAS_LAST && I == 0>(s, tid, log_n, sig_off, G, m, active);
     __syncthreads();
