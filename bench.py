@@ -364,6 +364,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
         uneven.pop("_items")
         uneven.pop("_mix")
 
+    rows = None if args.no_rows else run_rows(torch, y, stream, dc)
+
     # ---- end to end through the host-memory C ABI call --------------------
     pa = y.PinnedBuffer(a.shape)
     pb = y.PinnedBuffer(b.shape)
@@ -419,12 +421,77 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
             "batched_vs_per_call": value / per_call_value,
             "uneven_batch": uneven,
             "serving": serving,
+            "rows": rows,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+def run_rows(torch, y, stream, dc, reps: int = 5):
+    """Device throughput of the rows beside the polymul path, at the polymul
+    workload's sizes: seeded samplers filling 16 polys of N = 2^16, L = 32;
+    CRT lifting of the 16 product polys; the 32-bit moduli polymul at
+    N = 2^15, L = 32, 16 pairs.  Each timed with CUDA events on `stream`
+    over `reps` launches after one warm-up."""
+    from yell_gb300 import moduli32 as m32
+
+    hbm, peak_kind = peaks()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    out = {"peak_hbm_gbs": hbm, "peak_kind": peak_kind}
+    words = PAIRS * L * N
+    buf = torch.empty(words, dtype=torch.int64, device="cuda")
+    samplers = {
+        "uniform": lambda: y.sample_uniform(buf, PAIRS, L, LOG_N, seed=1, stream=stream),
+        "zo": lambda: y.sample_zo(buf, PAIRS, L, LOG_N, seed=2, stream=stream),
+        "gaussian": lambda: y.sample_gaussian(buf, PAIRS, L, LOG_N, seed=3, stream=stream),
+        "hwt_192": lambda: y.sample_hwt(buf, PAIRS, L, LOG_N, 192, seed=4, stream=stream),
+    }
+    for name, fn in samplers.items():
+        ms = timed(fn)
+        gbs = 8 * words / (ms * 1e-3) / 1e9
+        out[f"sample_{name}"] = {"ms": ms, "achieved_gbs": gbs, "frac": gbs / hbm,
+                                 "algorithmic_bytes": 8 * words, "bound": "hbm (writes)"}
+    del buf
+    # CRT lifting of the polymul output (16 polys, L = 32 -> W words per coefficient)
+    W = y.crt_words(L)
+    lifted = torch.empty(PAIRS * N * W, dtype=torch.int64, device="cuda")
+    ms = timed(lambda: y.dev_crt_lift(lifted, dc, PAIRS, L, LOG_N, stream=stream))
+    coeffs = PAIRS * N
+    byts = coeffs * 8 * (L + W)
+    out["crt_lift"] = {"ms": ms, "coefficients_per_s": coeffs / (ms * 1e-3),
+                       "achieved_gbs": byts / (ms * 1e-3) / 1e9, "frac": byts / (ms * 1e-3) / 1e9 / hbm,
+                       "algorithmic_bytes": byts, "words_per_coefficient": W,
+                       "mac64_per_s": coeffs * L * (W + 1) / (ms * 1e-3),
+                       "bound": "integer multiply-add (L x (W+1) 64-bit MACs per coefficient)"}
+    del lifted
+    # 32-bit moduli polymul
+    n32, log32 = 1 << 15, 15
+    w32 = PAIRS * L * n32
+    a32 = torch.randint(0, 1 << 29, (w32,), dtype=torch.int32, device="cuda")
+    b32 = torch.randint(0, 1 << 29, (w32,), dtype=torch.int32, device="cuda")
+    c32 = torch.empty_like(a32)
+    m32.init_ntt_tables(log32, L)
+    ms = timed(lambda: m32.dev_polymul(c32, a32, b32, PAIRS, L, log32, stream=stream))
+    byts = 12 * n32 * L * PAIRS
+    out["polymul32"] = {"ms": ms, "limb_ntts_per_s": 3 * L * PAIRS / (ms * 1e-3),
+                        "achieved_gbs": byts / (ms * 1e-3) / 1e9, "frac": byts / (ms * 1e-3) / 1e9 / hbm,
+                        "algorithmic_bytes": byts, "workload": "N=2^15, L=32, 16 pairs, 30-bit primes"}
+    return out
 
 
 def run_uneven(torch, y, stream, barrier, max_over_ranks, world, no_autotune=False):
@@ -530,6 +597,8 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch comparison")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving sweep")
+    ap.add_argument("--no-rows", action="store_true",
+                    help="skip the sampler, CRT-lifting and 32-bit-moduli measurements")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the selected launch variants (default or YELL_GB300_TUNE_FILE)")
     ap.add_argument("--serve-seconds", type=float, default=0.5, help="seconds per serving load point")

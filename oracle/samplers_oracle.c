@@ -10,7 +10,8 @@
  *   uniform  poly.hpp:200-229  mask to the bit length of p, subtract p once
  *   ZO       poly.hpp:262-275  byte r: r <= rho ? (r & 2 ? p - 1 : 1) : 0
  *   HWT      poly.hpp:282-325  exactly h coefficients +-1 ((rnd & 2) ? 1 : p - 1),
- *                              positions = the h smallest keys of a second stream
+ *                              positions = the indices a keyed Feistel permutation
+ *                              maps below h (a pseudorandom h-subset)
  *   gaussian poly.hpp:238-258  e * amplifier, e < 0 ? p + e : e, every limb
  * The gaussian integer e is the index of the first cumulative threshold above
  * one random word, thresholds floor(2^64 * CDF) of exp(-e^2 / 2 sigma^2)
@@ -67,37 +68,40 @@ void orc_sample_zo(uint64_t* out, uint32_t count, uint32_t L, uint32_t log_n, ui
   }
 }
 
-typedef struct { uint64_t key; uint64_t idx; } keyed;
+/* Keyed permutation of [0, 2^bits): 6 Feistel rounds over alternating index
+ * fields of floor/ceil(bits / 2) bits, round function splitmix64 of the
+ * round key plus the low field.  Coefficient i is nonzero when pi(i) < h. */
+static uint64_t mix(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
 
-static int by_key(const void* a, const void* b) {
-  const keyed* x = (const keyed*)a;
-  const keyed* y = (const keyed*)b;
-  if (x->key != y->key) return x->key < y->key ? -1 : 1;
-  return x->idx < y->idx ? -1 : (x->idx > y->idx);
+static uint32_t feistel(uint32_t x, uint32_t bits, uint64_t key) {
+  uint32_t b = bits >> 1, a = bits - b;
+  for (int r = 0; r < 6; ++r) {
+    const uint32_t lo = x & ((1u << b) - 1u), hi = x >> b;
+    const uint32_t f = (uint32_t)mix(word(key, (uint64_t)r) + lo);
+    x = (lo << a) | ((hi ^ f) & ((1u << a) - 1u));
+    const uint32_t t = a;
+    a = b;
+    b = t;
+  }
+  return x;
 }
 
 int orc_sample_hwt(uint64_t* out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0, uint32_t h,
                    uint64_t seed) {
   const uint64_t n = 1ull << log_n;
   if (h == 0 || h > n) return -1;
-  keyed* ks = (keyed*)malloc(n * sizeof(keyed));
-  uint8_t* take = (uint8_t*)malloc(n);
-  if (!ks || !take) return -1;
   for (uint64_t poly = 0; poly < count; ++poly) {
+    const uint64_t key = word(seed ^ SEED_POSITIONS, poly);
     for (uint64_t i = 0; i < n; ++i) {
-      ks[i].key = word(seed ^ SEED_POSITIONS, (poly << log_n) + i);
-      ks[i].idx = i;
-    }
-    qsort(ks, n, sizeof(keyed), by_key);
-    memset(take, 0, n);
-    for (uint32_t j = 0; j < h; ++j) take[ks[j].idx] = 1;
-    for (uint64_t i = 0; i < n; ++i) {
+      const int take = feistel((uint32_t)i, log_n, key) < h;
       const int plus = (word(seed ^ SEED_SIGNS, (poly << log_n) + i) & 2) != 0;
-      put_all_limbs(out, poly, L, log_n, cm0, i, take[i] ? (plus ? 1 : -1) : 0);
+      put_all_limbs(out, poly, L, log_n, cm0, i, take ? (plus ? 1 : -1) : 0);
     }
   }
-  free(ks);
-  free(take);
   return 0;
 }
 

@@ -104,3 +104,21 @@ def test_crt_oracle_is_the_crt(orc, L):
     w = to_words(xs, t.words())
     assert w.shape == (n, t.words())
     assert all(int.from_bytes(w[i].tobytes(), "little") == xs[i] for i in range(n))
+
+
+def test_hwt_positions_uniform(orc):
+    """Positions of the keyed-permutation HWT sampler: each index nonzero with
+    probability h/N and pairs with probability h(h-1)/(N(N-1)), as for a
+    uniform h-subset (chi-square and pair-frequency bounds)."""
+    log_n, h, cnt = 6, 5, 20000
+    n = 1 << log_n
+    nz = orc.sample_hwt(cnt, 1, log_n, h=h, seed=21)[:, 0] != 0
+    counts = nz.sum(0)
+    e = cnt * h / n
+    chi2 = float(((counts - e) ** 2 / e).sum())
+    assert chi2 < 2.0 * (n - 1)  # dof 63: mean 63, sd ~11
+    co = (nz[:, :, None].astype(np.float32) * nz[:, None, :]).sum(0)
+    exp = cnt * h * (h - 1) / (n * (n - 1))
+    off = co[~np.eye(n, dtype=bool)]
+    assert abs(off.mean() / exp - 1) < 0.02
+    assert ((off - exp) ** 2 / exp).mean() < 2.0

@@ -209,15 +209,26 @@ struct Limbs32 {
   __device__ __forceinline__ uint32_t cm(uint32_t k) const { return cm0 + k % L; }
 };
 
-// Tile <- limbs limb0 .. (16-byte global loads, 8-byte shared stores).
+// Tile <- limbs limb0 .. (16-byte global loads, 8-byte shared stores).  All
+// of a thread's loads are issued before its first store.
 template <class C>
 __device__ __forceinline__ void stage_in32(uint32_t* s, const uint32_t* g, uint32_t limb0, uint32_t count) {
-  for (uint32_t v = threadIdx.x * 4; v < (1u << C::T); v += C::THREADS * 4) {
+  constexpr int IT = (1 << C::T) / (C::THREADS * 4);
+  static_assert(IT * C::THREADS * 4 == (1 << C::T), "tile not a whole number of 16-byte chunks per thread");
+  uint4 d[IT];
+#pragma unroll
+  for (int i = 0; i < IT; ++i) {
+    const uint32_t v = (threadIdx.x + i * C::THREADS) * 4;
     const uint32_t limb = limb0 + (v >> C::K);
-    if (limb < count) {
-      const uint4 d = __ldg(reinterpret_cast<const uint4*>(g + ((size_t)limb << C::K) + (v & ((1u << C::K) - 1u))));
-      *reinterpret_cast<uint2*>(s + sidx(v)) = make_uint2(d.x, d.y);
-      *reinterpret_cast<uint2*>(s + sidx(v + 2)) = make_uint2(d.z, d.w);
+    if (limb < count)
+      d[i] = __ldg(reinterpret_cast<const uint4*>(g + ((size_t)limb << C::K) + (v & ((1u << C::K) - 1u))));
+  }
+#pragma unroll
+  for (int i = 0; i < IT; ++i) {
+    const uint32_t v = (threadIdx.x + i * C::THREADS) * 4;
+    if (limb0 + (v >> C::K) < count) {
+      *reinterpret_cast<uint2*>(s + sidx(v)) = make_uint2(d[i].x, d[i].y);
+      *reinterpret_cast<uint2*>(s + sidx(v + 2)) = make_uint2(d[i].z, d[i].w);
     }
   }
 }
@@ -245,7 +256,7 @@ __device__ __forceinline__ void stage_out32(const uint32_t* s, uint32_t* g, uint
 
 // DIR: 0 forward (reduced to [0, p)), 1 forward lazy ([0, 4p)), 2 backward.
 template <class C, int DIR>
-__global__ void __launch_bounds__(C::THREADS) k32_ntt(uint32_t* data, Limbs32 ls, const DevMod32* __restrict__ mods) {
+__global__ void __launch_bounds__(C::THREADS, 1024 / C::THREADS) k32_ntt(uint32_t* data, Limbs32 ls, const DevMod32* __restrict__ mods) {
   extern __shared__ __align__(16) uint32_t smem32[];
   constexpr int NR = C::NR;
   const uint32_t tid = threadIdx.x;
@@ -265,7 +276,7 @@ __global__ void __launch_bounds__(C::THREADS) k32_ntt(uint32_t* data, Limbs32 ls
 
 // c = INTT(NTT(a) * NTT(b)) per limb; c must not alias a or b.
 template <class C>
-__global__ void __launch_bounds__(C::THREADS) k32_polymul(uint32_t* c, const uint32_t* a, const uint32_t* b,
+__global__ void __launch_bounds__(C::THREADS, 1024 / C::THREADS) k32_polymul(uint32_t* c, const uint32_t* a, const uint32_t* b,
                                                           Limbs32 ls, const DevMod32* __restrict__ mods) {
   extern __shared__ __align__(16) uint32_t smem32[];
   constexpr int NR = C::NR, E = 1 << C::LOGE;

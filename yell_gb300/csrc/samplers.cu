@@ -11,8 +11,9 @@
 //   ZO(rho)  (poly.hpp:262-275): one random byte r per coefficient, shared by all
 //            limbs: r <= rho ? (r & 2 ? p - 1 : 1) : 0.
 //   HWT(h)   (poly.hpp:282-325): exactly h coefficients set to +-1 (same positions
-//            and signs in every limb), the positions uniform among all h-subsets;
-//            sign bit 1 of a random word: set -> +1, clear -> p - 1.
+//            and signs in every limb), the positions a pseudorandom h-subset (a
+//            keyed permutation of the indices, below); sign bit 1 of a random
+//            word: set -> +1, clear -> p - 1.
 //   gaussian (poly.hpp:238-258): a centred integer e per coefficient, shared by all
 //            limbs, times an amplifier, mapped e < 0 ? p + e : e.  e comes from a
 //            cumulative table of 64-bit thresholds (search of one random word), not
@@ -50,16 +51,24 @@ __host__ __device__ __forceinline__ uint64_t rand_word(uint64_t seed, uint64_t k
 constexpr uint64_t kSeedPositions = 0x5ca1ab1e0ddba11ull;
 constexpr uint64_t kSeedSigns = 0x0b5e55edc0ffee5ull;
 
+// Four consecutive words per thread (one limb row, since N >= 8): one
+// modulus lookup and two 16-byte stores per four words.
 __global__ void k_sample_uniform(uint64_t* out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
                                  const DevMod* __restrict__ mods, uint64_t seed) {
-  const size_t total = ((size_t)count * L) << log_n;
-  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
-    const uint32_t l = (uint32_t)((k >> log_n) % L);
+  const size_t quads = (((size_t)count * L) << log_n) >> 2;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < quads; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = t << 2;
+    const uint32_t l = (uint32_t)(k >> log_n) % L;
     const uint64_t p = __ldg(&mods[cm0 + l].p);
     const uint64_t mask = (2ull << (63 - __clzll(p))) - 1ull;  // 2^(floor(log2 p) + 1) - 1
-    uint64_t v = rand_word(seed, k) & mask;
-    if (v >= p) v -= p;
-    out[k] = v;
+    uint64_t v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      v[j] = rand_word(seed, k + j) & mask;
+      if (v[j] >= p) v[j] -= p;
+    }
+    reinterpret_cast<ulonglong2*>(out + k)[0] = make_ulonglong2(v[0], v[1]);
+    reinterpret_cast<ulonglong2*>(out + k)[1] = make_ulonglong2(v[2], v[3]);
   }
 }
 
@@ -96,59 +105,37 @@ __global__ void k_sample_shared_int(uint64_t* out, uint32_t count, uint32_t L, u
   }
 }
 
-// HWT: the h positions with the smallest random keys (a uniformly random
-// h-subset); found by an 8-bit-digit radix select over the 64-bit keys in one
-// CTA per poly, keys recomputed from the counter in every pass.
-constexpr int kHwtThreads = 512;
+// HWT: coefficient i of poly j is nonzero exactly when pi_j(i) < h, pi_j a
+// keyed pseudorandom permutation of [0, N) (a 6-round Feistel network over
+// the log2 N index bits, alternating halves of floor/ceil(log2 N / 2) bits,
+// round function splitmix64 of the round key plus the half).  A permutation
+// maps exactly h indices below h, so every poly has Hamming weight h; the
+// positions are a pseudorandom h-subset, as the reference's reservoir
+// sampling over a PRNG stream gives (details/poly.hpp:282-325).
+constexpr int kFeistelRounds = 6;
 
-__global__ void __launch_bounds__(kHwtThreads) k_sample_hwt(uint64_t* out, uint32_t L, uint32_t log_n, uint32_t cm0,
-                                                           const DevMod* __restrict__ mods, uint64_t seed, uint32_t h) {
-  __shared__ uint32_t hist[256];
-  __shared__ uint64_t prefix_s;
-  __shared__ uint32_t need_s;
-  const uint32_t n = 1u << log_n;
-  const uint64_t poly = blockIdx.x;
-  const uint64_t kbase = poly << log_n;
-  const uint64_t kseed = seed ^ kSeedPositions;
-  uint64_t prefix = 0;  // selected high digits of the threshold key
-  uint32_t need = h;    // how many keys below the threshold are still to take
-  for (int shift = 56; shift >= 0; shift -= 8) {
-    for (uint32_t t = threadIdx.x; t < 256; t += blockDim.x) hist[t] = 0;
-    __syncthreads();
-    const uint64_t hi_mask = shift == 56 ? 0ull : (~0ull << (shift + 8));
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-      const uint64_t key = rand_word(kseed, kbase + i);
-      if ((key & hi_mask) == prefix) atomicAdd(&hist[(key >> shift) & 0xFF], 1u);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t acc = 0, d = 0;
-      for (; d < 256; ++d) {
-        if (acc + hist[d] >= need) break;
-        acc += hist[d];
-      }
-      prefix_s = prefix | ((uint64_t)d << shift);
-      need_s = need - acc;
-    }
-    __syncthreads();
-    prefix = prefix_s;
-    need = need_s;
-    __syncthreads();
+__host__ __device__ __forceinline__ uint32_t feistel(uint32_t x, uint32_t bits, uint64_t key) {
+  uint32_t b = bits >> 1, a = bits - b;  // low field b bits, high field a bits
+  for (int r = 0; r < kFeistelRounds; ++r) {
+    const uint32_t lo = x & ((1u << b) - 1u), hi = x >> b;
+    const uint32_t f = (uint32_t)mix64(rand_word(key, (uint64_t)r) + lo);
+    x = (lo << a) | ((hi ^ f) & ((1u << a) - 1u));
+    const uint32_t t = a;  // the mixed field is now the low one
+    a = b;
+    b = t;
   }
-  // prefix is now the key of rank h (1-based): take keys < prefix, plus `need`
-  // keys equal to it (64-bit keys of distinct counters: ties do not occur in
-  // practice, and the first ones by index are taken if they do).
-  const uint64_t sseed = seed ^ kSeedSigns;
-  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-    const uint64_t key = rand_word(kseed, kbase + i);
-    bool take = key < prefix;
-    if (key == prefix) {
-      // rank among equal keys by index (rare path)
-      uint32_t before = 0;
-      for (uint32_t j = 0; j < i; ++j) before += rand_word(kseed, kbase + j) == prefix;
-      take = before < need;
-    }
-    const bool plus = (rand_word(sseed, kbase + i) & 2) != 0;
+  return x;
+}
+
+__global__ void k_sample_hwt(uint64_t* out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
+                             const DevMod* __restrict__ mods, uint64_t seed, uint32_t h) {
+  const size_t coeffs = (size_t)count << log_n;
+  const uint32_t nmask = (1u << log_n) - 1u;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < coeffs; k += (size_t)gridDim.x * blockDim.x) {
+    const size_t poly = k >> log_n;
+    const uint32_t i = (uint32_t)k & nmask;
+    const bool take = feistel(i, log_n, rand_word(seed ^ kSeedPositions, poly)) < h;
+    const bool plus = (rand_word(seed ^ kSeedSigns, k) & 2) != 0;
     for (uint32_t l = 0; l < L; ++l) {
       const uint64_t p = __ldg(&mods[cm0 + l].p);
       out[(((poly * L) + l) << log_n) + i] = take ? (plus ? 1ull : p - 1) : 0ull;
@@ -220,6 +207,7 @@ struct SamplerArgs {
 int prepare(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0, void* stream,
             SamplerArgs* a) {
   if (!d_out || count == 0) return fail(kInvalidArgument, "null output or zero count");
+  if (reinterpret_cast<uintptr_t>(d_out) % 16) return fail(kInvalidArgument, "d_out is not 16-byte aligned");
   int st = check_degree(log_n);
   if (st != kOk) return st;
   st = check_moduli(cm0, L);
@@ -242,7 +230,7 @@ int yell_dev_sample_uniform(uint64_t* d_out, uint32_t count, uint32_t L, uint32_
   int st = prepare(d_out, count, L, log_n, cm0, stream, &a);
   if (st != kOk) return st;
   LaunchScope ps("sample_uniform", a.st);
-  k_sample_uniform<<<grid_for(((size_t)count * L) << log_n), 256, 0, a.st>>>(d_out, count, L, log_n, cm0,
+  k_sample_uniform<<<grid_for((((size_t)count * L) << log_n) >> 2), 256, 0, a.st>>>(d_out, count, L, log_n, cm0,
                                                                             a.mods, seed);
   g_kernel_launches += 1;
   const cudaError_t e = cudaGetLastError();
@@ -270,7 +258,7 @@ int yell_dev_sample_hwt(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t lo
   int st = prepare(d_out, count, L, log_n, cm0, stream, &a);
   if (st != kOk) return st;
   LaunchScope ps("sample_hwt", a.st);
-  k_sample_hwt<<<count, kHwtThreads, 0, a.st>>>(d_out, L, log_n, cm0, a.mods, seed, h);
+  k_sample_hwt<<<grid_for((size_t)count << log_n), 256, 0, a.st>>>(d_out, count, L, log_n, cm0, a.mods, seed, h);
   g_kernel_launches += 1;
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? kOk : fail_cuda(e, "sample_hwt");
