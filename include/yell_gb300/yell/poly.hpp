@@ -1,11 +1,15 @@
 // Drop-in for yell/poly.hpp (include/yell/poly.hpp:43-171 and
-// include/yell/details/poly.hpp) without the samplers and GMP lifting:
-// yell::poly<N> keeps one host allocation per limb (raw_data() is the same
-// uint64_t** the reference exposes) and every NTT and arithmetic member runs
-// on the GPU through the yell_gb300 C ABI.
+// include/yell/details/poly.hpp): yell::poly<N> keeps one host allocation per
+// limb (raw_data() is the same uint64_t** the reference exposes) and every
+// NTT, arithmetic and sampling member runs on the GPU through the yell_gb300
+// C ABI.  The samplers take the reference's tag types (uniform, hwt_dist,
+// ZO_dist); the reference's gaussian<> wraps an MPFR-built FastGaussianNoise,
+// so the facade names the distribution instead (gaussian_dist).
 #pragma once
+#include <atomic>
 #include <cassert>
 #include <cstdlib>
+#include <random>
 #include <cstring>
 #include <stdexcept>
 #include <utility>
@@ -15,6 +19,37 @@
 #include "yell/params.hpp"
 
 namespace yell {
+
+// include/yell/poly.hpp:20-41
+struct uniform {};
+struct hwt_dist {
+  uint32_t hwt;
+  explicit hwt_dist(uint32_t hwt_) : hwt(hwt_) {}
+};
+struct ZO_dist {
+  uint8_t rho;  // P(1) = P(-1) ~ (rho / 0xFF) / 2
+  explicit ZO_dist(uint8_t rho_ = 0x7F) : rho(rho_) {}
+};
+// Discrete Gaussian exp(-e^2 / 2 sigma^2) on |e| <= tail, times amplifier.
+struct gaussian_dist {
+  double sigma;
+  uint32_t tail;
+  uint64_t amplifier;
+  explicit gaussian_dist(double sigma_ = 3.2, uint32_t tail_ = 19, uint64_t amp = 1)
+      : sigma(sigma_), tail(tail_), amplifier(amp) {}
+};
+
+namespace detail {
+// The reference's samplers draw from an unseeded stream; here each sampling
+// call takes the next seed of a process-wide counter that starts at a
+// random_device value, or at the value given to set_sampler_seed().
+inline std::atomic<uint64_t>& sampler_seed() {
+  static std::atomic<uint64_t> s{((uint64_t)std::random_device{}() << 32) ^ std::random_device{}()};
+  return s;
+}
+}  // namespace detail
+
+inline void set_sampler_seed(uint64_t seed) { detail::sampler_seed().store(seed); }
 
 template <size_t degree_>
 class poly {
@@ -44,6 +79,33 @@ class poly {
   explicit poly(size_t nmoduli_) : nmoduli(nmoduli_) {
     assert(nmoduli <= params::kMaxNbModuli);
     for (size_t cm = 0; cm < nmoduli; ++cm) _data.push_back(alloc_limb());
+  }
+  poly(size_t nmoduli_, uniform const& mode) : poly(nmoduli_) { set(mode); }
+  poly(size_t nmoduli_, hwt_dist const& mode) : poly(nmoduli_) { set(mode); }
+  poly(size_t nmoduli_, ZO_dist const& mode) : poly(nmoduli_) { set(mode); }
+  poly(size_t nmoduli_, gaussian_dist const& mode) : poly(nmoduli_) { set(mode); }
+
+  // details/poly.hpp:195-330, sampled on the device and copied into the limbs.
+  void set(uniform const&) {
+    sample([&](uint64_t* d, uint64_t seed) {
+      return yell_dev_sample_uniform(d, 1, (uint32_t)nmoduli, log_n, 0, seed, nullptr);
+    });
+  }
+  void set(hwt_dist const& mode) {
+    sample([&](uint64_t* d, uint64_t seed) {
+      return yell_dev_sample_hwt(d, 1, (uint32_t)nmoduli, log_n, 0, mode.hwt, seed, nullptr);
+    });
+  }
+  void set(ZO_dist const& mode) {
+    sample([&](uint64_t* d, uint64_t seed) {
+      return yell_dev_sample_zo(d, 1, (uint32_t)nmoduli, log_n, 0, mode.rho, seed, nullptr);
+    });
+  }
+  void set(gaussian_dist const& mode) {
+    sample([&](uint64_t* d, uint64_t seed) {
+      return yell_dev_sample_gaussian(d, 1, (uint32_t)nmoduli, log_n, 0, mode.sigma, mode.tail, mode.amplifier,
+                                      seed, nullptr);
+    });
   }
   ~poly() {
     for (auto& p : _data) std::free(p);
@@ -95,6 +157,22 @@ class poly {
 
   value_type const& operator()(size_t cm, size_t i) const { return _data[cm][i]; }
   value_type& operator()(size_t cm, size_t i) { return _data[cm][i]; }
+
+ private:
+  template <class F>
+  void sample(F&& fill) {
+    if (nmoduli == 0) return;
+    yell_dev_poly* h = nullptr;
+    check_status(yell_dev_poly_alloc((uint32_t)nmoduli, log_n, 0, &h), "sample (alloc)");
+    uint64_t* d = nullptr;
+    int st = yell_dev_poly_info(h, &d, nullptr, nullptr, nullptr);
+    if (st == YELL_OK) st = fill(d, detail::sampler_seed().fetch_add(1));
+    if (st == YELL_OK) st = yell_dev_poly_download(h, _data.data());
+    yell_dev_poly_free(h);
+    check_status(st, "sample");
+  }
+
+ public:
 
   // details/poly.hpp:170-186, one GPU call over all limbs each.
   void forward() { check_status(yell_poly_forward(_data.data(), (uint32_t)nmoduli, log_n), "forward"); }
