@@ -255,6 +255,14 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
     def step():
         y.dev_polymul(dc, da, db, pairs, L, LOG_N, 0, scratch=scratch, stream=stream)
 
+    if args.rows_only:  # profiling entry: one product, then the rows alone
+        step()
+        torch.cuda.synchronize()
+        rows = run_rows(torch, y, stream, dc)
+        if rank == 0:
+            print(json.dumps({"rows": rows}), flush=True)
+        return 0
+
     # ---- device-resident throughput (value) ---------------------------
     for _ in range(max(args.warmup, 3)):
         step()
@@ -597,6 +605,8 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch comparison")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving sweep")
+    ap.add_argument("--rows-only", action="store_true",
+                    help="run only the sampler, CRT-lifting and 32-bit measurements (for profiling)")
     ap.add_argument("--no-rows", action="store_true",
                     help="skip the sampler, CRT-lifting and 32-bit-moduli measurements")
     ap.add_argument("--no-autotune", action="store_true",

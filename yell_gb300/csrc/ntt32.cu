@@ -201,7 +201,7 @@ struct Cfg32 {
   static constexpr int T = LOGN > 11 ? LOGN : 11;
   static constexpr int LOGE = LOGN < 4 ? LOGN : (T == 15 ? 5 : 4);
   using C = TileCfg<T, LOGN, 0, LOGE>;
-  static constexpr size_t kSmem = tile_smem_words(1u << T) * sizeof(uint32_t);
+  static constexpr size_t kSmem = Smem<uint32_t>::words(1u << T) * sizeof(uint32_t);
 };
 
 struct Limbs32 {
@@ -209,8 +209,8 @@ struct Limbs32 {
   __device__ __forceinline__ uint32_t cm(uint32_t k) const { return cm0 + k % L; }
 };
 
-// Tile <- limbs limb0 .. (16-byte global loads, 8-byte shared stores).  All
-// of a thread's loads are issued before its first store.
+// Tile <- limbs limb0 .. (16-byte global loads and shared stores).  All of a
+// thread's loads are issued before its first store.
 template <class C>
 __device__ __forceinline__ void stage_in32(uint32_t* s, const uint32_t* g, uint32_t limb0, uint32_t count) {
   constexpr int IT = (1 << C::T) / (C::THREADS * 4);
@@ -226,10 +226,7 @@ __device__ __forceinline__ void stage_in32(uint32_t* s, const uint32_t* g, uint3
 #pragma unroll
   for (int i = 0; i < IT; ++i) {
     const uint32_t v = (threadIdx.x + i * C::THREADS) * 4;
-    if (limb0 + (v >> C::K) < count) {
-      *reinterpret_cast<uint2*>(s + sidx(v)) = make_uint2(d[i].x, d[i].y);
-      *reinterpret_cast<uint2*>(s + sidx(v + 2)) = make_uint2(d[i].z, d[i].w);
-    }
+    if (limb0 + (v >> C::K) < count) *reinterpret_cast<uint4*>(s + Smem<uint32_t>::idx(v)) = d[i];
   }
 }
 
@@ -239,9 +236,7 @@ __device__ __forceinline__ void stage_out32(const uint32_t* s, uint32_t* g, uint
   for (uint32_t v = threadIdx.x * 4; v < (1u << C::T); v += C::THREADS * 4) {
     const uint32_t limb = limb0 + (v >> C::K);
     if (limb < ls.count) {
-      const uint2 lo = *reinterpret_cast<const uint2*>(s + sidx(v));
-      const uint2 hi = *reinterpret_cast<const uint2*>(s + sidx(v + 2));
-      uint4 d = make_uint4(lo.x, lo.y, hi.x, hi.y);
+      uint4 d = *reinterpret_cast<const uint4*>(s + Smem<uint32_t>::idx(v));
       if (reduce) {
         const uint32_t p = __ldg(&mods[ls.cm(limb)].p), p2 = p << 1;
         d.x = fwd_correct(d.x, p, p2);

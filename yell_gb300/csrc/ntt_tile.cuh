@@ -36,6 +36,20 @@ namespace yell_gb300 {
 __host__ __device__ constexpr uint32_t sidx(uint32_t v) { return v + ((v >> 4) << 1); }
 __host__ __device__ constexpr uint32_t tile_smem_words(uint32_t n) { return n + (n >> 3); }
 
+// Shared-memory layout per word type.  64-bit words: sidx (2 pad words per
+// 16).  32-bit words: 4 pad words per 16, which keeps every aligned group of
+// 4 words 16-byte aligned, so a thread that owns 16 consecutive words (the
+// bottom round) moves them as four conflict-free 16-byte accesses.
+template <class W> struct Smem;
+template <> struct Smem<uint64_t> {
+  __host__ __device__ static constexpr uint32_t idx(uint32_t v) { return sidx(v); }
+  __host__ __device__ static constexpr uint32_t words(uint32_t n) { return tile_smem_words(n); }
+};
+template <> struct Smem<uint32_t> {
+  __host__ __device__ static constexpr uint32_t idx(uint32_t v) { return v + ((v >> 4) << 2); }
+  __host__ __device__ static constexpr uint32_t words(uint32_t n) { return n + (n >> 2); }
+};
+
 template <int T_, int K_, int LB_, int LOGE_>
 struct TileCfg {
   static constexpr int T = T_, K = K_, LB = LB_, LOGE = LOGE_;
@@ -87,25 +101,43 @@ struct Round {
 };
 
 // ---- register <-> shared memory ----------------------------------------------
+// A 32-bit round whose thread owns 2^R consecutive words starting at a
+// multiple of 16 (the bottom round of a row tile).
+template <class RG, class W>
+constexpr bool kContig32 = sizeof(W) == 4 && RG::EB == 0 && RG::BETA == 0 && RG::LB == 0 && RG::R >= 4;
+
 template <class RG, class W>
 __device__ __forceinline__ void smem_load(W* x, const W* s, uint32_t base_v) {
   constexpr int R = RG::R;
   using PW = typename PairOf<W>::type;
-  const W* sb = s + sidx(base_v);
-  if constexpr (RG::PAIRS) {
+  using SL = Smem<W>;
+  if constexpr (kContig32<RG, W>) {
+    const W* sb = s + SL::idx(base_v);
+#pragma unroll
+    for (int j = 0; j < (1 << R); j += 4) {
+      const uint4 v = *reinterpret_cast<const uint4*>(sb + j + ((j >> 4) << 2));
+      x[j] = v.x;
+      x[j + 1] = v.y;
+      x[j + 2] = v.z;
+      x[j + 3] = v.w;
+    }
+  } else if constexpr (RG::PAIRS) {
+    // base_v and the offsets occupy disjoint bits, so idx(base_v + off) = idx(base_v) + idx(off)
+    const W* sb = s + SL::idx(base_v);
 #pragma unroll
     for (int m = 0; m < RG::E / 2; ++m)
 #pragma unroll
       for (int j = 0; j < (1 << R); ++j) {
-        const PW v = *reinterpret_cast<const PW*>(sb + sidx(RG::off(2 * m, j)));
+        const PW v = *reinterpret_cast<const PW*>(sb + SL::idx(RG::off(2 * m, j)));
         x[((2 * m) << R) | j] = v.x;
         x[((2 * m + 1) << R) | j] = v.y;
       }
   } else {
+    const W* sb = s + SL::idx(base_v);
 #pragma unroll
     for (int ex = 0; ex < RG::E; ++ex)
 #pragma unroll
-      for (int j = 0; j < (1 << R); ++j) x[(ex << R) | j] = sb[sidx(RG::off(ex, j))];
+      for (int j = 0; j < (1 << R); ++j) x[(ex << R) | j] = sb[SL::idx(RG::off(ex, j))];
   }
 }
 
@@ -113,19 +145,45 @@ template <class RG, class W>
 __device__ __forceinline__ void smem_store(const W* x, W* s, uint32_t base_v) {
   constexpr int R = RG::R;
   using PW = typename PairOf<W>::type;
-  W* sb = s + sidx(base_v);
-  if constexpr (RG::PAIRS) {
+  using SL = Smem<W>;
+  if constexpr (kContig32<RG, W>) {
+    W* sb = s + SL::idx(base_v);
+#pragma unroll
+    for (int j = 0; j < (1 << R); j += 4)
+      *reinterpret_cast<uint4*>(sb + j + ((j >> 4) << 2)) = make_uint4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+  } else if constexpr (RG::PAIRS) {
+    W* sb = s + SL::idx(base_v);
 #pragma unroll
     for (int m = 0; m < RG::E / 2; ++m)
 #pragma unroll
       for (int j = 0; j < (1 << R); ++j)
-        *reinterpret_cast<PW*>(sb + sidx(RG::off(2 * m, j))) =
+        *reinterpret_cast<PW*>(sb + SL::idx(RG::off(2 * m, j))) =
             PairOf<W>::make(x[((2 * m) << R) | j], x[((2 * m + 1) << R) | j]);
   } else {
+    W* sb = s + SL::idx(base_v);
 #pragma unroll
     for (int ex = 0; ex < RG::E; ++ex)
 #pragma unroll
-      for (int j = 0; j < (1 << R); ++j) sb[sidx(RG::off(ex, j))] = x[(ex << R) | j];
+      for (int j = 0; j < (1 << R); ++j) sb[SL::idx(RG::off(ex, j))] = x[(ex << R) | j];
+  }
+}
+
+// NN consecutive twiddle pairs from src, which is aligned to NN pairs (every
+// caller's offset is a multiple of NN).  8-byte pairs (32-bit words) move
+// two per 16-byte load.
+template <int NN, class PW>
+__device__ __forceinline__ void ld_twiddles(PW* dst, const PW* __restrict__ src) {
+  if constexpr (sizeof(PW) == 8 && NN >= 2) {
+    const uint4* s4 = reinterpret_cast<const uint4*>(src);
+#pragma unroll
+    for (int i = 0; i < NN / 2; ++i) {
+      const uint4 v = __ldg(s4 + i);
+      dst[2 * i] = PW{v.x, v.y};
+      dst[2 * i + 1] = PW{v.z, v.w};
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < NN; ++i) dst[i] = __ldg(src + i);
   }
 }
 
@@ -142,9 +200,7 @@ __device__ __forceinline__ void ct_stages(W* x, const PW* __restrict__ tw, uint3
     constexpr int NN = (k + 1 < R) ? (2 << k) : 1;
     PW wn[NN];
     if constexpr (k + 1 < R) {
-      const PW* src = tw + (1u << (s_first + k + 1)) + (gr << (k + 1));
-#pragma unroll
-      for (int jj = 0; jj < NN; ++jj) wn[jj] = __ldg(src + jj);
+      ld_twiddles<NN>(wn, tw + (1u << (s_first + k + 1)) + (gr << (k + 1)));
     }
 #pragma unroll
     for (int jj = 0; jj < NJ; ++jj)
@@ -212,9 +268,7 @@ __device__ __forceinline__ void gs_stages(W* x, const PW* __restrict__ itw, uint
       constexpr int NN = NEXT ? (1 << (R - 2 - k)) : 1;
       PW wn[NN];
       if constexpr (NEXT) {
-        const PW* src = itw + (1u << (top - k - 1)) + (gr << (R - 2 - k));
-#pragma unroll
-        for (int jj = 0; jj < NN; ++jj) wn[jj] = __ldg(src + jj);
+        ld_twiddles<NN>(wn, itw + (1u << (top - k - 1)) + (gr << (R - 2 - k)));
       }
       const W np = (W)(0 - m.p), p2 = (W)(m.p << 1);
 #pragma unroll
@@ -240,9 +294,7 @@ __device__ __forceinline__ void gs_round(W* x, uint32_t log_n, uint32_t sigma_fi
   constexpr int N0 = ONLY_LAST ? 1 : (1 << (R - 1));
   PW w0[N0];
   if constexpr (!ONLY_LAST) {
-    const PW* src = m.inv + (1u << top) + (gr << (R - 1));
-#pragma unroll
-    for (int jj = 0; jj < N0; ++jj) w0[jj] = __ldg(src + jj);
+    ld_twiddles<N0>(w0, m.inv + (1u << top) + (gr << (R - 1)));
   }
   gs_stages<R, RG::E, LAST, 0>(x, m.inv, top, gr, m, w0);
 }
