@@ -172,6 +172,52 @@ def cpu_reference_run(a, b, threads: int):
     return secs, kind
 
 
+def rows_cpu_baseline(dc_host) -> dict:
+    """CPU timings of the rows beside the polymul path, on bounded samples of
+    the same workloads (single thread: the restatements are scalar C / Python):
+    samplers (oracle/samplers_oracle.c), CRT lifting (the big-integer
+    restatement of gmp::poly2mpz in oracle/crt.py), the 32-bit polymul
+    (oracle/yell_oracle32.c, or the reference's 32-bit build where present)."""
+    import oracle
+    from oracle.crt import poly2bigint
+
+    orc = oracle.Oracle("port")
+    out = {}
+
+    def timed(fn, min_s=0.5):
+        reps, t0 = 0, time.perf_counter()
+        while True:
+            fn()
+            reps += 1
+            el = time.perf_counter() - t0
+            if el >= min_s or reps >= 50:
+                return el / reps
+
+    words = L * N  # one poly of L = 32 limbs, N = 2^16
+    for name, fn in (("uniform", lambda: orc.sample_uniform(1, L, LOG_N, seed=1)),
+                     ("zo", lambda: orc.sample_zo(1, L, LOG_N, seed=2)),
+                     ("gaussian", lambda: orc.sample_gaussian(1, L, LOG_N, seed=3)),
+                     ("hwt_192", lambda: orc.sample_hwt(1, L, LOG_N, 192, seed=4))):
+        sec = timed(fn)
+        out[f"sample_{name}"] = {"gbs": 8 * words / sec / 1e9, "cores": 1, "kind": "port",
+                                 "sample": f"1 poly x {L} limbs x 2^{LOG_N}"}
+    ncoef = 1024
+    limbs = np.ascontiguousarray(dc_host[0, :, :ncoef])
+    primes = [orc.prime(j) for j in range(L)]
+    sec = timed(lambda: poly2bigint(limbs, primes), min_s=1.0)
+    out["crt_lift"] = {"coefficients_per_s": ncoef / sec, "cores": 1, "kind": "port",
+                       "sample": f"{ncoef} coefficients at L = {L} (Python integers, gmp::poly2mpz steps)"}
+    o32 = oracle.Oracle32("ref") if oracle.ref32_available() else oracle.Oracle32("port")
+    n32 = 1 << 15
+    rng = np.random.default_rng(0)
+    a32 = (rng.integers(0, 1 << 29, (L, n32))).astype(np.uint32)
+    b32 = (rng.integers(0, 1 << 29, (L, n32))).astype(np.uint32)
+    sec = timed(lambda: o32.polymul(a32, b32, 15), min_s=1.0)
+    out["polymul32"] = {"limb_ntts_per_s": 3 * L / sec, "cores": 1, "kind": o32.which if o32.which == "port" else "reference",
+                        "sample": f"1 pair x {L} limbs at N = 2^15"}
+    return out
+
+
 def run_reference(args, rank: int, world: int) -> int:
     if rank != 0:
         return 0
@@ -409,6 +455,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
                "kind": kind,
                "sample": f"{reps} x the full batch ({pairs} pairs x {L} limbs), {total:.2f} s wall, "
                          f"~{total * threads:.0f} core-s"}
+        if rows is not None:
+            rows["cpu_baseline"] = rows_cpu_baseline(dc.cpu().numpy().view(np.uint64).reshape(pairs, L, N))
 
     if rank == 0:
         line = {

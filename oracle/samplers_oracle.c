@@ -43,10 +43,12 @@ static uint64_t bitlen_mask(uint64_t p) {
 
 void orc_sample_uniform(uint64_t* out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0, uint64_t seed) {
   const uint64_t n = 1ull << log_n;
-  for (uint64_t k = 0; k < (uint64_t)count * L * n; ++k) {
-    const uint64_t p = orc_prime(cm0 + (uint32_t)((k / n) % L));
-    uint64_t v = word(seed, k) & bitlen_mask(p);
-    out[k] = v >= p ? v - p : v;
+  for (uint64_t row = 0; row < (uint64_t)count * L; ++row) {
+    const uint64_t p = orc_prime(cm0 + (uint32_t)(row % L)), mask = bitlen_mask(p);
+    for (uint64_t k = row * n; k < (row + 1) * n; ++k) {
+      const uint64_t v = word(seed, k) & mask;
+      out[k] = v >= p ? v - p : v;
+    }
   }
 }
 
