@@ -266,10 +266,12 @@ int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_
   }
   cudaStream_t h2d = ctx->pipe_stream[0], comp = ctx->pipe_stream[1], d2h = ctx->pipe_stream[2];
   uint32_t k = 0;
-  for (uint32_t p0 = 0; p0 < pairs; p0 += cp, ++k) {
+  for (uint32_t p0 = 0, np = 0; p0 < pairs; p0 += np, ++k) {
     const int s = (int)(k % DeviceContext::kPipeSlots);
     const bool reuse = k >= (uint32_t)DeviceContext::kPipeSlots;
-    const uint32_t np = std::min(cp, pairs - p0);
+    // the last cp pairs go one at a time: the compute and D2H left after the
+    // final H2D (the pipeline's tail) then cover one pair, not cp
+    np = pairs - p0 > cp ? cp : 1;
     const size_t w = np * pair_words;
     uint64_t* da = ctx->pipe_buf[s].ptr;
     uint64_t* db = da + cw;
