@@ -11,10 +11,10 @@
 //         f_j = floor(y_j * floor(2^125 / q_j) / 2^61); the estimate is v or v - 1
 //   x   = sum_j y_j * (Q/q_j) - v * Q, minus Q once more when still >= Q
 // sum_j y_j * (Q/q_j) = Q * sum_j y_j / q_j, so with the exact v this is x.
-// The multi-word sums run column by column (product scanning): a thread owns
-// one coefficient, keeps its y_j in shared memory and streams out the words
-// of x, least significant first; x is written as W little-endian words per
-// coefficient, W = words of Q, coefficient-major.
+// The multi-word sums run over 32-bit digits: a thread owns one coefficient
+// and keeps its y_j in shared memory; the cofactor digits are staged per tile
+// of output digits and shared by the block; x is written as W little-endian
+// words per coefficient, W = words of Q, coefficient-major.
 #include <cstring>
 #include <map>
 #include <memory>
@@ -36,8 +36,7 @@ namespace {
 
 typedef unsigned __int128 u128;
 
-constexpr uint32_t kCrtThreads = 64;
-constexpr uint32_t kCrtMaxModuli = 400;  // 64 threads * 400 words * 8 B = 200 KB of y per block
+constexpr uint32_t kCrtMaxModuli = 400;  // 32 threads * 400 words * 8 B = 100 KB of y per block
 
 // Per (device, cm0, L) constants, device resident:
 //   mods[j] = {q_j, inv_j, inv_j', c_j} with inv_j = (Q/q_j)^-1 mod q_j, inv_j' its
@@ -154,32 +153,52 @@ uint32_t crt_words(uint32_t cm0, uint32_t L) {
   return (uint32_t)Q.size();
 }
 
-__device__ __forceinline__ void acc_mac(uint64_t& a0, uint64_t& a1, uint64_t& a2, uint64_t x, uint64_t y) {
-  const uint64_t lo = x * y;
-  const uint64_t hi = __umul64hi(x, y);
-  asm("add.cc.u64 %0, %0, %3;\n\t"
-      "addc.cc.u64 %1, %1, %4;\n\t"
-      "addc.u64 %2, %2, 0;"
-      : "+l"(a0), "+l"(a1), "+l"(a2)
-      : "l"(lo), "l"(hi));
+// 32-bit digit d of a little-endian word array of `words` words (0 outside).
+__device__ __forceinline__ uint32_t digit(const uint64_t* w, int d, uint32_t words) {
+  return (d >= 0 && (uint32_t)d < 2 * words) ? __ldg(reinterpret_cast<const uint32_t*>(w) + d) : 0u;
 }
 
-// d = a - b - borrow_in, returns the borrow out.
+// (r0, r1, r2) += a * b, a 64-bit product into a 96-bit accumulator.
+__device__ __forceinline__ void mac32(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t a, uint32_t b) {
+  asm("mad.lo.cc.u32 %0, %3, %4, %0;\n\t"
+      "madc.hi.cc.u32 %1, %3, %4, %1;\n\t"
+      "addc.u32 %2, %2, 0;"
+      : "+r"(r0), "+r"(r1), "+r"(r2)
+      : "r"(a), "r"(b));
+}
+
+// d = a - b - bin (32-bit), returns the borrow out.
+__device__ __forceinline__ uint32_t sub_borrow32(uint32_t a, uint32_t b, uint32_t bin, uint32_t* d) {
+  const uint32_t t = a - b;
+  *d = t - bin;
+  return (uint32_t)(a < b) | (uint32_t)(t < bin);
+}
+
 __device__ __forceinline__ uint32_t sub_borrow(uint64_t a, uint64_t b, uint32_t bin, uint64_t* d) {
   const uint64_t t = a - b;
-  const uint32_t b1 = a < b;
   *d = t - bin;
-  return b1 | (t < (uint64_t)bin);
+  return (uint32_t)(a < b) | (uint32_t)(t < (uint64_t)bin);
 }
 
-__global__ void __launch_bounds__(kCrtThreads) k_crt_lift(uint64_t* __restrict__ out, const uint64_t* __restrict__ in,
-                                                          uint32_t count, uint32_t L, uint32_t log_n,
-                                                          const CrtConst* __restrict__ mods,
-                                                          const uint64_t* __restrict__ cof,
-                                                          const uint64_t* __restrict__ qw, uint32_t W) {
-  extern __shared__ uint64_t ys[];  // [L][kCrtThreads]
+// Output digits are produced in tiles of kDigitTile 32-bit digits.  For one
+// tile the block stages digits [e0 - 1, e0 + kDigitTile) of every cofactor in
+// shared memory; each thread then runs over j once, adding
+// y_j[0] * C_j[d] + y_j[1] * C_j[d - 1] into one 96-bit accumulator per digit
+// d of the tile (independent chains), and finally resolves the carries digit
+// by digit, subtracting v * Q on the way.
+constexpr int kDigitTile = 16;
+
+template <int T>
+__global__ void __launch_bounds__(T) k_crt_lift(uint64_t* __restrict__ out, const uint64_t* __restrict__ in,
+                                                uint32_t count, uint32_t L, uint32_t log_n,
+                                                const CrtConst* __restrict__ mods, const uint64_t* __restrict__ cof,
+                                                const uint64_t* __restrict__ qw, uint32_t W) {
+  extern __shared__ __align__(16) uint64_t smem_crt[];
+  uint64_t* ys = smem_crt;                                          // [L][T]
+  uint32_t* cs = reinterpret_cast<uint32_t*>(smem_crt + (size_t)L * T);  // [L][kDigitTile + 1]
+  constexpr int CT = kDigitTile + 1;
   const uint64_t coeffs = (uint64_t)count << log_n;
-  const uint64_t g = (uint64_t)blockIdx.x * kCrtThreads + threadIdx.x;
+  const uint64_t g = (uint64_t)blockIdx.x * T + threadIdx.x;
   const bool live = g < coeffs;
   const uint64_t poly = g >> log_n;
   const uint64_t i = g & ((1ull << log_n) - 1);
@@ -191,41 +210,75 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_lift(uint64_t* __restrict__
     uint64_t y = 0;
     if (live) {
       const CrtConst m = mods[j];
-      const uint64_t r = in[(poly * L + j) * n + i];
-      y = mulmod_shoup(r, m.inv, m.inv_s, m.q);
+      y = mulmod_shoup(in[(poly * L + j) * n + i], m.inv, m.inv_s, m.q);
       const uint64_t pl = y * m.c, ph = __umul64hi(y, m.c);
       const uint64_t f = (pl >> 61) | (ph << 3);  // floor(y c / 2^61) < 2^64
       asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, 0;" : "+l"(f_lo), "+l"(f_hi) : "l"(f));
     }
-    ys[j * kCrtThreads + threadIdx.x] = y;
+    ys[j * T + threadIdx.x] = y;
   }
-  __syncthreads();
-  if (!live) return;
   const uint64_t v = f_hi;
+  const uint32_t v0 = (uint32_t)v, v1 = (uint32_t)(v >> 32);
 
   uint64_t* dst = out + g * W;
-  uint64_t x0 = 0, x1 = 0, x2 = 0;  // column accumulator of sum y_j (Q/q_j)
-  uint64_t q0 = 0, q1 = 0;          // column accumulator of v Q
-  uint32_t br = 0, bq = 0;          // borrows of x - vQ and of (x - vQ) - Q
-  for (uint32_t w = 0; w <= W; ++w) {
-    if (w < W) {
-      for (uint32_t j = 0; j < L; ++j) acc_mac(x0, x1, x2, ys[j * kCrtThreads + threadIdx.x], __ldg(&cof[(size_t)j * W + w]));
-      const uint64_t qword = __ldg(&qw[w]);
-      const uint64_t lo = v * qword, hi = __umul64hi(v, qword);
-      asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, %3;" : "+l"(q0), "+l"(q1) : "l"(lo), "l"(hi));
+  const int digits = 2 * (int)W + 2;  // two digits past Q for the borrow chains
+  uint64_t cx = 0, cq = 0;            // carries of sum y_j (Q/q_j) and of v Q, in digits
+  uint32_t br = 0, bq = 0, lo_digit = 0;
+  for (int e0 = 0; e0 < digits; e0 += kDigitTile) {
+    __syncthreads();  // previous tile's cofactor digits are no longer read
+    for (uint32_t k = threadIdx.x; k < L * CT; k += T) {
+      const uint32_t j = k / CT;
+      const int d = e0 - 1 + (int)(k - j * CT);
+      cs[k] = digit(cof + (size_t)j * W, d, W);
     }
-    uint64_t r;
-    br = sub_borrow(x0, q0, br, &r);
-    uint64_t alt;
-    bq = sub_borrow(r, w < W ? __ldg(&qw[w]) : 0ull, bq, &alt);
-    if (w < W) dst[w] = r;
-    x0 = x1;
-    x1 = x2;
-    x2 = 0;
-    q0 = q1;
-    q1 = 0;
+    __syncthreads();
+    if (live) {
+      uint32_t r0[kDigitTile], r1[kDigitTile], r2[kDigitTile];
+#pragma unroll
+      for (int t = 0; t < kDigitTile; ++t) r0[t] = r1[t] = r2[t] = 0;
+      for (uint32_t j = 0; j < L; ++j) {
+        const uint64_t y = ys[j * T + threadIdx.x];
+        const uint32_t y0 = (uint32_t)y, y1 = (uint32_t)(y >> 32);
+        const uint32_t* c = cs + j * CT;  // c[t + 1] = C_j[e0 + t]
+        uint32_t prev = c[0];
+#pragma unroll
+        for (int t = 0; t < kDigitTile; ++t) {
+          const uint32_t cur = c[t + 1];
+          mac32(r0[t], r1[t], r2[t], y0, cur);
+          mac32(r0[t], r1[t], r2[t], y1, prev);
+          prev = cur;
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < kDigitTile; ++t) {
+        const int d = e0 + t;
+        if (d < digits) {
+          // x digit: accumulator + carry
+          uint64_t xl = ((uint64_t)r1[t] << 32 | r0[t]);
+          const uint64_t s = xl + cx;
+          const uint64_t xh = (uint64_t)r2[t] + (s < xl ? 1u : 0u);
+          const uint32_t xd = (uint32_t)s;
+          cx = (s >> 32) | (xh << 32);
+          // (v Q) digit
+          const uint32_t qd0 = digit(qw, d, W), qd1 = digit(qw, d - 1, W);
+          const uint64_t pq = (uint64_t)v0 * qd0, pq2 = (uint64_t)v1 * qd1;
+          const uint64_t sq = pq + pq2;
+          const uint64_t sq2 = sq + cq;
+          const uint64_t qh = (uint64_t)(sq < pq) + (uint64_t)(sq2 < sq);
+          const uint32_t qd = (uint32_t)sq2;
+          cq = (sq2 >> 32) | (qh << 32);
+          uint32_t rd, ad;
+          br = sub_borrow32(xd, qd, br, &rd);
+          bq = sub_borrow32(rd, qd0, bq, &ad);
+          if (d < 2 * (int)W) {
+            if (d & 1) dst[d >> 1] = (uint64_t)rd << 32 | lo_digit;
+            else lo_digit = rd;
+          }
+        }
+      }
+    }
   }
-  if (bq == 0) {  // x - vQ >= Q: the estimate of v was one short
+  if (live && bq == 0) {  // x - vQ >= Q: the estimate of v was one short
     uint32_t b = 0;
     for (uint32_t w = 0; w < W; ++w) {
       uint64_t d;
@@ -235,30 +288,41 @@ __global__ void __launch_bounds__(kCrtThreads) k_crt_lift(uint64_t* __restrict__
   }
 }
 
+size_t crt_smem(uint32_t L, int threads) {
+  return (size_t)L * threads * sizeof(uint64_t) + (size_t)L * (kDigitTile + 1) * sizeof(uint32_t);
+}
+
 int crt_lift(uint64_t* d_out, const uint64_t* d_in, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
              cudaStream_t st, int device) {
   const CrtTables* t = nullptr;
   int s = crt_tables(device, cm0, L, &t);
   if (s != kOk) return s;
-  const size_t smem = (size_t)L * kCrtThreads * sizeof(uint64_t);
+  // 64 threads per block while their y_j fit in 160 KB of shared memory, else 32
+  const int threads = crt_smem(L, 64) <= (160u << 10) ? 64 : 32;
+  const size_t smem = crt_smem(L, threads);
   cudaError_t e = cudaSuccess;
   {
-    // the shared-memory limit is a per-device attribute of the kernel
+    // the shared-memory limit is a per-device attribute of each kernel
     static std::mutex mu;
     static std::set<int> done;
     std::lock_guard<std::mutex> g(mu);
     if (!done.count(device)) {
-      e = cudaFuncSetAttribute(k_crt_lift, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)(kCrtMaxModuli * kCrtThreads * sizeof(uint64_t)));
+      e = cudaFuncSetAttribute(k_crt_lift<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(160u << 10));
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_crt_lift<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)crt_smem(kCrtMaxModuli, 32));
       if (e != cudaSuccess) return fail_cuda(e, "crt attributes");
       done.insert(device);
     }
   }
   const uint64_t coeffs = (uint64_t)count << log_n;
-  const uint32_t blocks = (uint32_t)((coeffs + kCrtThreads - 1) / kCrtThreads);
+  const uint32_t blocks = (uint32_t)((coeffs + threads - 1) / threads);
   {
     LaunchScope ps("crt_lift", st);
-    k_crt_lift<<<blocks, kCrtThreads, smem, st>>>(d_out, d_in, count, L, log_n, t->mods, t->cofactors, t->q, t->W);
+    if (threads == 64)
+      k_crt_lift<64><<<blocks, 64, smem, st>>>(d_out, d_in, count, L, log_n, t->mods, t->cofactors, t->q, t->W);
+    else
+      k_crt_lift<32><<<blocks, 32, smem, st>>>(d_out, d_in, count, L, log_n, t->mods, t->cofactors, t->q, t->W);
     g_kernel_launches += 1;
   }
   e = cudaGetLastError();
