@@ -18,6 +18,8 @@
 #include <utility>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "kernels.h"
 #include "ntt_tile.cuh"
 #include "profiler.h"
@@ -324,6 +326,189 @@ __global__ void __launch_bounds__(C::THREADS, 1024 / C::THREADS) k32_polymul(uin
   stage_out32<C>(smem32, c, limb0, ls, mods, false);
 }
 
+
+// ---- polymul by a CTA pair (thread-block cluster of 2) ------------------------
+// For N = 2^14 and 2^15 one limb is split over two CTAs of one cluster, each
+// holding half of it (2^(log N - 1) words, 80 KB at 2^15), so two CTAs fit on
+// an SM.  The forward stage that pairs words N/2 apart (stage 0, twiddle
+// w[1]) is applied while loading: each CTA reads both halves (the second read
+// of a word comes from L2) and keeps the butterfly output of its own half.
+// Stages 1 .. log N - 1 stay inside a half (group G = the CTA's rank).  The
+// inverse's last layer (N^-1 scaling fused) pairs the halves again: after a
+// cluster barrier each CTA reads the peer's words through distributed shared
+// memory and writes its own half of the outputs.
+template <int LOGN>
+struct PairCfg32 {
+  static constexpr int H = LOGN - 1;
+  using C = TileCfg<H, H, 0, 5>;
+  static constexpr size_t kSmem = Smem<uint32_t>::words(1u << H) * sizeof(uint32_t);
+};
+
+// Forward NTT of one half limb of `src` (the limb's first word) into the
+// bottom-round registers x of this thread: stage 0 while loading, stages
+// 1 .. log N - 1 in shared memory, the last round in registers.
+template <class C, bool CLUSTER_SYNC = false>
+__device__ __forceinline__ void pair_forward(uint32_t* x, const uint32_t* __restrict__ src, uint32_t* smem32,
+                                             uint32_t tid, uint32_t r, const DevMod32& m, uint2 w1) {
+  constexpr int H = C::K, NR = C::NR;
+  constexpr uint32_t half = 1u << H;
+  constexpr int IT = (int)(half / (C::THREADS * 4));
+  constexpr int BATCH = IT < 2 ? IT : 2;  // loads in flight per thread: 2 x BATCH x 16 bytes
+  using RB = Round<C, NR - 1>;
+  const uint32_t p = m.p, p2 = p << 1, np = 0u - p;
+#pragma unroll 1  // unrolled, the loads of every batch get hoisted together and spill
+  for (int i0 = 0; i0 < IT; i0 += BATCH) {
+    uint4 lo[BATCH], hi[BATCH];
+#pragma unroll
+    for (int i = 0; i < BATCH; ++i) {
+      const uint32_t v = (tid + (i0 + i) * C::THREADS) * 4;
+      lo[i] = __ldg(reinterpret_cast<const uint4*>(src + v));
+      hi[i] = __ldg(reinterpret_cast<const uint4*>(src + half + v));
+    }
+#pragma unroll
+    for (int i = 0; i < BATCH; ++i) {
+      const uint32_t v = (tid + (i0 + i) * C::THREADS) * 4;
+      uint32_t u0[4] = {lo[i].x, lo[i].y, lo[i].z, lo[i].w}, u1[4] = {hi[i].x, hi[i].y, hi[i].z, hi[i].w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) ct_bfly(u0[k], u1[k], w1.x, w1.y, np, p2);
+      *reinterpret_cast<uint4*>(smem32 + Smem<uint32_t>::idx(v)) =
+          r == 0 ? make_uint4(u0[0], u0[1], u0[2], u0[3]) : make_uint4(u1[0], u1[1], u1[2], u1[3]);
+    }
+  }
+  // an in-place transform may overwrite src only once both CTAs have read it
+  if constexpr (CLUSTER_SYNC) cooperative_groups::this_cluster().sync();
+  else __syncthreads();
+  fwd_rounds<C, 0, NR - 1>(smem32, tid, 1, r, m.fwd, p, true);
+  const uint32_t bb = RB::base(tid);
+  smem_load<RB>(x, smem32, bb);
+  ct_round<RB>(x, m.fwd, 1u + RB::HI, RB::gr(bb, r), p);
+}
+
+template <class C>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, 2)
+    k32_polymul_pair(uint32_t* c, const uint32_t* a, const uint32_t* b, Limbs32 ls,
+                     const DevMod32* __restrict__ mods) {
+  namespace cg = cooperative_groups;
+  extern __shared__ __align__(16) uint32_t smem32[];
+  constexpr int H = C::K, NR = C::NR, E = 1 << C::LOGE;
+  constexpr uint32_t log_n = H + 1, half = 1u << H;
+  constexpr int IT = (int)(half / (C::THREADS * 4));
+  using RB = Round<C, NR - 1>;
+  static_assert(RB::R == C::LOGE && RB::BETA == 0 && RB::EB == 0, "bottom round must own contiguous words");
+  static_assert(IT * C::THREADS * 4 == (int)half, "half limb not a whole number of 16-byte chunks per thread");
+  static_assert(IT % 2 == 0 || IT == 1, "stage-in batches of two");
+  cg::cluster_group cluster = cg::this_cluster();
+  const uint32_t r = cluster.block_rank();  // which half of the limb
+  const uint32_t limb = blockIdx.x >> 1;    // grid = 2 x limbs, every CTA active
+  const uint32_t tid = threadIdx.x;
+  const DevMod32 m = load_mod(mods, ls.cm(limb));
+  const uint32_t p = m.p, p2 = p << 1, np = 0u - p;
+  const uint2 w1 = __ldg(m.fwd + 1);
+  const size_t lbase = (size_t)limb << log_n;
+  const uint32_t bb = RB::base(tid);
+  uint32_t* park = c + lbase + r * half + bb;
+  uint32_t x[E];
+  pair_forward<C>(x, a + lbase, smem32, tid, r, m, w1);
+#pragma unroll
+  for (int i = 0; i < E; i += 4)
+    *reinterpret_cast<uint4*>(park + i) = make_uint4(fwd_correct(x[i], p, p2), fwd_correct(x[i + 1], p, p2),
+                                                     fwd_correct(x[i + 2], p, p2), fwd_correct(x[i + 3], p, p2));
+  __syncthreads();  // the buffer is reused for b
+  pair_forward<C>(x, b + lbase, smem32, tid, r, m, w1);
+#pragma unroll
+  for (int i = 0; i < E; i += 4) {
+    const uint4 ah = *reinterpret_cast<const uint4*>(park + i);  // written above by this thread
+    x[i] = mulmod_barrett(ah.x, fwd_correct(x[i], p, p2), p, m.pn);
+    x[i + 1] = mulmod_barrett(ah.y, fwd_correct(x[i + 1], p, p2), p, m.pn);
+    x[i + 2] = mulmod_barrett(ah.z, fwd_correct(x[i + 2], p, p2), p, m.pn);
+    x[i + 3] = mulmod_barrett(ah.w, fwd_correct(x[i + 3], p, p2), p, m.pn);
+  }
+  gs_round<RB, false>(x, log_n, (uint32_t)RB::BETA, RB::gr(bb, r), m);
+  smem_store<RB>(x, smem32, bb);
+  __syncthreads();
+  inv_rounds<C, NR - 2, -1, false>(smem32, tid, log_n, 0, r, m, true);
+  // last layer across the pair: u = word i (rank 0), w = word i + N/2 (rank 1)
+  cluster.sync();
+  const uint32_t* peer = cluster.map_shared_rank(smem32, (int)(r ^ 1u));
+  uint32_t* dst = c + lbase + r * half;
+#pragma unroll
+  for (int i = 0; i < IT; ++i) {
+    const uint32_t v = (tid + i * C::THREADS) * 4;
+    const uint4 own = *reinterpret_cast<const uint4*>(smem32 + Smem<uint32_t>::idx(v));
+    const uint4 oth = *reinterpret_cast<const uint4*>(peer + Smem<uint32_t>::idx(v));
+    const uint32_t o[4] = {own.x, own.y, own.z, own.w}, q[4] = {oth.x, oth.y, oth.z, oth.w};
+    uint32_t res[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint32_t u = r == 0 ? o[k] : q[k], w = r == 0 ? q[k] : o[k];
+      res[k] = r == 0 ? mulmod_shoup(u + w, m.inv_n, m.inv_n_s, p)
+                      : mulmod_shoup(u - w + p2, m.inv_n_iphi, m.inv_n_iphi_s, p);
+    }
+    *reinterpret_cast<uint4*>(dst + v) = make_uint4(res[0], res[1], res[2], res[3]);
+  }
+  cluster.sync();  // the peer may still be reading this CTA's shared memory
+}
+
+// In-place NTT of one limb by a CTA pair (DIR: 0 forward, 1 forward lazy,
+// 2 backward), same split as k32_polymul_pair.
+template <class C, int DIR>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, 2)
+    k32_ntt_pair(uint32_t* data, Limbs32 ls, const DevMod32* __restrict__ mods) {
+  namespace cg = cooperative_groups;
+  extern __shared__ __align__(16) uint32_t smem32[];
+  constexpr int H = C::K, NR = C::NR, E = 1 << C::LOGE;
+  constexpr uint32_t log_n = H + 1, half = 1u << H;
+  constexpr int IT = (int)(half / (C::THREADS * 4));
+  using RB = Round<C, NR - 1>;
+  cg::cluster_group cluster = cg::this_cluster();
+  const uint32_t r = cluster.block_rank();
+  const uint32_t limb = blockIdx.x >> 1;
+  const uint32_t tid = threadIdx.x;
+  const DevMod32 m = load_mod(mods, ls.cm(limb));
+  const uint32_t p = m.p, p2 = p << 1;
+  uint32_t* base = data + ((size_t)limb << log_n);
+  if constexpr (DIR != 2) {
+    uint32_t x[E];
+    pair_forward<C, true>(x, base, smem32, tid, r, m, __ldg(m.fwd + 1));
+    uint32_t* out = base + r * half + RB::base(tid);
+#pragma unroll
+    for (int i = 0; i < E; i += 4) {
+      uint4 v = make_uint4(x[i], x[i + 1], x[i + 2], x[i + 3]);
+      if (DIR == 0) v = make_uint4(fwd_correct(v.x, p, p2), fwd_correct(v.y, p, p2), fwd_correct(v.z, p, p2),
+                                   fwd_correct(v.w, p, p2));
+      *reinterpret_cast<uint4*>(out + i) = v;
+    }
+  } else {
+    const uint32_t* own = base + r * half;
+#pragma unroll 1
+    for (int i = 0; i < IT; ++i) {
+      const uint32_t v = (tid + i * C::THREADS) * 4;
+      *reinterpret_cast<uint4*>(smem32 + Smem<uint32_t>::idx(v)) = __ldg(reinterpret_cast<const uint4*>(own + v));
+    }
+    __syncthreads();
+    inv_rounds<C, NR - 1, -1, false>(smem32, tid, log_n, 0, r, m, true);
+    cluster.sync();
+    const uint32_t* peer = cluster.map_shared_rank(smem32, (int)(r ^ 1u));
+    uint32_t* dst = base + r * half;
+#pragma unroll 1
+    for (int i = 0; i < IT; ++i) {
+      const uint32_t v = (tid + i * C::THREADS) * 4;
+      const uint4 a4 = *reinterpret_cast<const uint4*>(smem32 + Smem<uint32_t>::idx(v));
+      const uint4 b4 = *reinterpret_cast<const uint4*>(peer + Smem<uint32_t>::idx(v));
+      const uint32_t o[4] = {a4.x, a4.y, a4.z, a4.w}, q[4] = {b4.x, b4.y, b4.z, b4.w};
+      uint32_t res[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const uint32_t u = r == 0 ? o[k] : q[k], w = r == 0 ? q[k] : o[k];
+        res[k] = r == 0 ? mulmod_shoup(u + w, m.inv_n, m.inv_n_s, p)
+                        : mulmod_shoup(u - w + p2, m.inv_n_iphi, m.inv_n_iphi_s, p);
+      }
+      *reinterpret_cast<uint4*>(dst + v) = make_uint4(res[0], res[1], res[2], res[3]);
+    }
+    cluster.sync();
+  }
+}
+
 template <int OP>
 __global__ void k32_elementwise(uint32_t* dst, const uint32_t* a, const uint32_t* b, size_t total, uint32_t log_n,
                                 Limbs32 ls, const DevMod32* __restrict__ mods) {
@@ -339,6 +524,9 @@ __global__ void k32_elementwise(uint32_t* dst, const uint32_t* a, const uint32_t
 }
 
 // ---- launch ----------------------------------------------------------------------
+// Degrees whose polymul runs on a CTA pair.
+constexpr int kMinPairLogN = 14;
+
 template <int LOGN>
 cudaError_t set_attrs32() {
   using C = typename Cfg32<LOGN>::C;
@@ -347,6 +535,14 @@ cudaError_t set_attrs32() {
   for (auto k : {k32_ntt<C, 0>, k32_ntt<C, 1>, k32_ntt<C, 2>})
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k32_polymul<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if constexpr (LOGN >= kMinPairLogN) {
+    using PC = PairCfg32<LOGN>;
+    for (auto k : {k32_ntt_pair<typename PC::C, 0>, k32_ntt_pair<typename PC::C, 1>, k32_ntt_pair<typename PC::C, 2>})
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PC::kSmem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k32_polymul_pair<typename PC::C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)PC::kSmem);
+  }
   return e;
 }
 
@@ -356,6 +552,16 @@ cudaError_t launch32(int kind, uint32_t* c, const uint32_t* a, const uint32_t* b
   using CF = Cfg32<LOGN>;
   using C = typename CF::C;
   const uint32_t blocks = (ls.count + (1u << (C::T - LOGN)) - 1) >> (C::T - LOGN);
+  if constexpr (LOGN >= kMinPairLogN) {
+    using PC = PairCfg32<LOGN>;
+    using P = typename PC::C;
+    const uint32_t g = 2 * ls.count;
+    if (kind == 0) k32_ntt_pair<P, 0><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
+    else if (kind == 1) k32_ntt_pair<P, 1><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
+    else if (kind == 2) k32_ntt_pair<P, 2><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
+    else k32_polymul_pair<P><<<g, P::THREADS, PC::kSmem, st>>>(c, a, b, ls, mods);
+    return cudaGetLastError();
+  }
   if (kind == 0) k32_ntt<C, 0><<<blocks, C::THREADS, CF::kSmem, st>>>(c, ls, mods);
   else if (kind == 1) k32_ntt<C, 1><<<blocks, C::THREADS, CF::kSmem, st>>>(c, ls, mods);
   else if (kind == 2) k32_ntt<C, 2><<<blocks, C::THREADS, CF::kSmem, st>>>(c, ls, mods);
