@@ -255,6 +255,19 @@ int yell32_dev_polymul(uint32_t* d_c, const uint32_t* d_a, const uint32_t* d_b, 
                        uint32_t L, uint32_t log_n, uint32_t cm0, void* stream);
 int yell32_dev_elementwise(int op, uint32_t* d_dst, const uint32_t* d_a, const uint32_t* d_b,
                            uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0, void* stream);
+/* poly<N> members on host limbs (moduli 0 .. L-1), as yell_poly_* above */
+int yell32_poly_forward(uint32_t* const* limbs, uint32_t L, uint32_t log_n);
+int yell32_poly_forward_lazy(uint32_t* const* limbs, uint32_t L, uint32_t log_n);
+int yell32_poly_backward(uint32_t* const* limbs, uint32_t L, uint32_t log_n);
+int yell32_poly_mulmod(uint32_t* const* dst, const uint32_t* const* a, const uint32_t* const* b, uint32_t L,
+                       uint32_t log_n);
+int yell32_poly_addmod(uint32_t* const* dst, const uint32_t* const* a, const uint32_t* const* b, uint32_t L,
+                       uint32_t log_n);
+int yell32_poly_submod(uint32_t* const* dst, const uint32_t* const* a, const uint32_t* const* b, uint32_t L,
+                       uint32_t log_n);
+int yell32_poly_add_product_of(uint32_t* const* acc, const uint32_t* const* a, const uint32_t* const* b,
+                               uint32_t L, uint32_t log_n);
+int yell32_poly_negate(uint32_t* const* limbs, uint32_t L, uint32_t log_n);
 
 /* ---- device-resident poly handles (the device-side poly<N>) -------------
  * A handle owns one poly in HBM: L limbs of N words, limb l under prime

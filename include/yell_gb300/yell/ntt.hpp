@@ -31,6 +31,23 @@ struct static_log2<1> {
   static constexpr uint32_t value = 0;
 };
 
+namespace detail {
+// The C ABI entry points of the word size the build selected.
+#ifdef YELL_USE_32BITS_MODULI
+inline int ntt_init_table(uint32_t log_n, uint32_t cm) { return yell32_init_ntt_tables(log_n, cm, 1); }
+inline int ntt_init_tables(uint32_t log_n, uint32_t K) { return yell32_init_ntt_tables(log_n, 0, K); }
+inline int ntt_forward(uint32_t* op, uint32_t log_n, uint32_t cm) { return yell32_ntt_forward(op, log_n, cm); }
+inline int ntt_forward_lazy(uint32_t* op, uint32_t log_n, uint32_t cm) { return yell32_ntt_forward_lazy(op, log_n, cm); }
+inline int ntt_backward(uint32_t* op, uint32_t log_n, uint32_t cm) { return yell32_ntt_backward(op, log_n, cm); }
+#else
+inline int ntt_init_table(uint32_t log_n, uint32_t cm) { return yell_init_table(log_n, cm); }
+inline int ntt_init_tables(uint32_t log_n, uint32_t K) { return yell_init_ntt_tables(log_n, K); }
+inline int ntt_forward(uint64_t* op, uint32_t log_n, uint32_t cm) { return yell_ntt_forward(op, log_n, cm); }
+inline int ntt_forward_lazy(uint64_t* op, uint32_t log_n, uint32_t cm) { return yell_ntt_forward_lazy(op, log_n, cm); }
+inline int ntt_backward(uint64_t* op, uint32_t log_n, uint32_t cm) { return yell_ntt_backward(op, log_n, cm); }
+#endif
+}  // namespace detail
+
 template <size_t degree_>
 class ntt {
   using T = params::value_type;
@@ -39,19 +56,19 @@ class ntt {
  public:
   static constexpr size_t degree = degree_;
   // ntt.hpp:50: builds the table of modulus cm (on the GPU, kept for the process).
-  static void init_table(size_t cm) { check_status(yell_init_table(log_n, (uint32_t)cm), "init_table"); }
+  static void init_table(size_t cm) { check_status(detail::ntt_init_table(log_n, (uint32_t)cm), "init_table"); }
   // ntt.hpp:53-56
   static void init_ntt_tables(size_t K) {
-    check_status(yell_init_ntt_tables(log_n, (uint32_t)K), "init_ntt_tables");
+    check_status(detail::ntt_init_tables(log_n, (uint32_t)K), "init_ntt_tables");
   }
   // ntt.hpp:59: in place, bit-reversed output in [0, p).
-  static void forward(T* op, size_t cm) { check_status(yell_ntt_forward(op, log_n, (uint32_t)cm), "forward"); }
+  static void forward(T* op, size_t cm) { check_status(detail::ntt_forward(op, log_n, (uint32_t)cm), "forward"); }
   // ntt.hpp:62: in place, output in [0, 4p).
   static void forward_lazy(T* op, size_t cm) {
-    check_status(yell_ntt_forward_lazy(op, log_n, (uint32_t)cm), "forward_lazy");
+    check_status(detail::ntt_forward_lazy(op, log_n, (uint32_t)cm), "forward_lazy");
   }
   // ntt.hpp:65: in place, natural-order output in [0, p).
-  static void backward(T* op, size_t cm) { check_status(yell_ntt_backward(op, log_n, (uint32_t)cm), "backward"); }
+  static void backward(T* op, size_t cm) { check_status(detail::ntt_backward(op, log_n, (uint32_t)cm), "backward"); }
 };
 
 }  // namespace yell

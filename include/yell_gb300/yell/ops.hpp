@@ -16,21 +16,25 @@ static inline void mod_correct(T& a, const T p) {
   a -= (a >= p) ? p : T(0);
 }
 
+constexpr unsigned kWordBits = params::kModulusRepresentationBitsize;
+constexpr unsigned kDelta = params::kModulusRepresentationBitsize - params::kModulusBitsize;
+
 // lib/ops.cpp:5-21
 inline void barret_reduction(params::gt_value_type* x, size_t cm) {
   if (!x) return;
+  using T = params::value_type;
   using gT = params::gt_value_type;
   const gT xv = *x;
-  const gT q = (gT)params::Pn[cm] * (uint64_t)(xv >> 64) + (xv << 2);
-  const uint64_t p = params::P[cm];
-  uint64_t r = (uint64_t)xv - (uint64_t)(q >> 64) * p;
+  const gT q = (gT)params::Pn[cm] * (T)(xv >> kWordBits) + (xv << kDelta);
+  const T p = params::P[cm];
+  T r = (T)xv - (T)(q >> kWordBits) * p;
   mod_correct(r, p);
   *x = r;
 }
 
 // lib/ops.cpp:23-27
 inline params::value_type shoupify(params::value_type x, size_t cm) {
-  return (params::value_type)(((params::gt_value_type)x << 64) / params::P[cm]);
+  return (params::value_type)(((params::gt_value_type)x << kWordBits) / params::P[cm]);
 }
 
 struct addmod {
@@ -64,7 +68,7 @@ struct mulmod_shoup {
   T operator()(T x, T y, T yprime, size_t cm) const { compute(x, y, yprime, cm); return x; }
   void compute(T& x, T y, T yprime, size_t cm) const {
     const T p = params::P[cm];
-    const T q = (T)(((params::gt_value_type)x * yprime) >> 64) * p;
+    const T q = (T)(((params::gt_value_type)x * yprime) >> kWordBits) * p;
     x = x * y - q;
     mod_correct(x, p);
   }

@@ -51,6 +51,46 @@ inline std::atomic<uint64_t>& sampler_seed() {
 
 inline void set_sampler_seed(uint64_t seed) { detail::sampler_seed().store(seed); }
 
+namespace detail {
+// poly<N> entry points of the word size the build selected.
+using W = params::value_type;
+#ifdef YELL_USE_32BITS_MODULI
+inline int poly_forward(W* const* l, uint32_t L, uint32_t n) { return yell32_poly_forward(l, L, n); }
+inline int poly_forward_lazy(W* const* l, uint32_t L, uint32_t n) { return yell32_poly_forward_lazy(l, L, n); }
+inline int poly_backward(W* const* l, uint32_t L, uint32_t n) { return yell32_poly_backward(l, L, n); }
+inline int poly_negate(W* const* l, uint32_t L, uint32_t n) { return yell32_poly_negate(l, L, n); }
+inline int poly_mulmod(W* const* d, const W* const* a, const W* const* b, uint32_t L, uint32_t n) {
+  return yell32_poly_mulmod(d, a, b, L, n);
+}
+inline int poly_addmod(W* const* d, const W* const* a, const W* const* b, uint32_t L, uint32_t n) {
+  return yell32_poly_addmod(d, a, b, L, n);
+}
+inline int poly_submod(W* const* d, const W* const* a, const W* const* b, uint32_t L, uint32_t n) {
+  return yell32_poly_submod(d, a, b, L, n);
+}
+inline int poly_add_product_of(W* const* d, const W* const* a, const W* const* b, uint32_t L, uint32_t n) {
+  return yell32_poly_add_product_of(d, a, b, L, n);
+}
+#else
+inline int poly_forward(W* const* l, uint32_t L, uint32_t n) { return yell_poly_forward(l, L, n); }
+inline int poly_forward_lazy(W* const* l, uint32_t L, uint32_t n) { return yell_poly_forward_lazy(l, L, n); }
+inline int poly_backward(W* const* l, uint32_t L, uint32_t n) { return yell_poly_backward(l, L, n); }
+inline int poly_negate(W* const* l, uint32_t L, uint32_t n) { return yell_poly_negate(l, L, n); }
+inline int poly_mulmod(W* const* d, const W* const* a, const W* const* b, uint32_t L, uint32_t n) {
+  return yell_poly_mulmod(d, a, b, L, n);
+}
+inline int poly_addmod(W* const* d, const W* const* a, const W* const* b, uint32_t L, uint32_t n) {
+  return yell_poly_addmod(d, a, b, L, n);
+}
+inline int poly_submod(W* const* d, const W* const* a, const W* const* b, uint32_t L, uint32_t n) {
+  return yell_poly_submod(d, a, b, L, n);
+}
+inline int poly_add_product_of(W* const* d, const W* const* a, const W* const* b, uint32_t L, uint32_t n) {
+  return yell_poly_add_product_of(d, a, b, L, n);
+}
+#endif
+}  // namespace detail
+
 template <size_t degree_>
 class poly {
   static_assert(degree_ < params::kMaxPolyDegree, "");
@@ -80,6 +120,8 @@ class poly {
     assert(nmoduli <= params::kMaxNbModuli);
     for (size_t cm = 0; cm < nmoduli; ++cm) _data.push_back(alloc_limb());
   }
+#ifndef YELL_USE_32BITS_MODULI
+  // the device samplers fill 64-bit words; the 32-bit mode has none
   poly(size_t nmoduli_, uniform const& mode) : poly(nmoduli_) { set(mode); }
   poly(size_t nmoduli_, hwt_dist const& mode) : poly(nmoduli_) { set(mode); }
   poly(size_t nmoduli_, ZO_dist const& mode) : poly(nmoduli_) { set(mode); }
@@ -107,6 +149,7 @@ class poly {
                                       seed, nullptr);
     });
   }
+#endif
   ~poly() {
     for (auto& p : _data) std::free(p);
   }
@@ -136,13 +179,13 @@ class poly {
   // details/poly.hpp:118-132: *this += op0 * op1 (ops::muladd per word).
   poly& add_product_of(const poly& op0, const poly& op1) {
     assert(nmoduli == op0.nmoduli && nmoduli == op1.nmoduli);
-    check_status(yell_poly_add_product_of(_data.data(), op0._data.data(), op1._data.data(),
+    check_status(detail::poly_add_product_of(_data.data(), op0._data.data(), op1._data.data(),
                                           (uint32_t)nmoduli, log_n),
                  "add_product_of");
     return *this;
   }
   // details/poly.hpp:151-157
-  void negate() { check_status(yell_poly_negate(_data.data(), (uint32_t)nmoduli, log_n), "negate"); }
+  void negate() { check_status(detail::poly_negate(_data.data(), (uint32_t)nmoduli, log_n), "negate"); }
 
   // details/poly.hpp:90-109
   void resize_moduli_count(size_t new_nmoduli) {
@@ -158,6 +201,7 @@ class poly {
   value_type const& operator()(size_t cm, size_t i) const { return _data[cm][i]; }
   value_type& operator()(size_t cm, size_t i) { return _data[cm][i]; }
 
+#ifndef YELL_USE_32BITS_MODULI
  private:
   template <class F>
   void sample(F&& fill) {
@@ -173,13 +217,14 @@ class poly {
   }
 
  public:
+#endif
 
   // details/poly.hpp:170-186, one GPU call over all limbs each.
-  void forward() { check_status(yell_poly_forward(_data.data(), (uint32_t)nmoduli, log_n), "forward"); }
+  void forward() { check_status(detail::poly_forward(_data.data(), (uint32_t)nmoduli, log_n), "forward"); }
   void forward_lazy() {
-    check_status(yell_poly_forward_lazy(_data.data(), (uint32_t)nmoduli, log_n), "forward_lazy");
+    check_status(detail::poly_forward_lazy(_data.data(), (uint32_t)nmoduli, log_n), "forward_lazy");
   }
-  void backward() { check_status(yell_poly_backward(_data.data(), (uint32_t)nmoduli, log_n), "backward"); }
+  void backward() { check_status(detail::poly_backward(_data.data(), (uint32_t)nmoduli, log_n), "backward"); }
 
   value_type get_modulus(size_t cm) { return params::P[cm]; }
   params::value_type** raw_data() { return _data.data(); }
@@ -195,16 +240,14 @@ class poly {
 };
 
 namespace detail {
-template <size_t N, int (*FN)(uint64_t* const*, const uint64_t* const*, const uint64_t* const*, uint32_t,
-                              uint32_t)>
+template <size_t N, int (*FN)(W* const*, const W* const*, const W* const*, uint32_t, uint32_t)>
 poly<N> binary_op(poly<N> const& a, poly<N> const& b, const char* name) {
   const size_t L = a.moduli_count() < b.moduli_count() ? a.moduli_count() : b.moduli_count();
   poly<N> r(L);
   check_status(FN(r.raw_data(), a.raw_data(), b.raw_data(), (uint32_t)L, poly<N>::logn), name);
   return r;
 }
-template <size_t N, int (*FN)(uint64_t* const*, const uint64_t* const*, const uint64_t* const*, uint32_t,
-                              uint32_t)>
+template <size_t N, int (*FN)(W* const*, const W* const*, const W* const*, uint32_t, uint32_t)>
 poly<N>& self_op(poly<N>& a, poly<N> const& b, const char* name) {
   const size_t L = a.moduli_count() < b.moduli_count() ? a.moduli_count() : b.moduli_count();
   check_status(FN(a.raw_data(), a.raw_data(), b.raw_data(), (uint32_t)L, poly<N>::logn), name);
@@ -213,11 +256,11 @@ poly<N>& self_op(poly<N>& a, poly<N> const& b, const char* name) {
 }  // namespace detail
 
 // include/yell/poly.hpp:163-168 (the YELL_BINARY_OPERATOR loops of ops.hpp:7-41).
-template <size_t N> poly<N> operator*(poly<N> const& a, poly<N> const& b) { return detail::binary_op<N, yell_poly_mulmod>(a, b, "operator*"); }
-template <size_t N> poly<N> operator+(poly<N> const& a, poly<N> const& b) { return detail::binary_op<N, yell_poly_addmod>(a, b, "operator+"); }
-template <size_t N> poly<N> operator-(poly<N> const& a, poly<N> const& b) { return detail::binary_op<N, yell_poly_submod>(a, b, "operator-"); }
-template <size_t N> poly<N>& operator*=(poly<N>& a, poly<N> const& b) { return detail::self_op<N, yell_poly_mulmod>(a, b, "operator*="); }
-template <size_t N> poly<N>& operator+=(poly<N>& a, poly<N> const& b) { return detail::self_op<N, yell_poly_addmod>(a, b, "operator+="); }
-template <size_t N> poly<N>& operator-=(poly<N>& a, poly<N> const& b) { return detail::self_op<N, yell_poly_submod>(a, b, "operator-="); }
+template <size_t N> poly<N> operator*(poly<N> const& a, poly<N> const& b) { return detail::binary_op<N, detail::poly_mulmod>(a, b, "operator*"); }
+template <size_t N> poly<N> operator+(poly<N> const& a, poly<N> const& b) { return detail::binary_op<N, detail::poly_addmod>(a, b, "operator+"); }
+template <size_t N> poly<N> operator-(poly<N> const& a, poly<N> const& b) { return detail::binary_op<N, detail::poly_submod>(a, b, "operator-"); }
+template <size_t N> poly<N>& operator*=(poly<N>& a, poly<N> const& b) { return detail::self_op<N, detail::poly_mulmod>(a, b, "operator*="); }
+template <size_t N> poly<N>& operator+=(poly<N>& a, poly<N> const& b) { return detail::self_op<N, detail::poly_addmod>(a, b, "operator+="); }
+template <size_t N> poly<N>& operator-=(poly<N>& a, poly<N> const& b) { return detail::self_op<N, detail::poly_submod>(a, b, "operator-="); }
 
 }  // namespace yell

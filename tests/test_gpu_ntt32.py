@@ -139,3 +139,38 @@ def test_errors(cuda):
         m32.dev_polymul(t, t, t, 1, 1, 10)
     with pytest.raises(YellError):
         m32.dev_ntt(t[1:], 1, 1, 10, 0)  # misaligned
+
+
+def test_host_poly_dropins(cuda, o32):
+    """yell32_poly_* (poly<N> members on host limbs, moduli 0 .. L-1)."""
+    import ctypes
+
+    from yell_gb300._capi import call
+
+    L, log_n = 3, 11
+    n = 1 << log_n
+    a = [np.ascontiguousarray(x) for x in _polys(31, 1, L, log_n, 0)[0]]
+    b = [np.ascontiguousarray(x) for x in _polys(32, 1, L, log_n, 0)[0]]
+
+    def arr(ls):
+        return (ctypes.c_void_p * len(ls))(*[x.ctypes.data for x in ls])
+
+    f = [x.copy() for x in a]
+    call("yell32_poly_forward", arr(f), L, log_n)
+    for l in range(L):
+        assert np.array_equal(f[l], o32.forward(a[l], log_n, l))
+    d = [np.zeros(n, np.uint32) for _ in range(L)]
+    call("yell32_poly_mulmod", arr(d), arr(f), arr(b), L, log_n)
+    for l in range(L):
+        assert np.array_equal(d[l], o32.mulmod(f[l], b[l], l))
+    acc = [x.copy() for x in b]
+    call("yell32_poly_add_product_of", arr(acc), arr(f), arr(a), L, log_n)
+    for l in range(L):
+        assert np.array_equal(acc[l], o32.muladd(b[l], f[l], a[l], l))
+    call("yell32_poly_backward", arr(f), L, log_n)
+    for l in range(L):
+        assert np.array_equal(f[l], a[l])
+    g = [x.copy() for x in a]
+    call("yell32_poly_negate", arr(g), L, log_n)
+    for l in range(L):
+        assert np.array_equal(g[l], o32.negate(a[l], l))

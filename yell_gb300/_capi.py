@@ -102,6 +102,14 @@ SIGNATURES = {
     "yell32_dev_ntt": (_int, [_vp, _u32, _u32, _u32, _u32, _int, _vp]),
     "yell32_dev_polymul": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),
     "yell32_dev_elementwise": (_int, [_int, _vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),
+    "yell32_poly_forward": (_int, [_vp, _u32, _u32]),
+    "yell32_poly_forward_lazy": (_int, [_vp, _u32, _u32]),
+    "yell32_poly_backward": (_int, [_vp, _u32, _u32]),
+    "yell32_poly_mulmod": (_int, [_vp, _vp, _vp, _u32, _u32]),
+    "yell32_poly_addmod": (_int, [_vp, _vp, _vp, _u32, _u32]),
+    "yell32_poly_submod": (_int, [_vp, _vp, _vp, _u32, _u32]),
+    "yell32_poly_add_product_of": (_int, [_vp, _vp, _vp, _u32, _u32]),
+    "yell32_poly_negate": (_int, [_vp, _u32, _u32]),
     "yell_dev_poly_alloc": (_int, [_u32, _u32, _u32, _vp]),
     "yell_dev_poly_free": (_int, [_vp]),
     "yell_dev_poly_info": (_int, [_vp, _vp, _vp, _vp, _vp]),

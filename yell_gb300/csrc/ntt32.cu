@@ -724,4 +724,75 @@ int yell32_dev_elementwise(int op, uint32_t* d_dst, const uint32_t* d_a, const u
   return e == cudaSuccess ? kOk : fail_cuda(e, "elementwise32");
 }
 
+// ---- host-memory poly<N> drop-ins (limb pointer arrays, moduli 0 .. L-1) ----
+// The reference's poly<N> members in 32-bit mode (details/poly.hpp:118-186 and
+// the operators of poly.hpp:163-168): limbs staged through device memory,
+// one launch over all limbs, copied back; synchronous.
+
+static int host_poly32(int kind, int op, uint32_t* const* dst, const uint32_t* const* a, const uint32_t* const* b,
+                       uint32_t L, uint32_t log_n) {
+  // kind 0..2: NTT of dst in place; kind 3: element-wise op
+  if (!dst || L == 0) return fail(kInvalidArgument, "null limb array or zero limbs");
+  const bool binary = kind == 3 && op != YELL_OP_NEGATE;
+  if (kind == 3 && (!a || (binary && !b))) return fail(kInvalidArgument, "null limb array");
+  for (uint32_t l = 0; l < L; ++l)
+    if (!dst[l] || (kind == 3 && !a[l]) || (binary && !b[l])) return fail(kInvalidArgument, "null limb pointer");
+  DeviceContext* ctx;
+  const DevMod32* mods;
+  int st = prepare32(log_n, 0, L, &ctx, &mods);
+  if (st != kOk) return st;
+  const size_t n = (size_t)1 << log_n, w = n * L;
+  std::lock_guard<std::mutex> g(ctx->staging.lock);
+  st = ctx->staging.reserve((3 * w + 1) / 2);  // three uint32 operands in uint64 words
+  if (st != kOk) return st;
+  uint32_t* dd = reinterpret_cast<uint32_t*>(ctx->staging.ptr);
+  uint32_t* da = dd + w;
+  uint32_t* db = da + w;
+  cudaStream_t s = ctx->stream();
+  cudaError_t e = cudaSuccess;
+  const bool need_dst = kind != 3 || op == YELL_OP_MULADD;
+  for (uint32_t l = 0; l < L && e == cudaSuccess; ++l) {
+    if (need_dst) e = cudaMemcpyAsync(dd + l * n, dst[l], n * 4, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && kind == 3) e = cudaMemcpyAsync(da + l * n, a[l], n * 4, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && binary) e = cudaMemcpyAsync(db + l * n, b[l], n * 4, cudaMemcpyHostToDevice, s);
+  }
+  if (e != cudaSuccess) return fail_cuda(e, "H2D limbs");
+  st = kind == 3 ? yell32_dev_elementwise(op, dd, da, binary ? db : nullptr, 1, L, log_n, 0, s)
+                 : run32(kind, dd, nullptr, nullptr, 1, L, log_n, 0, s);
+  if (st != kOk) return st;
+  for (uint32_t l = 0; l < L && e == cudaSuccess; ++l)
+    e = cudaMemcpyAsync(dst[l], dd + l * n, n * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? kOk : fail_cuda(e, "D2H limbs");
+}
+
+int yell32_poly_forward(uint32_t* const* limbs, uint32_t L, uint32_t log_n) {
+  return host_poly32(0, 0, limbs, nullptr, nullptr, L, log_n);
+}
+int yell32_poly_forward_lazy(uint32_t* const* limbs, uint32_t L, uint32_t log_n) {
+  return host_poly32(1, 0, limbs, nullptr, nullptr, L, log_n);
+}
+int yell32_poly_backward(uint32_t* const* limbs, uint32_t L, uint32_t log_n) {
+  return host_poly32(2, 0, limbs, nullptr, nullptr, L, log_n);
+}
+int yell32_poly_mulmod(uint32_t* const* dst, const uint32_t* const* a, const uint32_t* const* b, uint32_t L,
+                       uint32_t log_n) {
+  return host_poly32(3, YELL_OP_MULMOD, dst, a, b, L, log_n);
+}
+int yell32_poly_addmod(uint32_t* const* dst, const uint32_t* const* a, const uint32_t* const* b, uint32_t L,
+                       uint32_t log_n) {
+  return host_poly32(3, YELL_OP_ADDMOD, dst, a, b, L, log_n);
+}
+int yell32_poly_submod(uint32_t* const* dst, const uint32_t* const* a, const uint32_t* const* b, uint32_t L,
+                       uint32_t log_n) {
+  return host_poly32(3, YELL_OP_SUBMOD, dst, a, b, L, log_n);
+}
+int yell32_poly_add_product_of(uint32_t* const* acc, const uint32_t* const* a, const uint32_t* const* b, uint32_t L,
+                               uint32_t log_n) {
+  return host_poly32(3, YELL_OP_MULADD, acc, a, b, L, log_n);
+}
+int yell32_poly_negate(uint32_t* const* limbs, uint32_t L, uint32_t log_n) {
+  return host_poly32(3, YELL_OP_NEGATE, limbs, limbs, nullptr, L, log_n);
+}
+
 }  // extern "C"
