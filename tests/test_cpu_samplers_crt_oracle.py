@@ -117,7 +117,8 @@ def test_hwt_positions_uniform(orc):
     e = cnt * h / n
     chi2 = float(((counts - e) ** 2 / e).sum())
     assert chi2 < 2.0 * (n - 1)  # dof 63: mean 63, sd ~11
-    co = (nz[:, :, None].astype(np.float32) * nz[:, None, :]).sum(0)
+    z = nz.astype(np.float64)
+    co = z.T @ z
     exp = cnt * h * (h - 1) / (n * (n - 1))
     off = co[~np.eye(n, dtype=bool)]
     assert abs(off.mean() / exp - 1) < 0.02
