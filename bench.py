@@ -552,7 +552,8 @@ def run_rows(torch, y, stream, dc, reps: int = 5):
 
 def run_uneven(torch, y, stream, barrier, max_over_ranks, world, no_autotune=False):
     """512 polymuls of mixed degree and limb count (seed 4): one batched call
-    (bucketed, CUDA graph per batch shape) against 512 plain per-call calls."""
+    (bucketed, CUDA graph per batch shape), one launch of the persistent
+    work-queue kernel, and 512 plain per-call calls."""
     from yell_gb300.workloads import mix_limb_ntts, mix_operands, uneven_mix
 
     mix = uneven_mix(4, 512)
@@ -576,13 +577,16 @@ def run_uneven(torch, y, stream, barrier, max_over_ranks, world, no_autotune=Fal
     def batched():
         y.dev_polymul_batch(items, stream=stream)
 
+    def queue():
+        y.dev_polymul_batch_queue(items, stream=stream)
+
     def per_call():
         for (dc, da, db, log_n, L, cm0), sc in zip(items, singles):
             y.dev_polymul(dc, da, db, 1, L, log_n, cm0, scratch=sc, stream=stream)
 
     out = {"workload": "512 polymuls, log2 N uniform in 10..16, L uniform in 1..16 (seed 4)",
            "limb_ntts": limb_ntts}
-    for name, fn, steps in (("batched", batched, 10), ("per_call", per_call, 3)):
+    for name, fn, steps in (("batched", batched, 10), ("persistent_queue", queue, 10), ("per_call", per_call, 3)):
         for _ in range(2):
             fn()
         barrier()
@@ -593,7 +597,11 @@ def run_uneven(torch, y, stream, barrier, max_over_ranks, world, no_autotune=Fal
         torch.cuda.synchronize()
         ms = max_over_ranks(e0.elapsed_time(e1)) / steps
         out[name] = {"value": world * limb_ntts / (ms * 1e-3), "unit": UNIT, "ms_per_batch": ms}
+    out["batched"]["path"] = "degree buckets on forked streams, one CUDA graph per batch shape"
+    out["persistent_queue"]["path"] = "one launch: resident CTAs take work items from a device queue"
+    out["persistent_queue"]["status"] = y.batch_queue_status()
     out["batched_vs_per_call"] = out["batched"]["value"] / out["per_call"]["value"]
+    out["queue_vs_per_call"] = out["persistent_queue"]["value"] / out["per_call"]["value"]
     out["_items"] = items
     out["_mix"] = mix
     return out

@@ -173,6 +173,19 @@ typedef struct yell_polymul_desc {
   uint32_t reserved;
 } yell_polymul_desc;
 int yell_dev_polymul_batch(const yell_polymul_desc* descs, uint32_t n, void* stream);
+/* The same batch as ONE launch of a persistent kernel driven by a device
+ * work queue: resident CTAs take work items (whole-limb tiles; for
+ * N >= 2^13 the column pass, row step and inverse column pass of each tile)
+ * in queue order from a device ticket counter; a step waits for the steps of
+ * its limb it depends on.  Each wait is bounded (2 s); one that runs out
+ * records YELL_ERR_TIMEOUT, read (and cleared) by yell_batch_queue_status,
+ * which waits for the queued work.  Asynchronous on `stream`. */
+int yell_dev_polymul_batch_queue(const yell_polymul_desc* descs, uint32_t n, void* stream);
+int yell_batch_queue_status(uint32_t* status);
+/* Check of the bounded wait: a queue whose row steps wait on column passes
+ * that are never queued; every wait runs out after timeout_ns (<= 10 s) and
+ * *status receives YELL_ERR_TIMEOUT.  Synchronous. */
+int yell_batch_queue_wait_check(uint64_t timeout_ns, uint32_t* status);
 
 /* ---- serving loop (no counterpart in the reference) ------------------------
  * Continuous batching of polymul requests of mixed size.  A scheduler thread

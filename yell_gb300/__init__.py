@@ -26,7 +26,7 @@ __all__ = [
     "dev_ntt_limbs", "dev_elementwise", "dev_polymul", "polymul_scratch_words", "kernel_launches",
     "Poly", "PinnedBuffer", "sample_uniform", "sample_zo", "sample_hwt", "sample_gaussian",
     "crt_words", "dev_crt_lift", "poly_to_bigint", "words_to_ints", "DevPoly", "BatchTicket",
-    "batch_submit",
+    "batch_submit", "dev_polymul_batch_queue", "batch_queue_status", "batch_queue_wait_check",
 ]
 
 
@@ -248,6 +248,28 @@ def dev_polymul_batch(items, stream=None) -> None:
     for i, (c, a, b, log_n, L, cm0) in enumerate(items):
         descs[i] = _capi.PolymulDesc(_dptr(c), _dptr(a), _dptr(b), log_n, L, cm0, 0)
     call("yell_dev_polymul_batch", ctypes.addressof(descs), len(items), _stream(stream))
+
+
+def dev_polymul_batch_queue(items, stream=None) -> None:
+    """The uneven batch as one launch of the persistent work-queue kernel."""
+    descs = (_capi.PolymulDesc * len(items))()
+    for i, (c, a, b, log_n, L, cm0) in enumerate(items):
+        descs[i] = _capi.PolymulDesc(_dptr(c), _dptr(a), _dptr(b), log_n, L, cm0, 0)
+    call("yell_dev_polymul_batch_queue", ctypes.addressof(descs), len(items), _stream(stream))
+
+
+def batch_queue_status() -> int:
+    """Waits for queued work; returns (and clears) the queue kernel's status word."""
+    st = ctypes.c_uint32()
+    call("yell_batch_queue_status", ctypes.byref(st))
+    return int(st.value)
+
+
+def batch_queue_wait_check(timeout_s: float) -> int:
+    """Runs a queue whose waits cannot be satisfied; returns the recorded status."""
+    st = ctypes.c_uint32()
+    call("yell_batch_queue_wait_check", int(timeout_s * 1e9), ctypes.byref(st))
+    return int(st.value)
 
 
 def sample_uniform(t, count: int, L: int, log_n: int, cm0: int = 0, seed: int = 0, stream=None):

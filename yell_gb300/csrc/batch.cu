@@ -11,6 +11,9 @@
 #include "batch.h"
 
 #include <algorithm>
+#include <array>
+
+#include "batch_queue.h"
 #include <cstring>
 #include <memory>
 
@@ -36,6 +39,7 @@ BatchExecutor::~BatchExecutor() {
   if (d_lists_) cudaFree(d_lists_);
   if (h_lists_) cudaFreeHost(h_lists_);
   if (d_scratch_) cudaFree(d_scratch_);
+  if (d_queue_ctl_) cudaFree(d_queue_ctl_);
   for (int i = 0; i < kDegrees; ++i) {
     if (side_[i]) cudaStreamDestroy(side_[i]);
     if (join_[i]) cudaEventDestroy(join_[i]);
@@ -214,11 +218,228 @@ int BatchExecutor::run(DeviceContext* ctx, const yell_polymul_desc* descs, uint6
   return kOk;
 }
 
+int BatchExecutor::reserve_queue_ctl(size_t words) {
+  if (words <= queue_ctl_words_) return kOk;
+  // keep the sticky status word across the regrowth
+  uint32_t status = 0;
+  if (d_queue_ctl_) {
+    cudaError_t e = cudaMemcpy(&status, d_queue_ctl_, 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail_cuda(e, "queue status");
+    cudaFree(d_queue_ctl_);
+    d_queue_ctl_ = nullptr;
+    queue_ctl_words_ = 0;
+  }
+  const size_t want = std::max<size_t>(words, 4096) * 2;
+  cudaError_t e = cudaMalloc(&d_queue_ctl_, want * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemset(d_queue_ctl_, 0, want * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemcpy(d_queue_ctl_, &status, 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return fail_cuda(e, "cudaMalloc(queue control)");
+  queue_ctl_words_ = want;
+  return kOk;
+}
+
+int BatchExecutor::run_queue(DeviceContext* ctx, const yell_polymul_desc* descs, uint32_t n, cudaStream_t s,
+                             uint64_t timeout_ns) {
+  if (!queue_attrs_) {
+    const cudaError_t e = queue_set_attributes();
+    if (e != cudaSuccess) return fail_cuda(e, "queue kernel attributes");
+    queue_attrs_ = true;
+  }
+  // ---- buckets: limb lists, scratch for the two-pass degrees -------------
+  std::array<std::vector<uint32_t>, kDegrees> members;
+  for (uint32_t i = 0; i < n; ++i) members[descs[i].log_n - kMinLogN].push_back(i);
+  std::vector<Bucket> buckets;
+  std::vector<uint32_t> counter_off;
+  size_t bytes = 0, scratch = 0, counters = 0;
+  for (int k = 0; k < kDegrees; ++k) {
+    if (members[k].empty()) continue;
+    Bucket b;
+    b.log_n = kMinLogN + k;
+    for (uint32_t i : members[k]) b.limbs += descs[i].L;
+    b.mods = ctx->mods_if_ready(b.log_n);
+    if (!b.mods) return fail(kInvalidArgument, "batch: twiddle tables not built");
+    b.c_off = bytes;
+    bytes += 8 * (size_t)b.limbs;
+    b.a_off = bytes;
+    bytes += 8 * (size_t)b.limbs;
+    b.b_off = bytes;
+    bytes += 8 * (size_t)b.limbs;
+    b.s_off = bytes;
+    bytes += 8 * (size_t)b.limbs;
+    b.cm_off = bytes;
+    bytes += ((4 * (size_t)b.limbs + 15) / 16) * 16;
+    b.scratch_off = scratch;
+    counter_off.push_back((uint32_t)counters);
+    if (b.log_n >= kQueueFirstTwoPass) {
+      scratch += (size_t)b.limbs << b.log_n;
+      counters += 2 * (size_t)b.limbs;
+    }
+    buckets.push_back(b);
+  }
+  if (buckets.size() > (1u << 24)) return fail(kInvalidArgument, "batch: too many buckets");
+  // ---- queue: forward column passes, whole-limb tiles, row steps, inverse column passes
+  std::vector<QueueItem> items;
+  for (int phase = 0; phase < 4; ++phase)
+    for (size_t bi = 0; bi < buckets.size(); ++bi) {
+      const Bucket& b = buckets[bi];
+      const bool two_pass = b.log_n >= kQueueFirstTwoPass;
+      if (two_pass == (phase == 1)) continue;  // phase 1 holds the whole-limb tiles only
+      uint32_t kind, tiles;
+      if (two_pass) {
+        kind = phase == 0 ? kItemColFwd : (phase == 2 ? kItemRows : kItemColInv);
+        tiles = b.limbs << (b.log_n - kQueueTileLog);
+      } else {
+        kind = kItemWhole;
+        const uint32_t t = b.log_n >= 4 ? kQueueTileLog : kQueueTileLog - 1;
+        const uint32_t per = 1u << (t - b.log_n);
+        tiles = (b.limbs + per - 1) / per;
+      }
+      for (uint32_t t = 0; t < tiles; ++t) items.push_back(QueueItem{(uint32_t)bi << 8 | kind, t});
+    }
+  const size_t buckets_off = (bytes + 15) / 16 * 16;
+  bytes = buckets_off + buckets.size() * sizeof(QueueBucket);
+  const size_t items_off = (bytes + 15) / 16 * 16;
+  bytes = items_off + items.size() * sizeof(QueueItem);
+  int st = reserve_lists(bytes);
+  if (st == kOk) st = reserve_scratch(std::max<size_t>(scratch, 2));
+  if (st == kOk) st = reserve_queue_ctl(2 + std::max<size_t>(counters, 1));
+  if (st != kOk) return st;
+
+  // ---- host staging after the previous upload has drained -------------------
+  cudaError_t e = cudaEventSynchronize(staged_);
+  if (e != cudaSuccess) return fail_cuda(e, "batch staging wait");
+  QueueBucket* qb = reinterpret_cast<QueueBucket*>(h_lists_ + buckets_off);
+  for (size_t bi = 0; bi < buckets.size(); ++bi) {
+    const Bucket& b = buckets[bi];
+    uint64_t* c = reinterpret_cast<uint64_t*>(h_lists_ + b.c_off);
+    uint64_t* a = reinterpret_cast<uint64_t*>(h_lists_ + b.a_off);
+    uint64_t* bb = reinterpret_cast<uint64_t*>(h_lists_ + b.b_off);
+    uint64_t* sc = reinterpret_cast<uint64_t*>(h_lists_ + b.s_off);
+    uint32_t* cm = reinterpret_cast<uint32_t*>(h_lists_ + b.cm_off);
+    const size_t nw = (size_t)1 << b.log_n;
+    size_t k = 0;
+    for (uint32_t i : members[b.log_n - kMinLogN]) {
+      const yell_polymul_desc& d = descs[i];
+      for (uint32_t l = 0; l < d.L; ++l, ++k) {
+        c[k] = reinterpret_cast<uint64_t>(d.c + l * nw);
+        a[k] = reinterpret_cast<uint64_t>(d.a + l * nw);
+        bb[k] = reinterpret_cast<uint64_t>(d.b + l * nw);
+        sc[k] = reinterpret_cast<uint64_t>(d_scratch_ + b.scratch_off + k * nw);
+        cm[k] = d.cm0 + l;
+      }
+    }
+    QueueBucket q;
+    const uint32_t* cms = reinterpret_cast<const uint32_t*>(d_lists_ + b.cm_off);
+    q.c = LimbSet{nullptr, reinterpret_cast<uint64_t* const*>(d_lists_ + b.c_off), cms, b.limbs, 1, 0, 0};
+    q.a = ConstLimbSet{nullptr, reinterpret_cast<const uint64_t* const*>(d_lists_ + b.a_off), cms, b.limbs, 1, 0, 0};
+    q.b = ConstLimbSet{nullptr, reinterpret_cast<const uint64_t* const*>(d_lists_ + b.b_off), cms, b.limbs, 1, 0, 0};
+    q.s = LimbSet{nullptr, reinterpret_cast<uint64_t* const*>(d_lists_ + b.s_off), cms, b.limbs, 1, 0, 0};
+    q.mods = b.mods;
+    q.log_n = b.log_n;
+    q.counter_off = counter_off[bi];
+    qb[bi] = q;
+  }
+  std::memcpy(h_lists_ + items_off, items.data(), items.size() * sizeof(QueueItem));
+  e = cudaMemcpyAsync(d_lists_, h_lists_, bytes, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaEventRecord(staged_, s);
+  // ticket counter and limb counters start at zero; the status word (index 0) is sticky
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_queue_ctl_ + 1, 0, (1 + counters) * sizeof(uint32_t), s);
+  if (e != cudaSuccess) return fail_cuda(e, "queue upload");
+
+  QueueLaunch ql;
+  ql.buckets = reinterpret_cast<const QueueBucket*>(d_lists_ + buckets_off);
+  ql.items = reinterpret_cast<const QueueItem*>(d_lists_ + items_off);
+  ql.n_items = (uint32_t)items.size();
+  ql.status = d_queue_ctl_;
+  ql.next = d_queue_ctl_ + 1;
+  ql.done = d_queue_ctl_ + 2;
+  ql.timeout_ns = timeout_ns;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device());
+  ql.grid = (uint32_t)std::min<size_t>(items.size(), (size_t)std::max(sms, 1) * 2);
+  const uint64_t l0 = g_kernel_launches.load();
+  e = launch_batch_queue(ql, s);
+  last_launches_ = g_kernel_launches.load() - l0;
+  return e == cudaSuccess ? kOk : fail_cuda(e, "queue launch");
+}
+
+int BatchExecutor::queue_status(cudaStream_t s, uint32_t* status) {
+  *status = 0;
+  if (!d_queue_ctl_) return kOk;
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = cudaMemcpy(status, d_queue_ctl_, 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemset(d_queue_ctl_, 0, 4);
+  return e == cudaSuccess ? kOk : fail_cuda(e, "queue status");
+}
+
+int BatchExecutor::queue_wait_check(DeviceContext* ctx, cudaStream_t s, uint64_t timeout_ns, uint32_t* status) {
+  // one N = 2^14 limb whose column passes are never queued: its 4 row steps
+  // and 4 inverse column passes each wait on a counter nothing increments
+  constexpr uint32_t log_n = 14;
+  const DevMod* mods;
+  int st = ctx->ensure_tables(log_n, 0, 1, &mods);
+  if (st != kOk) return st;
+  if (!queue_attrs_) {
+    const cudaError_t e = queue_set_attributes();
+    if (e != cudaSuccess) return fail_cuda(e, "queue kernel attributes");
+    queue_attrs_ = true;
+  }
+  const size_t nw = (size_t)1 << log_n;
+  st = reserve_scratch(3 * nw);  // c, a = b, scratch: real buffers, the items touch them
+  if (st == kOk) st = reserve_lists(4096);
+  if (st == kOk) st = reserve_queue_ctl(4);
+  if (st != kOk) return st;
+  cudaError_t e = cudaEventSynchronize(staged_);
+  if (e != cudaSuccess) return fail_cuda(e, "batch staging wait");
+  uint64_t* ptrs = reinterpret_cast<uint64_t*>(h_lists_);
+  ptrs[0] = reinterpret_cast<uint64_t>(d_scratch_);           // c
+  ptrs[1] = reinterpret_cast<uint64_t>(d_scratch_ + nw);      // a, b
+  ptrs[2] = reinterpret_cast<uint64_t>(d_scratch_ + 2 * nw);  // scratch
+  reinterpret_cast<uint32_t*>(h_lists_ + 32)[0] = 0;          // cm
+  QueueBucket q;
+  const uint32_t* cms = reinterpret_cast<const uint32_t*>(d_lists_ + 32);
+  q.c = LimbSet{nullptr, reinterpret_cast<uint64_t* const*>(d_lists_), cms, 1, 1, 0, 0};
+  q.a = ConstLimbSet{nullptr, reinterpret_cast<const uint64_t* const*>(d_lists_ + 8), cms, 1, 1, 0, 0};
+  q.b = q.a;
+  q.s = LimbSet{nullptr, reinterpret_cast<uint64_t* const*>(d_lists_ + 16), cms, 1, 1, 0, 0};
+  q.mods = mods;
+  q.log_n = log_n;
+  q.counter_off = 0;
+  std::memcpy(h_lists_ + 64, &q, sizeof q);
+  QueueItem* items = reinterpret_cast<QueueItem*>(h_lists_ + 64 + sizeof(QueueBucket) + 16);
+  const uint32_t tiles = 1u << (log_n - kQueueTileLog);
+  for (uint32_t t = 0; t < tiles; ++t) {
+    items[t] = QueueItem{kItemRows, t};
+    items[tiles + t] = QueueItem{kItemColInv, t};
+  }
+  const size_t bytes = 64 + sizeof(QueueBucket) + 16 + 2 * tiles * sizeof(QueueItem);
+  e = cudaMemsetAsync(d_scratch_, 0, 3 * nw * sizeof(uint64_t), s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_lists_, h_lists_, bytes, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaEventRecord(staged_, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_queue_ctl_ + 1, 0, 3 * sizeof(uint32_t), s);
+  if (e != cudaSuccess) return fail_cuda(e, "queue check upload");
+  QueueLaunch ql;
+  ql.buckets = reinterpret_cast<const QueueBucket*>(d_lists_ + 64);
+  ql.items = reinterpret_cast<const QueueItem*>(d_lists_ + 64 + sizeof(QueueBucket) + 16);
+  ql.n_items = 2 * tiles;
+  ql.status = d_queue_ctl_;
+  ql.next = d_queue_ctl_ + 1;
+  ql.done = d_queue_ctl_ + 2;
+  ql.timeout_ns = timeout_ns;
+  ql.grid = 2;
+  e = launch_batch_queue(ql, s);
+  if (e != cudaSuccess) return fail_cuda(e, "queue check launch");
+  return queue_status(s, status);
+}
+
 }  // namespace yell_gb300
 
 using namespace yell_gb300;
 
 namespace {
+
+// Bound of each dependency wait in the persistent batch kernel.
+constexpr uint64_t kQueueWaitNs = 2'000'000'000ull;
 
 int validate(const yell_polymul_desc& d) {
   if (!d.c || !d.a || !d.b) return fail(kInvalidArgument, "null pointer in a batch entry");
@@ -292,4 +513,61 @@ extern "C" int yell_dev_polymul_batch(const yell_polymul_desc* descs, uint32_t n
     if (e != cudaSuccess) return fail_cuda(e, "batch stream ordering");
   }
   return kOk;
+}
+
+extern "C" int yell_dev_polymul_batch_queue(const yell_polymul_desc* descs, uint32_t n, void* stream) {
+  if (!descs || n == 0) return fail(kInvalidArgument, "empty batch");
+  for (uint32_t i = 0; i < n; ++i) {
+    const int st = validate(descs[i]);
+    if (st != kOk) return st;
+  }
+  int st = kOk;
+  DeviceContext* ctx = DeviceContext::current(&st);
+  if (!ctx) return st;
+  for (uint32_t i = 0; i < n; ++i) {
+    const DevMod* mods;
+    st = ctx->ensure_tables(descs[i].log_n, descs[i].cm0, descs[i].L, &mods);
+    if (st != kOk) return st;
+  }
+  DeviceBatch* db = device_batch(ctx->device(), &st);
+  if (!db) return st;
+  std::lock_guard<std::mutex> g(db->mu);
+  cudaStream_t s = ctx->stream();
+  cudaError_t e;
+  if (stream) {
+    e = cudaEventRecord(db->user_ev, static_cast<cudaStream_t>(stream));
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, db->user_ev, 0);
+    if (e != cudaSuccess) return fail_cuda(e, "batch stream ordering");
+  }
+  st = db->exec.run_queue(ctx, descs, n, s, kQueueWaitNs);
+  if (st != kOk) return st;
+  if (stream) {
+    e = cudaEventRecord(db->done_ev, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(static_cast<cudaStream_t>(stream), db->done_ev, 0);
+    if (e != cudaSuccess) return fail_cuda(e, "batch stream ordering");
+  }
+  return kOk;
+}
+
+extern "C" int yell_batch_queue_status(uint32_t* status) {
+  if (!status) return fail(kInvalidArgument, "null output");
+  int st = kOk;
+  DeviceContext* ctx = DeviceContext::current(&st);
+  if (!ctx) return st;
+  DeviceBatch* db = device_batch(ctx->device(), &st);
+  if (!db) return st;
+  std::lock_guard<std::mutex> g(db->mu);
+  return db->exec.queue_status(ctx->stream(), status);
+}
+
+extern "C" int yell_batch_queue_wait_check(uint64_t timeout_ns, uint32_t* status) {
+  if (!status) return fail(kInvalidArgument, "null output");
+  if (timeout_ns == 0 || timeout_ns > 10'000'000'000ull) return fail(kInvalidArgument, "timeout must be in (0, 10 s]");
+  int st = kOk;
+  DeviceContext* ctx = DeviceContext::current(&st);
+  if (!ctx) return st;
+  DeviceBatch* db = device_batch(ctx->device(), &st);
+  if (!db) return st;
+  std::lock_guard<std::mutex> g(db->mu);
+  return db->exec.queue_wait_check(ctx, ctx->stream(), timeout_ns, status);
 }

@@ -33,6 +33,18 @@ class BatchExecutor {
   int run(DeviceContext* ctx, const yell_polymul_desc* descs, uint64_t* const* desc_scratch,
           uint32_t n, cudaStream_t s, bool use_graph, bool fork = true);
 
+  // The same batch as one launch of the persistent queue kernel: the work
+  // items of every bucket in one device queue (batch_queue.h).  Asynchronous
+  // on s; a dependency wait that exceeds timeout_ns records YELL_ERR_TIMEOUT
+  // in the status word read by queue_status().
+  int run_queue(DeviceContext* ctx, const yell_polymul_desc* descs, uint32_t n, cudaStream_t s,
+                uint64_t timeout_ns);
+  // Waits for s and returns (and clears) the queue kernel's status word.
+  int queue_status(cudaStream_t s, uint32_t* status);
+  // A queue whose row steps depend on column passes that are never queued:
+  // every wait runs out after timeout_ns (the bounded-wait check).
+  int queue_wait_check(DeviceContext* ctx, cudaStream_t s, uint64_t timeout_ns, uint32_t* status);
+
   // Grows the list buffers to hold `limbs` limbs now (so later runs do not
   // reallocate, which would synchronise the device).
   int reserve_limbs(size_t limbs);
@@ -55,6 +67,7 @@ class BatchExecutor {
 
   int reserve_lists(size_t bytes);
   int reserve_scratch(size_t words);
+  int reserve_queue_ctl(size_t words);
   void drop_graphs();
   cudaError_t launch_buckets(const std::vector<Bucket>& buckets, cudaStream_t s, bool scratch_lists,
                              bool fork);
@@ -64,6 +77,9 @@ class BatchExecutor {
   size_t lists_bytes_ = 0;
   uint64_t* d_scratch_ = nullptr;
   size_t scratch_words_ = 0;
+  uint32_t* d_queue_ctl_ = nullptr;  // [0] status, [1] ticket counter, [2..] per-limb counters
+  size_t queue_ctl_words_ = 0;
+  bool queue_attrs_ = false;
   uint64_t generation_ = 0;
   std::array<cudaStream_t, kDegrees> side_{};
   std::array<cudaEvent_t, kDegrees> join_{};

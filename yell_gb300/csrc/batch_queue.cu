@@ -1,0 +1,144 @@
+// The persistent batch kernel.  A grid of resident CTAs takes tickets from a
+// device counter in queue order; the host writes the queue so that every item
+// comes after the items it depends on (all forward column passes, then the
+// whole-limb items, then the row steps, then the inverse column passes).
+// Whoever holds the smallest unfinished ticket has all its dependencies done,
+// so the queue always makes progress.  A dependency wait (a row step waits
+// for the column passes of its limb, an inverse column pass for the row
+// steps) is bounded in time and in iterations: on expiry it records
+// YELL_ERR_TIMEOUT in a status word the host reads, and proceeds.
+//
+// Item bodies are the polymul kernels' own bodies (ntt_kernels.cuh) called
+// with the item's tile index; words written by other CTAs of this launch are
+// read through L2 (ld.global.cg), never the non-coherent path; a finished
+// item publishes its stores with a fence before bumping its limb's counter.
+#include "batch_queue.h"
+
+#include "ntt_kernels.cuh"
+#include "yell_gb300.h"
+
+namespace yell_gb300 {
+namespace {
+
+constexpr int kQueueThreads = 256;
+static_assert(kQueueTileLog == (uint32_t)kTileLog, "queue tiles are the two-pass tiles");
+
+template <int LOGN>
+constexpr int k1_of() {
+  return LOGN == 13 ? 6 : (LOGN <= 15 ? 7 : (LOGN == 16 ? 9 : 8));
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait until *p >= need (one thread).  Gives up when the global
+// timer has advanced timeout_ns, or the SM clock 3 * timeout_ns cycles (a
+// second bound that does not rely on the global timer), or after 2^24 polls,
+// recording YELL_ERR_TIMEOUT.
+__device__ void wait_count(const uint32_t* p, uint32_t need, uint32_t* status, uint64_t timeout_ns) {
+  const uint64_t t0 = global_ns();
+  const long long c0 = clock64();
+  const long long cycles = (long long)(3 * timeout_ns);
+  uint32_t sleep_ns = 32;
+  for (uint32_t polls = 0;; ++polls) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    if (v >= need) return;
+    if (global_ns() - t0 > timeout_ns || clock64() - c0 > cycles || polls >= (1u << 24)) {
+      atomicCAS(status, 0u, (uint32_t)YELL_ERR_TIMEOUT);
+      return;
+    }
+    __nanosleep(sleep_ns);
+    if (sleep_ns < 1024) sleep_ns <<= 1;
+  }
+}
+
+template <int LOGN>
+__device__ __forceinline__ void run_item(uint32_t kind, const QueueBucket& B, uint32_t bid, uint64_t* smem) {
+  if constexpr (LOGN < (int)kQueueFirstTwoPass) {
+    using C = TileCfg<(LOGN >= 4 ? kTileLog : kTileLog - 1), LOGN, 0, (LOGN >= 4 ? 4 : 3)>;
+    static_assert(C::THREADS == kQueueThreads, "whole-limb tile of the queue kernel");
+    polymul_whole_body<C>(B.c, B.a, B.b, B.mods, bid, smem);
+  } else {
+    constexpr int K1 = k1_of<LOGN>(), LOGB = LOGN - K1;
+    using CC = ColCfg<LOGN, K1>;
+    using RC = RowCfg<LOGN, K1>;
+    static_assert(CC::THREADS == kQueueThreads && RC::THREADS == kQueueThreads, "two-pass tiles of the queue kernel");
+    if (kind == kItemColFwd) col_pass2_body<CC, LOGB>(B.a, B.b, B.c, B.s, B.mods, bid, smem);
+    else if (kind == kItemRows) polymul_rows_body<RC, K1, true>(B.c, as_const(B.s), B.mods, bid, smem);
+    else col_pass_body<CC, LOGB, true, true>(as_const(B.c), B.c, B.mods, bid, smem);
+  }
+}
+
+__device__ __forceinline__ void dispatch(uint32_t kind, const QueueBucket& B, uint32_t bid, uint64_t* smem) {
+  switch (B.log_n) {
+    case 3: run_item<3>(kind, B, bid, smem); break;
+    case 4: run_item<4>(kind, B, bid, smem); break;
+    case 5: run_item<5>(kind, B, bid, smem); break;
+    case 6: run_item<6>(kind, B, bid, smem); break;
+    case 7: run_item<7>(kind, B, bid, smem); break;
+    case 8: run_item<8>(kind, B, bid, smem); break;
+    case 9: run_item<9>(kind, B, bid, smem); break;
+    case 10: run_item<10>(kind, B, bid, smem); break;
+    case 11: run_item<11>(kind, B, bid, smem); break;
+    case 12: run_item<12>(kind, B, bid, smem); break;
+    case 13: run_item<13>(kind, B, bid, smem); break;
+    case 14: run_item<14>(kind, B, bid, smem); break;
+    case 15: run_item<15>(kind, B, bid, smem); break;
+    case 16: run_item<16>(kind, B, bid, smem); break;
+    case 17: run_item<17>(kind, B, bid, smem); break;
+    default: break;
+  }
+}
+
+__global__ void __launch_bounds__(kQueueThreads, 2) k_batch_queue(QueueLaunch q) {
+  extern __shared__ __align__(16) uint64_t smem[];
+  __shared__ uint32_t s_ticket;
+  for (;;) {
+    if (threadIdx.x == 0) s_ticket = atomicAdd(q.next, 1u);
+    __syncthreads();
+    const uint32_t t = s_ticket;
+    if (t >= q.n_items) break;
+    const QueueItem it = q.items[t];
+    const uint32_t kind = it.bucket_kind & 0xFFu;
+    const QueueBucket B = q.buckets[it.bucket_kind >> 8];
+    uint32_t* publish = nullptr;
+    if (kind != kItemWhole) {
+      const uint32_t tpl = B.log_n - kTileLog;  // tiles per limb: 2^tpl
+      uint32_t* cnt = q.done + B.counter_off + 2 * B.c.ordered(it.bid >> tpl);
+      if (kind != kItemColFwd) {
+        if (threadIdx.x == 0) wait_count(cnt + (kind == kItemRows ? 0 : 1), 1u << tpl, q.status, q.timeout_ns);
+        __syncthreads();
+      }
+      if (kind != kItemColInv) publish = cnt + (kind == kItemColFwd ? 0 : 1);
+    }
+    dispatch(kind, B, it.bid, smem);
+    __syncthreads();  // every thread's stores issued; the tiles are free again
+    if (publish && threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(publish, 1u);
+    }
+  }
+}
+
+}  // namespace
+
+uint32_t queue_k1(uint32_t log_n) { return log_n == 13 ? 6u : (log_n <= 15 ? 7u : (log_n == 16 ? 9u : 8u)); }
+
+size_t queue_smem_bytes() { return 2 * kTileSmemBytes; }
+
+cudaError_t queue_set_attributes() {
+  return cudaFuncSetAttribute(k_batch_queue, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)queue_smem_bytes());
+}
+
+cudaError_t launch_batch_queue(const QueueLaunch& q, cudaStream_t s) {
+  LaunchScope ps("batch_queue", s);
+  k_batch_queue<<<q.grid, kQueueThreads, queue_smem_bytes(), s>>>(q);
+  g_kernel_launches += 1;
+  return cudaGetLastError();
+}
+
+}  // namespace yell_gb300

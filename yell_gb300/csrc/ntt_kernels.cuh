@@ -40,6 +40,29 @@ __device__ __forceinline__ ulonglong2 ld_pair(const uint64_t* p) {
   return __ldg(reinterpret_cast<const ulonglong2*>(p));
 }
 
+// Loads of words another CTA of the same launch wrote (the persistent batch
+// kernel's intermediates): through L2, never the non-coherent read-only path.
+__device__ __forceinline__ ulonglong2 ld_pair_cg(const uint64_t* p) {
+  ulonglong2 v;
+  asm volatile("ld.global.cg.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ uint64_t ld_cg(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.global.cg.u64 %0, [%1];" : "=l"(v) : "l"(p));
+  return v;
+}
+template <bool COH>
+__device__ __forceinline__ ulonglong2 ld_pair_t(const uint64_t* p) {
+  if constexpr (COH) return ld_pair_cg(p);
+  else return ld_pair(p);
+}
+template <bool COH>
+__device__ __forceinline__ uint64_t ld_word_t(const uint64_t* p) {
+  if constexpr (COH) return ld_cg(p);
+  else return __ldg(p);
+}
+
 __device__ __forceinline__ void st_pair(uint64_t* p, uint64_t a, uint64_t b) {
   *reinterpret_cast<ulonglong2*>(p) = make_ulonglong2(a, b);
 }
@@ -47,7 +70,7 @@ __device__ __forceinline__ void st_pair(uint64_t* p, uint64_t a, uint64_t b) {
 // ---- direct global access for one round ---------------------------------------
 // Row-type region: word u of the region at g[u]; base_u and offsets are
 // u-space (tile bits below LB + K, LB = 0).
-template <class RG>
+template <class RG, bool COH = false>
 __device__ __forceinline__ void gload_rows(uint64_t* x, const uint64_t* g, uint32_t base_u) {
   constexpr int R = RG::R;
   const uint64_t* gb = g + base_u;
@@ -56,7 +79,7 @@ __device__ __forceinline__ void gload_rows(uint64_t* x, const uint64_t* g, uint3
     for (int m = 0; m < RG::E / 2; ++m)
 #pragma unroll
       for (int j = 0; j < (1 << R); ++j) {
-        const ulonglong2 v = ld_pair(gb + RG::off(2 * m, j));
+        const ulonglong2 v = ld_pair_t<COH>(gb + RG::off(2 * m, j));
         x[((2 * m) << R) | j] = v.x;
         x[((2 * m + 1) << R) | j] = v.y;
       }
@@ -64,7 +87,7 @@ __device__ __forceinline__ void gload_rows(uint64_t* x, const uint64_t* g, uint3
 #pragma unroll
     for (int ex = 0; ex < RG::E; ++ex)
 #pragma unroll
-      for (int j = 0; j < (1 << R); ++j) x[(ex << R) | j] = __ldg(gb + RG::off(ex, j));
+      for (int j = 0; j < (1 << R); ++j) x[(ex << R) | j] = ld_word_t<COH>(gb + RG::off(ex, j));
   }
 }
 
@@ -93,7 +116,7 @@ __device__ __forceinline__ size_t col_base(uint32_t base_v) {
   return ((size_t)(base_v >> RG::LB) << LOGB) + (base_v & ((1u << RG::LB) - 1u));
 }
 
-template <class RG, int LOGB>
+template <class RG, int LOGB, bool COH = false>
 __device__ __forceinline__ void gload_cols(uint64_t* x, const uint64_t* g, uint32_t base_v) {
   constexpr int R = RG::R;
   const uint64_t* gb = g + col_base<RG, LOGB>(base_v);
@@ -101,7 +124,7 @@ __device__ __forceinline__ void gload_cols(uint64_t* x, const uint64_t* g, uint3
   for (int ex = 0; ex < RG::E; ++ex)
 #pragma unroll
     for (int j = 0; j < (1 << R); ++j)
-      x[(ex << R) | j] = __ldg(gb + ((size_t)(RG::off(ex, j) >> RG::LB) << LOGB));
+      x[(ex << R) | j] = ld_word_t<COH>(gb + ((size_t)(RG::off(ex, j) >> RG::LB) << LOGB));
 }
 
 template <class RG, int LOGB>
@@ -235,16 +258,15 @@ __global__ void __launch_bounds__(C::THREADS) k_ntt_whole(LimbSet ls, const DevM
 // limb word (c << LOGB) + col0 + col.  Forward: stages 0..K-1; inverse:
 // stages LOGB..log_n-1 with the scaled last layer.  src and dst may alias.
 // ===========================================================================
-template <class C, int LOGB, bool INV>
-__global__ void __launch_bounds__(C::THREADS) k_col_pass(ConstLimbSet src, LimbSet dst,
-                                                         const DevMod* __restrict__ mods) {
-  extern __shared__ __align__(16) uint64_t smem[];
+template <class C, int LOGB, bool INV, bool COH = false>
+__device__ __forceinline__ void col_pass_body(ConstLimbSet src, LimbSet dst, const DevMod* __restrict__ mods,
+                                              uint32_t bid, uint64_t* smem) {
   constexpr int K = C::K, LB = C::LB, NR = C::NR;
   constexpr uint32_t log_n = K + LOGB;
   constexpr int TPL = LOGB - LB;  // log2(tiles per limb)
   const uint32_t tid = threadIdx.x;
-  const uint32_t limb = dst.ordered(blockIdx.x >> TPL);
-  const uint32_t col0 = (blockIdx.x & ((1u << TPL) - 1u)) << LB;
+  const uint32_t limb = dst.ordered(bid >> TPL);
+  const uint32_t col0 = (bid & ((1u << TPL) - 1u)) << LB;
   const uint64_t* in = src.limb(limb, log_n) + col0;
   uint64_t* out = dst.limb(limb, log_n) + col0;
   const DevMod m = load_mod(mods, dst.cm(limb));
@@ -252,7 +274,7 @@ __global__ void __launch_bounds__(C::THREADS) k_col_pass(ConstLimbSet src, LimbS
   if constexpr (!INV) {
     using R0 = Round<C, 0>;
     const uint32_t b0 = R0::base(tid);
-    gload_cols<R0, LOGB>(x, in, b0);
+    gload_cols<R0, LOGB, COH>(x, in, b0);
     ct_round<R0>(x, m.fwd, R0::HI, R0::gr(b0, 0), m.p);
     if constexpr (NR == 1) {
       gstore_cols<R0, LOGB>(x, out, b0);
@@ -269,7 +291,7 @@ __global__ void __launch_bounds__(C::THREADS) k_col_pass(ConstLimbSet src, LimbS
   } else {
     using RB = Round<C, NR - 1>;  // bottom round, executed first
     const uint32_t bb = RB::base(tid);
-    gload_cols<RB, LOGB>(x, in, bb);
+    gload_cols<RB, LOGB, COH>(x, in, bb);
     if constexpr (NR == 1) {
       gs_round<RB, true>(x, log_n, LOGB + RB::BETA, RB::gr(bb, 0), m);
       gstore_cols<RB, LOGB>(x, out, bb);
@@ -285,6 +307,13 @@ __global__ void __launch_bounds__(C::THREADS) k_col_pass(ConstLimbSet src, LimbS
       gstore_cols<RT, LOGB>(x, out, bt);
     }
   }
+}
+
+template <class C, int LOGB, bool INV>
+__global__ void __launch_bounds__(C::THREADS) k_col_pass(ConstLimbSet src, LimbSet dst,
+                                                         const DevMod* __restrict__ mods) {
+  extern __shared__ __align__(16) uint64_t smem[];
+  col_pass_body<C, LOGB, INV>(src, dst, mods, blockIdx.x, smem);
 }
 
 // ===========================================================================
@@ -351,15 +380,14 @@ __device__ __forceinline__ void fused_product(uint64_t* xa, uint64_t* xb, uint32
 
 // Whole-limb fused polymul: c = INTT(NTT(a) * NTT(b)), N <= 2^13.
 template <class C>
-__global__ void __launch_bounds__(C::THREADS) k_polymul_whole(LimbSet c, ConstLimbSet a, ConstLimbSet b,
-                                                              const DevMod* __restrict__ mods) {
-  extern __shared__ __align__(16) uint64_t smem[];
+__device__ __forceinline__ void polymul_whole_body(LimbSet c, ConstLimbSet a, ConstLimbSet b,
+                                                   const DevMod* __restrict__ mods, uint32_t bid, uint64_t* smem) {
   constexpr int K = C::K, NR = C::NR;
   constexpr uint32_t log_n = K;
   uint64_t* sa = smem;
   uint64_t* sb = smem + tile_smem_words(1u << C::T);
   const uint32_t tid = threadIdx.x;
-  const uint32_t limb0 = blockIdx.x << (C::T - K);
+  const uint32_t limb0 = bid << (C::T - K);
   const uint32_t my_limb = limb0 + C::sub(tid);
   const bool active = my_limb < c.count;
   const DevMod m = load_mod(mods, c.cm(active ? my_limb : 0));
@@ -411,21 +439,27 @@ __global__ void __launch_bounds__(C::THREADS) k_polymul_whole(LimbSet c, ConstLi
   }
 }
 
+template <class C>
+__global__ void __launch_bounds__(C::THREADS) k_polymul_whole(LimbSet c, ConstLimbSet a, ConstLimbSet b,
+                                                              const DevMod* __restrict__ mods) {
+  extern __shared__ __align__(16) uint64_t smem[];
+  polymul_whole_body<C>(c, a, b, mods, blockIdx.x, smem);
+}
+
 // Forward column pass of both polymul operands in one CTA: each thread
 // applies the same butterflies to a's and b's words at the same positions,
 // so every twiddle load serves two butterflies.  a -> ca, b -> cb.
 template <class C, int LOGB>
-__global__ void __launch_bounds__(C::THREADS, 2) k_col_pass2(ConstLimbSet a, ConstLimbSet b, LimbSet ca,
-                                                             LimbSet cb, const DevMod* __restrict__ mods) {
-  extern __shared__ __align__(16) uint64_t smem[];
+__device__ __forceinline__ void col_pass2_body(ConstLimbSet a, ConstLimbSet b, LimbSet ca, LimbSet cb,
+                                               const DevMod* __restrict__ mods, uint32_t bid, uint64_t* smem) {
   constexpr int K = C::K, LB = C::LB, NR = C::NR;
   constexpr uint32_t log_n = K + LOGB;
   constexpr int TPL = LOGB - LB;
   uint64_t* sa = smem;
   uint64_t* sb = smem + tile_smem_words(1u << kTileLog);
   const uint32_t tid = threadIdx.x;
-  const uint32_t limb = ca.ordered(blockIdx.x >> TPL);
-  const uint32_t col0 = (blockIdx.x & ((1u << TPL) - 1u)) << LB;
+  const uint32_t limb = ca.ordered(bid >> TPL);
+  const uint32_t col0 = (bid & ((1u << TPL) - 1u)) << LB;
   const DevMod m = load_mod(mods, ca.cm(limb));
   const uint64_t np = 0 - m.p, p2 = m.p << 1;
   constexpr int E = 1 << C::LOGE;
@@ -454,20 +488,26 @@ __global__ void __launch_bounds__(C::THREADS, 2) k_col_pass2(ConstLimbSet a, Con
   }
 }
 
+template <class C, int LOGB>
+__global__ void __launch_bounds__(C::THREADS, 2) k_col_pass2(ConstLimbSet a, ConstLimbSet b, LimbSet ca,
+                                                             LimbSet cb, const DevMod* __restrict__ mods) {
+  extern __shared__ __align__(16) uint64_t smem[];
+  col_pass2_body<C, LOGB>(a, b, ca, cb, mods, blockIdx.x, smem);
+}
+
 // Two-pass fused row step: ca holds a's column-pass output and receives the
 // row-pass output of the product; sbuf holds b's column-pass output.
-template <class C, int K1>
-__global__ void __launch_bounds__(C::THREADS, 2) k_polymul_rows(LimbSet ca, ConstLimbSet sbuf,
-                                                                const DevMod* __restrict__ mods) {
-  extern __shared__ __align__(16) uint64_t smem[];
+template <class C, int K1, bool COH = false>
+__device__ __forceinline__ void polymul_rows_body(LimbSet ca, ConstLimbSet sbuf, const DevMod* __restrict__ mods,
+                                                  uint32_t bid, uint64_t* smem) {
   constexpr int K = C::K, NR = C::NR;
   constexpr uint32_t log_n = K + K1;
   constexpr int TPL = log_n - kTileLog;
   uint64_t* sa = smem;
   uint64_t* sb = smem + tile_smem_words(1u << kTileLog);
   const uint32_t tid = threadIdx.x;
-  const uint32_t limb = ca.ordered(blockIdx.x >> TPL);
-  const uint32_t off = (blockIdx.x & ((1u << TPL) - 1u)) << kTileLog;
+  const uint32_t limb = ca.ordered(bid >> TPL);
+  const uint32_t off = (bid & ((1u << TPL) - 1u)) << kTileLog;
   uint64_t* pa = ca.limb(limb, log_n) + off;
   const uint64_t* pb = sbuf.limb(limb, log_n) + off;
   const DevMod m = load_mod(mods, ca.cm(limb));
@@ -476,8 +516,8 @@ __global__ void __launch_bounds__(C::THREADS, 2) k_polymul_rows(LimbSet ca, Cons
   uint64_t xa[E], xb[E];
   using R0 = Round<C, 0>;
   const uint32_t b0 = R0::base(tid);
-  gload_rows<R0>(xa, pa, b0);
-  gload_rows<R0>(xb, pb, b0);
+  gload_rows<R0, COH>(xa, pa, b0);
+  gload_rows<R0, COH>(xb, pb, b0);
   ct_stages2<R0::R, R0::E, 0>(xa, xb, m.fwd, K1 + R0::HI, R0::gr(b0, G), 0 - m.p, m.p << 1);
   smem_store<R0>(xa, sa, b0);
   smem_store<R0>(xb, sb, b0);
@@ -495,6 +535,13 @@ __global__ void __launch_bounds__(C::THREADS, 2) k_polymul_rows(LimbSet ca, Cons
   smem_load<R0>(xa, sa, b0);
   gs_round<R0, false>(xa, log_n, R0::BETA, R0::gr(b0, G), m);
   gstore_rows<R0>(xa, pa, b0);
+}
+
+template <class C, int K1>
+__global__ void __launch_bounds__(C::THREADS, 2) k_polymul_rows(LimbSet ca, ConstLimbSet sbuf,
+                                                                const DevMod* __restrict__ mods) {
+  extern __shared__ __align__(16) uint64_t smem[];
+  polymul_rows_body<C, K1>(ca, sbuf, mods, blockIdx.x, smem);
 }
 
 // ===========================================================================
