@@ -57,45 +57,44 @@ __device__ void wait_count(const uint32_t* p, uint32_t need, uint32_t* status, u
 }
 
 template <int LOGN>
-__device__ __forceinline__ void run_item(uint32_t kind, const QueueBucket& B, uint32_t bid, uint64_t* smem) {
+__device__ __forceinline__ void run_item(uint32_t kind, const QueueBucket& B, uint32_t bid) {
   if constexpr (LOGN < (int)kQueueFirstTwoPass) {
     using C = TileCfg<(LOGN >= 4 ? kTileLog : kTileLog - 1), LOGN, 0, (LOGN >= 4 ? 4 : 3)>;
     static_assert(C::THREADS == kQueueThreads, "whole-limb tile of the queue kernel");
-    polymul_whole_body<C>(B.c, B.a, B.b, B.mods, bid, smem);
+    polymul_whole_body<C>(B.c, B.a, B.b, B.mods, bid);
   } else {
     constexpr int K1 = k1_of<LOGN>(), LOGB = LOGN - K1;
     using CC = ColCfg<LOGN, K1>;
     using RC = RowCfg<LOGN, K1>;
     static_assert(CC::THREADS == kQueueThreads && RC::THREADS == kQueueThreads, "two-pass tiles of the queue kernel");
-    if (kind == kItemColFwd) col_pass2_body<CC, LOGB>(B.a, B.b, B.c, B.s, B.mods, bid, smem);
-    else if (kind == kItemRows) polymul_rows_body<RC, K1, true>(B.c, as_const(B.s), B.mods, bid, smem);
-    else col_pass_body<CC, LOGB, true, true>(as_const(B.c), B.c, B.mods, bid, smem);
+    if (kind == kItemColFwd) col_pass2_body<CC, LOGB>(B.a, B.b, B.c, B.s, B.mods, bid);
+    else if (kind == kItemRows) polymul_rows_body<RC, K1, true>(B.c, as_const(B.s), B.mods, bid);
+    else col_pass_body<CC, LOGB, true, true>(as_const(B.c), B.c, B.mods, bid);
   }
 }
 
-__device__ __forceinline__ void dispatch(uint32_t kind, const QueueBucket& B, uint32_t bid, uint64_t* smem) {
+__device__ __forceinline__ void dispatch(uint32_t kind, const QueueBucket& B, uint32_t bid) {
   switch (B.log_n) {
-    case 3: run_item<3>(kind, B, bid, smem); break;
-    case 4: run_item<4>(kind, B, bid, smem); break;
-    case 5: run_item<5>(kind, B, bid, smem); break;
-    case 6: run_item<6>(kind, B, bid, smem); break;
-    case 7: run_item<7>(kind, B, bid, smem); break;
-    case 8: run_item<8>(kind, B, bid, smem); break;
-    case 9: run_item<9>(kind, B, bid, smem); break;
-    case 10: run_item<10>(kind, B, bid, smem); break;
-    case 11: run_item<11>(kind, B, bid, smem); break;
-    case 12: run_item<12>(kind, B, bid, smem); break;
-    case 13: run_item<13>(kind, B, bid, smem); break;
-    case 14: run_item<14>(kind, B, bid, smem); break;
-    case 15: run_item<15>(kind, B, bid, smem); break;
-    case 16: run_item<16>(kind, B, bid, smem); break;
-    case 17: run_item<17>(kind, B, bid, smem); break;
+    case 3: run_item<3>(kind, B, bid); break;
+    case 4: run_item<4>(kind, B, bid); break;
+    case 5: run_item<5>(kind, B, bid); break;
+    case 6: run_item<6>(kind, B, bid); break;
+    case 7: run_item<7>(kind, B, bid); break;
+    case 8: run_item<8>(kind, B, bid); break;
+    case 9: run_item<9>(kind, B, bid); break;
+    case 10: run_item<10>(kind, B, bid); break;
+    case 11: run_item<11>(kind, B, bid); break;
+    case 12: run_item<12>(kind, B, bid); break;
+    case 13: run_item<13>(kind, B, bid); break;
+    case 14: run_item<14>(kind, B, bid); break;
+    case 15: run_item<15>(kind, B, bid); break;
+    case 16: run_item<16>(kind, B, bid); break;
+    case 17: run_item<17>(kind, B, bid); break;
     default: break;
   }
 }
 
 __global__ void __launch_bounds__(kQueueThreads, 2) k_batch_queue(QueueLaunch q) {
-  extern __shared__ __align__(16) uint64_t smem[];
   __shared__ uint32_t s_ticket;
   for (;;) {
     if (threadIdx.x == 0) s_ticket = atomicAdd(q.next, 1u);
@@ -115,7 +114,7 @@ __global__ void __launch_bounds__(kQueueThreads, 2) k_batch_queue(QueueLaunch q)
       }
       if (kind != kItemColInv) publish = cnt + (kind == kItemColFwd ? 0 : 1);
     }
-    dispatch(kind, B, it.bid, smem);
+    dispatch(kind, B, it.bid);
     __syncthreads();  // every thread's stores issued; the tiles are free again
     if (publish && threadIdx.x == 0) {
       __threadfence();
