@@ -188,7 +188,7 @@ int yell_batch_queue_status(uint32_t* status);
 int yell_batch_queue_wait_check(uint64_t timeout_ns, uint32_t* status);
 
 /* ---- serving loop (no counterpart in the reference) ------------------------
- * Continuous batching of polymul requests of mixed size.  A scheduler thread
+ * Continuous batching of polymul and NTT requests of mixed size.  A scheduler thread
  * owns max_inflight stream slots; whenever one is free it admits queued
  * requests in arrival order while an HBM budget (a device arena allocated at
  * create time) can hold their buffers, and launches everything admitted as
@@ -205,9 +205,12 @@ typedef struct yell_server_config {
   uint32_t reserved;
 } yell_server_config;
 enum yell_request_flags {
-  YELL_REQ_HOST = 0,           /* a, b, c are host arrays of L*N words */
-  YELL_REQ_DEVICE = 1,         /* a, b, c are device arrays (16-byte aligned) */
-  YELL_REQ_DISCARD_OUTPUT = 2  /* compute into a server buffer and drop it (load tests) */
+  YELL_REQ_HOST = 0,            /* a, b, c are host arrays of L*N words */
+  YELL_REQ_DEVICE = 1,          /* a, b, c are device arrays (16-byte aligned) */
+  YELL_REQ_DISCARD_OUTPUT = 2,  /* compute into a server buffer and drop it (load tests) */
+  /* the request's operation (none of these: polymul c = a * b) */
+  YELL_REQ_NTT_FORWARD = 4,     /* c = ntt<N>::forward(a), b unused */
+  YELL_REQ_NTT_BACKWARD = 8     /* c = ntt<N>::backward(a), b unused */
 };
 typedef struct yell_polymul_request {
   const uint64_t* a;

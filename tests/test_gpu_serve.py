@@ -162,3 +162,39 @@ def test_poisson_load_device_resident(cuda):
         st = srv.load_test(templates, offered_rps=20000, duration_s=0.3, seed=5)
     assert st["completed"] == st["submitted"] > 1000
     assert st["failed"] == 0 and 0 < st["p50_us"] <= st["p99_us"] <= st["max_us"]
+
+
+def test_ntt_requests_in_a_mix(cuda, orc):
+    """Forward and backward NTT requests (host and device, in place and not)
+    served in the same batches as polymul requests; each equals the oracle."""
+    torch = cuda
+    with Server(hbm_budget_bytes=2 << 30, max_inflight=3) as srv:
+        jobs = []
+        for i, (log_n, L) in enumerate([(10, 2), (14, 1), (12, 3), (16, 2), (11, 1), (13, 2)]):
+            a, b = _operands(3000 + 4 * i, log_n, L, i)
+            # host forward
+            f = np.zeros_like(a)
+            jobs.append(("fwd", srv.submit(a, None, f, log_n, L, cm0=i, op="forward"), a, f, log_n, L, i))
+            # host backward of the forward output's reference values
+            fa = np.stack([orc.forward(a[l], log_n, i + l) for l in range(L)])
+            bk = np.zeros_like(a)
+            jobs.append(("bwd", srv.submit(fa, None, bk, log_n, L, cm0=i, op="backward"), fa, bk, log_n, L, i))
+            # device forward in place
+            d = torch.from_numpy(a.view(np.int64).copy()).cuda()
+            jobs.append(("dfwd", srv.submit(d, None, d, log_n, L, cm0=i, device=True, op="forward"), a, d, log_n, L, i))
+            # a polymul in the same batch
+            c = np.zeros_like(a)
+            jobs.append(("mul", srv.submit(a, b, c, log_n, L, cm0=i), (a, b), c, log_n, L, i))
+        for kind, rid, x, out, log_n, L, cm0 in jobs:
+            assert srv.wait(rid)["status"] == 0, kind
+            if kind == "mul":
+                want = orc.polymul(x[0], x[1], log_n, cm0)
+            elif kind == "bwd":
+                want = np.stack([orc.backward(x[l], log_n, cm0 + l) for l in range(L)])
+            else:
+                want = np.stack([orc.forward(x[l], log_n, cm0 + l) for l in range(L)])
+            got = out if isinstance(out, np.ndarray) else out.cpu().numpy().view(np.uint64).reshape(want.shape)
+            assert np.array_equal(got, want), (kind, log_n, L)
+        with pytest.raises(y.YellError):
+            a, _ = _operands(9, 10, 1)
+            srv._submit_flags(a, None, np.zeros_like(a), 10, 1, 0, 4 | 8)

@@ -103,10 +103,16 @@ struct yell_server {
 
 namespace {
 
+bool is_ntt(const yell_polymul_request& r) { return r.flags & (YELL_REQ_NTT_FORWARD | YELL_REQ_NTT_BACKWARD); }
+
 size_t footprint_of(const yell_polymul_request& r, size_t words, uint32_t log_n) {
   size_t bytes = 0;
   const size_t limb_bytes = words * sizeof(uint64_t);
   const bool device = r.flags & YELL_REQ_DEVICE;
+  if (is_ntt(r)) {  // the transform runs in place in the output buffer
+    if (!device || (r.flags & YELL_REQ_DISCARD_OUTPUT)) bytes += RangeAllocator::round(limb_bytes);
+    return bytes;
+  }
   if (!device) bytes += 2 * RangeAllocator::round(limb_bytes);  // a, b
   if (!device || (r.flags & YELL_REQ_DISCARD_OUTPUT)) bytes += RangeAllocator::round(limb_bytes);  // c
   if (log_n > 13) bytes += RangeAllocator::round(limb_bytes);  // two-pass scratch
@@ -174,7 +180,7 @@ void yell_server::complete(const ReqPtr& r, int status, Clock::time_point t) {
   if (status == kOk) {
     ++completed;
     latencies.push_back(us_between(r->t_submit, t));
-    limb_ntts += 3.0 * r->req.L;
+    limb_ntts += (is_ntt(r->req) ? 1.0 : 3.0) * r->req.L;
     last_done = t;
   } else if (status == kCancelled) {
     ++cancelled;
@@ -220,7 +226,10 @@ bool yell_server::admit_into(Slot& s, std::vector<ReqPtr>* batch) {
     uint8_t* p = arena + off;
     const size_t lb = RangeAllocator::round(r->words * sizeof(uint64_t));
     const bool device = r->req.flags & YELL_REQ_DEVICE;
-    if (!device) {
+    if (is_ntt(r->req)) {
+      r->d_a = device ? const_cast<uint64_t*>(r->req.a) : nullptr;  // host input goes straight to c
+      r->d_b = nullptr;
+    } else if (!device) {
       r->d_a = reinterpret_cast<uint64_t*>(p);
       p += lb;
       r->d_b = reinterpret_cast<uint64_t*>(p);
@@ -235,7 +244,7 @@ bool yell_server::admit_into(Slot& s, std::vector<ReqPtr>* batch) {
     } else {
       r->d_c = r->req.c;
     }
-    r->d_s = r->req.log_n > 13 ? reinterpret_cast<uint64_t*>(p) : nullptr;
+    r->d_s = (r->req.log_n > 13 && !is_ntt(r->req)) ? reinterpret_cast<uint64_t*>(p) : nullptr;
     r->t_start = t;
     batch->push_back(r);
   }
@@ -244,22 +253,50 @@ bool yell_server::admit_into(Slot& s, std::vector<ReqPtr>* batch) {
 
 int yell_server::launch(Slot& s, std::vector<ReqPtr>& batch) {
   const size_t n = batch.size();
-  std::vector<yell_polymul_desc> descs(n);
-  std::vector<uint64_t*> scratch(n);
+  std::vector<yell_polymul_desc> descs;
+  std::vector<uint64_t*> scratch;
+  descs.reserve(n);
+  scratch.reserve(n);
   cudaError_t e = cudaSuccess;
   for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
     Request& r = *batch[i];
     const size_t bytes = r.words * sizeof(uint64_t);
+    if (is_ntt(r.req)) {  // input into the output buffer, transformed there in place
+      if (!(r.req.flags & YELL_REQ_DEVICE))
+        e = cudaMemcpyAsync(r.d_c, r.req.a, bytes, cudaMemcpyHostToDevice, s.stream);
+      else if (r.d_c != r.d_a)
+        e = cudaMemcpyAsync(r.d_c, r.d_a, bytes, cudaMemcpyDeviceToDevice, s.stream);
+      continue;
+    }
     if (!(r.req.flags & YELL_REQ_DEVICE)) {
       e = cudaMemcpyAsync(r.d_a, r.req.a, bytes, cudaMemcpyHostToDevice, s.stream);
       if (e == cudaSuccess) e = cudaMemcpyAsync(r.d_b, r.req.b, bytes, cudaMemcpyHostToDevice, s.stream);
     }
-    descs[i] = yell_polymul_desc{r.d_c, r.d_a, r.d_b, r.req.log_n, r.req.L, r.req.cm0, 0};
-    scratch[i] = r.d_s;
+    descs.push_back(yell_polymul_desc{r.d_c, r.d_a, r.d_b, r.req.log_n, r.req.L, r.req.cm0, 0});
+    scratch.push_back(r.d_s);
   }
   if (e != cudaSuccess) return fail_cuda(e, "server H2D");
-  const int st = s.exec.run(ctx, descs.data(), scratch.data(), (uint32_t)n, s.stream, false, false);
-  if (st != kOk) return st;
+  if (!descs.empty()) {
+    const int st = s.exec.run(ctx, descs.data(), scratch.data(), (uint32_t)descs.size(), s.stream, false, false);
+    if (st != kOk) return st;
+  }
+  for (size_t i = 0; i < n && e == cudaSuccess; ++i) {  // NTT requests: one launch sequence each
+    Request& r = *batch[i];
+    if (!is_ntt(r.req)) continue;
+    const DevMod* mods = ctx->tables_ready(r.req.log_n, r.req.cm0, r.req.L);
+    if (!mods) return fail(kInvalidArgument, "server: twiddle tables not built");
+    LimbSet ls;
+    ls.base = r.d_c;
+    ls.ptrs = nullptr;
+    ls.cms = nullptr;
+    ls.count = r.req.L;
+    ls.L = r.req.L;
+    ls.cm0 = r.req.cm0;
+    ls.pad_ = 0;
+    e = launch_ntt(ls, r.req.log_n, mods,
+                   (r.req.flags & YELL_REQ_NTT_FORWARD) ? NttDir::kForward : NttDir::kBackward, ctx->shape,
+                   s.stream);
+  }
   for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
     Request& r = *batch[i];
     if (!(r.req.flags & YELL_REQ_DEVICE))
@@ -369,15 +406,21 @@ int yell_server_destroy(yell_server* s) {
 
 int yell_server_submit(yell_server* s, const yell_polymul_request* r, uint64_t* id) {
   if (!s || !r || !id) return fail(kInvalidArgument, "null argument");
-  if (!r->a || !r->b || (!r->c && !(r->flags & YELL_REQ_DISCARD_OUTPUT)))
+  const bool ntt = is_ntt(*r);
+  if ((r->flags & YELL_REQ_NTT_FORWARD) && (r->flags & YELL_REQ_NTT_BACKWARD))
+    return fail(kInvalidArgument, "a request is a forward or a backward NTT, not both");
+  if (!r->a || (!ntt && !r->b) || (!r->c && !(r->flags & YELL_REQ_DISCARD_OUTPUT)))
     return fail(kInvalidArgument, "null operand");
+  if (!ntt && (r->flags & YELL_REQ_DEVICE) && !(r->flags & YELL_REQ_DISCARD_OUTPUT) &&
+      (r->c == r->a || r->c == r->b))
+    return fail(kInvalidArgument, "a device polymul's output may not overwrite an operand");
   int st = check_degree(r->log_n);
   if (st != kOk) return st;
   st = check_moduli(r->cm0, r->L);
   if (st != kOk) return st;
   if (r->flags & YELL_REQ_DEVICE) {
     const uintptr_t m = reinterpret_cast<uintptr_t>(r->a) | reinterpret_cast<uintptr_t>(r->b) |
-                        reinterpret_cast<uintptr_t>(r->c);
+                        reinterpret_cast<uintptr_t>(r->c);  // b may be null for an NTT
     if (m % 16) return fail(kInvalidArgument, "device operands must be 16-byte aligned");
   }
   auto req = std::make_shared<Request>();

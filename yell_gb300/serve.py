@@ -12,6 +12,8 @@ from . import _capi
 from ._capi import call, load
 
 YELL_REQ_HOST, YELL_REQ_DEVICE, YELL_REQ_DISCARD_OUTPUT = 0, 1, 2
+YELL_REQ_NTT_FORWARD, YELL_REQ_NTT_BACKWARD = 4, 8
+_OPS = {"polymul": 0, "forward": YELL_REQ_NTT_FORWARD, "backward": YELL_REQ_NTT_BACKWARD}
 
 
 class ServerConfig(ctypes.Structure):
@@ -90,16 +92,26 @@ class Server:
         self._keep = {}
         self._lock = threading.Lock()
 
-    def submit(self, a, b, c, log_n: int, L: int, cm0: int = 0, device: bool = False) -> int:
+    def submit(self, a, b, c, log_n: int, L: int, cm0: int = 0, device: bool = False,
+               op: str = "polymul") -> int:
         """a, b, c: (L, N) uint64 numpy arrays (host) or 64-bit CUDA tensors (device=True).
+        op: "polymul" (c = a * b), "forward" or "backward" (c = NTT of a; b unused, may be None).
         Host buffers must stay alive until wait() returns; the handle keeps them."""
-        req = Request(_addr(a), _addr(b), _addr(c), log_n, L, cm0,
-                      YELL_REQ_DEVICE if device else YELL_REQ_HOST)
+        flags = (YELL_REQ_DEVICE if device else YELL_REQ_HOST) | _OPS[op]
+        req = Request(_addr(a), _addr(b) if b is not None else None, _addr(c), log_n, L, cm0, flags)
         rid = ctypes.c_uint64()
         _capi.check(load().yell_server_submit(self._h, ctypes.byref(req), ctypes.byref(rid)),
                     "yell_server_submit")
         with self._lock:
             self._keep[rid.value] = (a, b, c)
+        return rid.value
+
+    def _submit_flags(self, a, b, c, log_n: int, L: int, cm0: int, flags: int) -> int:
+        """Submission with raw request flags (tests of the validation)."""
+        req = Request(_addr(a), _addr(b) if b is not None else None, _addr(c), log_n, L, cm0, flags)
+        rid = ctypes.c_uint64()
+        _capi.check(load().yell_server_submit(self._h, ctypes.byref(req), ctypes.byref(rid)),
+                    "yell_server_submit")
         return rid.value
 
     def wait(self, rid: int, timeout: float = 30.0) -> dict:
