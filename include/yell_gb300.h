@@ -102,6 +102,18 @@ int yell_ntt_forward(uint64_t* op, uint32_t log_n, uint32_t cm);
 int yell_ntt_forward_lazy(uint64_t* op, uint32_t log_n, uint32_t cm);
 int yell_ntt_backward(uint64_t* op, uint32_t log_n, uint32_t cm);
 
+/* ---- runtime-N free functions: negacylic_forward_lazy / negacylic_backward_lazy
+ * (include/yell/details/ntt.hpp:10-23, lib/ntt.cpp:89-210): in place on host
+ * memory, any power-of-two degree 4 .. 2^20, caller-supplied bit-reversed
+ * twiddles w and their Shoup companions wshoup (degree words each), p < 2^62.
+ * Forward: all log N CT stages, [0,4p) in and out.  Backward: the GS stages
+ * except the last layer (m = 1) for N >= 8, as the reference leaves it to its
+ * caller.  Drop-ins (one CTA per call), not the batched path. */
+int yell_negacyclic_forward_lazy(uint64_t* x, uint64_t degree, const uint64_t* w, const uint64_t* wshoup,
+                                 uint64_t p);
+int yell_negacyclic_backward_lazy(uint64_t* x, uint64_t degree, const uint64_t* w, const uint64_t* wshoup,
+                                  uint64_t p);
+
 /* ---- drop-in, one poly in host memory -----------------------------------
  * limbs = poly<N>::raw_data(): L separate arrays of N words, limb cm using
  * prime cm.  Replace poly<N>::forward / forward_lazy / backward

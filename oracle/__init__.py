@@ -62,6 +62,8 @@ def _bind(lib, prefix: str):
         "submod_n": (None, [_U64P, _U64P, _U64P, sz, u32]),
         "muladd_n": (None, [_U64P, _U64P, _U64P, sz, u32]),
         "mulmod_shoup_n": (None, [_U64P, _U64P, u64, sz, u32]),
+        "negacyclic_forward_lazy": (ctypes.c_int, [_U64P, u64, _U64P, _U64P, u64]),
+        "negacyclic_backward_lazy": (ctypes.c_int, [_U64P, u64, _U64P, _U64P, u64]),
     }
     if prefix == "orc_":
         sig.update({
@@ -193,6 +195,16 @@ class Oracle:
         d = np.zeros_like(a)
         self._f(name)(_ptr(d), _ptr(a), _ptr(b), a.size, cm)
         return d
+
+    def negacyclic_lazy(self, x, w, ws, p, inverse=False):
+        """The free functions with caller tables (details/ntt.hpp:10-23)."""
+        a = np.ascontiguousarray(x, dtype=np.uint64).copy()
+        w = np.ascontiguousarray(w, dtype=np.uint64)
+        ws = np.ascontiguousarray(ws, dtype=np.uint64)
+        fn = self._f("negacyclic_backward_lazy" if inverse else "negacyclic_forward_lazy")
+        if fn(_ptr(a), a.size, _ptr(w), _ptr(ws), p) != 0:
+            raise ValueError("negacyclic_lazy: bad arguments")
+        return a
 
     def mulmod(self, a, b, cm):
         return self._ew("mulmod_n", a, b, cm)

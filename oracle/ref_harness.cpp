@@ -167,6 +167,16 @@ void ref_mulmod_shoup_n(uint64_t* d, const uint64_t* a, uint64_t y, size_t n, ui
   for (size_t i = 0; i < n; ++i) d[i] = op(a[i], y, yp, cm);
 }
 
+int ref_negacyclic_forward_lazy(uint64_t* x, uint64_t degree, const uint64_t* w, const uint64_t* ws, uint64_t p) {
+  yell::negacylic_forward_lazy(x, (size_t)degree, w, ws, p);
+  return 0;
+}
+
+int ref_negacyclic_backward_lazy(uint64_t* x, uint64_t degree, const uint64_t* w, const uint64_t* ws, uint64_t p) {
+  yell::negacylic_backward_lazy(x, (size_t)degree, w, ws, p);
+  return 0;
+}
+
 double ref_polymul_batch(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_t pairs,
                          uint32_t L, uint32_t log_n, uint32_t threads) {
   double t = -1.0;

@@ -402,6 +402,20 @@ static void backward_lazy_loop(uint64_t* x, size_t n, const uint64_t* w, const u
   }
 }
 
+/* The loops with caller tables: negacylic_forward_lazy / negacylic_backward_lazy
+ * (include/yell/details/ntt.hpp:10-23). */
+int orc_negacyclic_forward_lazy(uint64_t* x, uint64_t degree, const uint64_t* w, const uint64_t* ws, uint64_t p) {
+  if (degree < 4 || (degree & (degree - 1))) return -1;
+  forward_lazy_loop(x, (size_t)degree, w, ws, p);
+  return 0;
+}
+
+int orc_negacyclic_backward_lazy(uint64_t* x, uint64_t degree, const uint64_t* w, const uint64_t* ws, uint64_t p) {
+  if (degree < 4 || (degree & (degree - 1))) return -1;
+  backward_lazy_loop(x, (size_t)degree, w, ws, p);
+  return 0;
+}
+
 /* details/ntt.hpp:194-203 */
 static void forward_lazy_t(uint64_t* x, const orc_tables* t) {
   forward_lazy_loop(x, (size_t)1 << t->log_n, t->phi, t->phi_s, t->p);

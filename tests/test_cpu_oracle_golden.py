@@ -118,3 +118,22 @@ def test_port_matches_reference_build(orc):
             assert np.array_equal(orc.forward(x, log_n, cm), ref.forward(x, log_n, cm))
             y = x % np.uint64(2 * p)
             assert np.array_equal(orc.backward(y, log_n, cm), ref.backward(y, log_n, cm))
+
+
+@pytest.mark.skipif(not __import__("oracle").ref_available(), reason="reference build not present")
+def test_free_functions_match_reference_build(orc):
+    """negacylic_forward_lazy / backward_lazy with caller tables: the port
+    against the reference's own compiled functions."""
+    import oracle
+
+    ref = oracle.Oracle("ref")
+    for log_n in (2, 3, 5, 8, 12, 15):
+        for cm in (0, 999):
+            p = orc.prime(cm)
+            t, _ = orc.tables(log_n, cm)
+            n = 1 << log_n
+            x4 = splitmix64(60 + log_n + cm, n) % np.uint64(4 * p)
+            x2 = splitmix64(70 + log_n + cm, n) % np.uint64(2 * p)
+            assert np.array_equal(orc.negacyclic_lazy(x4, t[0], t[1], p), ref.negacyclic_lazy(x4, t[0], t[1], p))
+            assert np.array_equal(orc.negacyclic_lazy(x2, t[2], t[3], p, True),
+                                  ref.negacyclic_lazy(x2, t[2], t[3], p, True))
