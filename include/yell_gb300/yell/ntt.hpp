@@ -48,6 +48,19 @@ inline int ntt_backward(uint64_t* op, uint32_t log_n, uint32_t cm) { return yell
 #endif
 }  // namespace detail
 
+#ifndef YELL_USE_32BITS_MODULI
+// include/yell/details/ntt.hpp:10-23: the runtime-N lazy loops with caller
+// tables (forward: [0,4p) in and out; backward: all layers but m = 1).
+inline void negacylic_forward_lazy(params::value_type* x, const size_t degree, const params::value_type* w,
+                                   const params::value_type* wshoup, const params::value_type p) {
+  check_status(yell_negacyclic_forward_lazy(x, degree, w, wshoup, p), "negacylic_forward_lazy");
+}
+inline void negacylic_backward_lazy(params::value_type* x, const size_t degree, const params::value_type* w,
+                                    const params::value_type* wshoup, const params::value_type p) {
+  check_status(yell_negacyclic_backward_lazy(x, degree, w, wshoup, p), "negacylic_backward_lazy");
+}
+#endif
+
 template <size_t degree_>
 class ntt {
   using T = params::value_type;
