@@ -455,6 +455,14 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
                "kind": kind,
                "sample": f"{reps} x the full batch ({pairs} pairs x {L} limbs), {total:.2f} s wall, "
                          f"~{total * threads:.0f} core-s"}
+        # one host core, on one pair of the batch repeated for about a second
+        total1, reps1 = 0.0, 0
+        while (reps1 < 2 or total1 < 1.0) and reps1 < 50:
+            secs, _ = cpu_reference_run(a[:1], b[:1], 1)
+            total1 += secs
+            reps1 += 1
+        cpu["single_core"] = {"value": reps1 * 3 * L / total1, "unit": UNIT, "cores": 1,
+                              "sample": f"{reps1} x 1 pair x {L} limbs, {total1:.2f} s"}
         if rows is not None:
             rows["cpu_baseline"] = rows_cpu_baseline(dc.cpu().numpy().view(np.uint64).reshape(pairs, L, N))
 

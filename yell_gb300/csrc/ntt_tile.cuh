@@ -37,17 +37,22 @@ __host__ __device__ constexpr uint32_t sidx(uint32_t v) { return v + ((v >> 4) <
 __host__ __device__ constexpr uint32_t tile_smem_words(uint32_t n) { return n + (n >> 3); }
 
 // Shared-memory layout per word type.  64-bit words: sidx (2 pad words per
-// 16).  32-bit words: 4 pad words per 16, which keeps every aligned group of
-// 4 words 16-byte aligned, so a thread that owns 16 consecutive words (the
-// bottom round) moves them as four conflict-free 16-byte accesses.
+// 16), an additive map: idx(base + off) = idx(base) + idx(off) for the
+// disjoint bit fields a round combines.  32-bit words: no padding; in each
+// 32-word row, 4-word groups are XOR-swizzled by the row index (bits 2..4 ^=
+// bits 5..7), a linear map over GF(2): idx(base ^ off) = idx(base) ^ idx(off),
+// every 4-word group stays contiguous and 16-byte aligned, and contiguous,
+// paired and 16-byte-per-lane accesses all spread over the 32 banks.
 template <class W> struct Smem;
 template <> struct Smem<uint64_t> {
+  static constexpr bool kXor = false;
   __host__ __device__ static constexpr uint32_t idx(uint32_t v) { return sidx(v); }
   __host__ __device__ static constexpr uint32_t words(uint32_t n) { return tile_smem_words(n); }
 };
 template <> struct Smem<uint32_t> {
-  __host__ __device__ static constexpr uint32_t idx(uint32_t v) { return v + ((v >> 4) << 2); }
-  __host__ __device__ static constexpr uint32_t words(uint32_t n) { return n + (n >> 2); }
+  static constexpr bool kXor = true;
+  __host__ __device__ static constexpr uint32_t idx(uint32_t v) { return v ^ (((v >> 5) & 7u) << 2); }
+  __host__ __device__ static constexpr uint32_t words(uint32_t n) { return n; }
 };
 
 template <int T_, int K_, int LB_, int LOGE_>
@@ -112,14 +117,32 @@ __device__ __forceinline__ void smem_load(W* x, const W* s, uint32_t base_v) {
   using PW = typename PairOf<W>::type;
   using SL = Smem<W>;
   if constexpr (kContig32<RG, W>) {
-    const W* sb = s + SL::idx(base_v);
+    // base_v has no bits below 2^R (R >= 4): idx(base_v + j) = idx(base_v) ^ j
+    const uint32_t ib = SL::idx(base_v);
 #pragma unroll
     for (int j = 0; j < (1 << R); j += 4) {
-      const uint4 v = *reinterpret_cast<const uint4*>(sb + j + ((j >> 4) << 2));
+      const uint4 v = *reinterpret_cast<const uint4*>(s + (ib ^ (uint32_t)j));
       x[j] = v.x;
       x[j + 1] = v.y;
       x[j + 2] = v.z;
       x[j + 3] = v.w;
+    }
+  } else if constexpr (SL::kXor) {
+    const uint32_t ib = SL::idx(base_v);
+    if constexpr (RG::PAIRS) {
+#pragma unroll
+      for (int m = 0; m < RG::E / 2; ++m)
+#pragma unroll
+        for (int j = 0; j < (1 << R); ++j) {
+          const PW v = *reinterpret_cast<const PW*>(s + (ib ^ SL::idx(RG::off(2 * m, j))));
+          x[((2 * m) << R) | j] = v.x;
+          x[((2 * m + 1) << R) | j] = v.y;
+        }
+    } else {
+#pragma unroll
+      for (int ex = 0; ex < RG::E; ++ex)
+#pragma unroll
+        for (int j = 0; j < (1 << R); ++j) x[(ex << R) | j] = s[ib ^ SL::idx(RG::off(ex, j))];
     }
   } else if constexpr (RG::PAIRS) {
     // base_v and the offsets occupy disjoint bits, so idx(base_v + off) = idx(base_v) + idx(off)
@@ -147,10 +170,25 @@ __device__ __forceinline__ void smem_store(const W* x, W* s, uint32_t base_v) {
   using PW = typename PairOf<W>::type;
   using SL = Smem<W>;
   if constexpr (kContig32<RG, W>) {
-    W* sb = s + SL::idx(base_v);
+    const uint32_t ib = SL::idx(base_v);
 #pragma unroll
     for (int j = 0; j < (1 << R); j += 4)
-      *reinterpret_cast<uint4*>(sb + j + ((j >> 4) << 2)) = make_uint4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+      *reinterpret_cast<uint4*>(s + (ib ^ (uint32_t)j)) = make_uint4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+  } else if constexpr (SL::kXor) {
+    const uint32_t ib = SL::idx(base_v);
+    if constexpr (RG::PAIRS) {
+#pragma unroll
+      for (int m = 0; m < RG::E / 2; ++m)
+#pragma unroll
+        for (int j = 0; j < (1 << R); ++j)
+          *reinterpret_cast<PW*>(s + (ib ^ SL::idx(RG::off(2 * m, j)))) =
+              PairOf<W>::make(x[((2 * m) << R) | j], x[((2 * m + 1) << R) | j]);
+    } else {
+#pragma unroll
+      for (int ex = 0; ex < RG::E; ++ex)
+#pragma unroll
+        for (int j = 0; j < (1 << R); ++j) s[ib ^ SL::idx(RG::off(ex, j))] = x[(ex << R) | j];
+    }
   } else if constexpr (RG::PAIRS) {
     W* sb = s + SL::idx(base_v);
 #pragma unroll
