@@ -62,9 +62,10 @@ __global__ void k_sample_uniform(uint64_t* out, uint32_t count, uint32_t L, uint
     const uint64_t p = __ldg(&mods[cm0 + l].p);
     const uint64_t mask = (2ull << (63 - __clzll(p))) - 1ull;  // 2^(floor(log2 p) + 1) - 1
     uint64_t v[4];
+    uint64_t z = seed + (k + 1) * 0x9E3779B97F4A7C15ull;  // counter of word k; + gamma per word
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      v[j] = rand_word(seed, k + j) & mask;
+    for (int j = 0; j < 4; ++j, z += 0x9E3779B97F4A7C15ull) {
+      v[j] = mix64(z) & mask;
       if (v[j] >= p) v[j] -= p;
     }
     reinterpret_cast<ulonglong2*>(out + k)[0] = make_ulonglong2(v[0], v[1]);
