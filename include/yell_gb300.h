@@ -160,9 +160,9 @@ int yell_dev_ntt_limbs(uint64_t* const* d_limbs, const uint32_t* d_cms, uint32_t
 int yell_dev_elementwise(int op, uint64_t* d_dst, const uint64_t* d_a, const uint64_t* d_b,
                          uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0, void* stream);
 /* Fused polymul of `pairs` pairs; d_c may not alias d_a or d_b.  Degrees
- * above the whole-limb path need scratch of yell_polymul_scratch_words()
- * words; pass NULL to use the library's per-device scratch (grown on demand,
- * serialised by a lock per device). */
+ * with a two-pass polymul (N >= 2^13) need scratch of
+ * yell_polymul_scratch_words() words; pass NULL to use the library's
+ * per-device scratch (grown on demand, serialised by a lock per device). */
 size_t yell_polymul_scratch_words(uint32_t pairs, uint32_t L, uint32_t log_n);
 int yell_dev_polymul(uint64_t* d_c, const uint64_t* d_a, const uint64_t* d_b, uint32_t pairs,
                      uint32_t L, uint32_t log_n, uint32_t cm0, uint64_t* d_scratch,
@@ -366,7 +366,8 @@ int yell_poly_to_bigint(uint64_t* out, const uint64_t* const* limbs, uint32_t L,
 /* ---- launch variants and the autotuner (no counterpart in the reference) --
  * Every degree has one or more launch variants that apply exactly the same
  * butterflies (same output words) with a different split of the work: limbs
- * per CTA for whole-limb degrees, column/row split k1 for 2^14 and up.
+ * per CTA for whole-limb degrees, column/row split k1 for 2^13 and up
+ * (2^13 has both kinds).
  * yell_autotune times the fused polymul of every variant of log_n on
  * synthetic data of the given size on the current device and selects the
  * fastest; with YELL_GB300_TUNE_FILE set the choice is saved there and
@@ -391,10 +392,11 @@ int yell_synchronize(void);
  * owned by a fixed budget or a pooled allocator that forbids allocations
  * outside the pool, or a latency-critical caller that cannot afford
  * cudaMalloc/cudaFree synchronising the device.  Same arguments and results
- * as yell_dev_polymul, but the scratch of the two-pass degrees (2^14 and up)
+ * as yell_dev_polymul, but the scratch of the two-pass degrees (2^13 and up)
  * is a fixed 16 MiB device array inside the library (2^21 words: at most
  * 2^21 / N limbs = pairs * L per call, e.g. 32 limbs at N = 2^16); larger
- * calls return YELL_ERR_INVALID_ARGUMENT.  The twiddle tables must already be
+ * calls return YELL_ERR_INVALID_ARGUMENT, except at 2^13, where they run the
+ * whole-limb polymul, which needs no scratch.  The twiddle tables must already be
  * resident (yell_init_ntt_tables_range), since building them allocates.
  * The first call on a device looks up the array's device address; make that
  * first call before any stream capture.  All calls share the one array: calls

@@ -72,7 +72,8 @@ def test_argument_errors_without_touching_cuda(ylib):
 
 
 def test_polymul_scratch_sizes(ylib):
-    assert y.polymul_scratch_words(16, 32, 13) == 0
+    assert y.polymul_scratch_words(16, 32, 12) == 0
+    assert y.polymul_scratch_words(16, 32, 13) == 16 * 32 << 13  # two-pass variants at 2^13
     assert y.polymul_scratch_words(16, 32, 16) == 16 * 32 << 16
     assert y.polymul_scratch_words(1, 1, 18) == 0
 

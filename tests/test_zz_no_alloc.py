@@ -65,3 +65,33 @@ def test_noalloc_rejects_oversize_and_missing_tables(cuda):
                                       15, 990, None)
     assert st == _capi.YELL_ERR_INVALID_ARGUMENT
     assert b"not resident" in lib.yell_last_error()
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+def test_noalloc_two_pass_degree_13_beyond_fixed_scratch(cuda, variant):
+    """2^13 with a two-pass variant selected: 160 pairs of L = 2 (320 limbs)
+    need more scratch than the fixed array holds (256 limbs), so the call runs
+    the scratch-free whole-limb polymul, and its words equal the two-pass
+    result of yell_dev_polymul."""
+    torch = cuda
+    lib = y.load()
+    log_n, pairs, L = 13, 160, 2
+    assert y.polymul_scratch_words(pairs, L, log_n) > 1 << 21
+    y.init_ntt_tables(log_n, L, 0)
+    ps = y.primes(L, 0)
+    a = uniform_polys(1300 + variant, pairs, L, log_n, ps)
+    b = uniform_polys(1350 + variant, pairs, L, log_n, ps)
+    da, db = _dev(torch, a), _dev(torch, b)
+    before = y.get_variant(log_n)
+    y.set_variant(log_n, variant)
+    try:
+        want = torch.empty(a.size, dtype=torch.int64, device="cuda")
+        y.dev_polymul(want, da, db, pairs, L, log_n, 0)
+        got = torch.full((a.size,), -1, dtype=torch.int64, device="cuda")
+        st = lib.yell_dev_polymul_noalloc(got.data_ptr(), da.data_ptr(), db.data_ptr(), pairs, L,
+                                          log_n, 0, None)
+        assert st == _capi.YELL_OK, lib.yell_last_error()
+        assert lib.yell_synchronize() == _capi.YELL_OK
+    finally:
+        y.set_variant(log_n, before)
+    assert torch.equal(got, want)

@@ -46,6 +46,9 @@ cudaError_t launch_elementwise(EwOp op, const LimbSet& dst, const ConstLimbSet& 
                                cudaStream_t st);
 
 size_t polymul_scratch_words(uint32_t count, uint32_t log_n, const NttShape& shape);
+// True when the degree also has a polymul that needs no scratch
+// (launch_polymul falls back to it when given none).
+bool polymul_scratch_optional(uint32_t log_n);
 
 // Sets the dynamic shared-memory limits of every kernel on the current
 // device (called once per device, outside any stream capture).

@@ -7,7 +7,9 @@
 // outside the pool), and latency-critical callers, since cudaMalloc/cudaFree
 // can synchronise the whole device and stall every other stream.  For them
 // the scratch of the two-pass polymul (one operand's worth of words at
-// N >= 2^14) lives in the file-scope array below instead of in an allocation.
+// N >= 2^13) lives in the file-scope array below instead of in an allocation.
+// At 2^13, where a whole-limb polymul also exists, a batch too large for the
+// array runs whole-limb instead.
 #include <mutex>
 #include <string>
 
@@ -20,7 +22,7 @@ using namespace yell_gb300;
 namespace {
 
 // 2^21 words = 16 MiB: scratch for up to 32 limbs at N = 2^16 (e.g. one
-// pair of 32-limb polys), 16 at 2^17, 64 at 2^15, 128 at 2^14.  Every GPU
+// pair of 32-limb polys), 16 at 2^17, 64 at 2^15, 128 at 2^14, 256 at 2^13.  Every GPU
 // that loads this module holds the array until the process exits.
 constexpr size_t kNoAllocScratchWords = size_t(1) << 21;
 static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocScratchWords];
@@ -61,7 +63,8 @@ extern "C" int yell_dev_polymul_noalloc(uint64_t* d_c, const uint64_t* d_a, cons
   const size_t count = (size_t)pairs * L;
   DeviceContext* ctx = DeviceContext::current(&st);
   if (!ctx) return st;
-  const size_t need = polymul_scratch_words((uint32_t)count, log_n, ctx->shape);
+  size_t need = polymul_scratch_words((uint32_t)count, log_n, ctx->shape);
+  if (need > kNoAllocScratchWords && polymul_scratch_optional(log_n)) need = 0;  // scratch-free variant
   if (need > kNoAllocScratchWords)
     return fail(kInvalidArgument,
                 "yell_dev_polymul_noalloc: " + std::to_string(count) + " limbs of degree 2^" +

@@ -138,8 +138,21 @@ cudaError_t init_kernel_attributes() {
 uint32_t ntt_launch_count(uint32_t log_n, const NttShape&) { return pick(log_n).ntt_launches; }
 uint32_t polymul_launch_count(uint32_t log_n, const NttShape&) { return pick(log_n).polymul_launches; }
 
+// The words a polymul of this degree may need, whichever variant is selected
+// (the selection can change between the caller's allocation and its call).
 size_t polymul_scratch_words(uint32_t count, uint32_t log_n, const NttShape&) {
-  return log_n <= 13 ? 0 : ((size_t)count << log_n);
+  if (log_n < kMinLogN || log_n > kMaxLogN) return 0;
+  for (const Variant& v : variants_of(log_n))
+    if (v.polymul_scratch) return (size_t)count << log_n;
+  return 0;
+}
+
+// True when some variant of this degree runs its polymul without scratch.
+bool polymul_scratch_optional(uint32_t log_n) {
+  if (log_n < kMinLogN || log_n > kMaxLogN) return true;
+  for (const Variant& v : variants_of(log_n))
+    if (!v.polymul_scratch) return true;
+  return false;
 }
 
 cudaError_t launch_ntt(const LimbSet& ls, uint32_t log_n, const DevMod* mods, NttDir dir,
@@ -154,8 +167,18 @@ cudaError_t launch_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstL
                            const NttShape&, cudaStream_t st, uint64_t* const* scratch_ptrs) {
   if (c.count == 0) return cudaSuccess;
   if (log_n < kMinLogN || log_n > kMaxLogN) return cudaErrorInvalidValue;
-  if (log_n > 13 && scratch == nullptr && scratch_ptrs == nullptr) return cudaErrorInvalidValue;
-  return pick(log_n).polymul(c, a, b, mods, scratch, scratch_ptrs, st);
+  const Variant* v = &pick(log_n);
+  if (v->polymul_scratch && scratch == nullptr && scratch_ptrs == nullptr) {
+    // Without scratch, the first (selection order) variant that needs none.
+    v = nullptr;
+    for (const Variant& w : variants_of(log_n))
+      if (!w.polymul_scratch) {
+        v = &w;
+        break;
+      }
+    if (!v) return cudaErrorInvalidValue;
+  }
+  return v->polymul(c, a, b, mods, scratch, scratch_ptrs, st);
 }
 
 cudaError_t launch_elementwise(EwOp op, const LimbSet& dst, const ConstLimbSet& a,

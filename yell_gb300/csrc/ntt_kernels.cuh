@@ -742,6 +742,7 @@ Variant two_pass_variant() {
   v.set_attrs = &set_attrs_two_pass<LOGN, K1>;
   v.ntt_launches = 2;
   v.polymul_launches = 3;
+  v.polymul_scratch = true;
   return v;
 }
 

@@ -21,11 +21,12 @@ struct Variant {
   cudaError_t (*set_attrs)() = nullptr;
   uint32_t ntt_launches = 0;
   uint32_t polymul_launches = 0;
+  bool polymul_scratch = false;  // the polymul needs one operand's worth of scratch words
 };
 
 // Registration, one per translation unit (by_degree has kMaxLogN + 1 entries).
 void add_whole_variants_small(std::vector<Variant>* by_degree);  // 2^3 .. 2^8
-void add_whole_variants_large(std::vector<Variant>* by_degree);  // 2^9 .. 2^13
+void add_whole_variants_large(std::vector<Variant>* by_degree);  // 2^9 .. 2^13 (and two-pass 2^13)
 void add_two_pass_variants_a(std::vector<Variant>* by_degree);   // 2^14, 2^15
 void add_two_pass_variants_b(std::vector<Variant>* by_degree);   // 2^16, 2^17
 

@@ -115,7 +115,7 @@ size_t footprint_of(const yell_polymul_request& r, size_t words, uint32_t log_n)
   }
   if (!device) bytes += 2 * RangeAllocator::round(limb_bytes);  // a, b
   if (!device || (r.flags & YELL_REQ_DISCARD_OUTPUT)) bytes += RangeAllocator::round(limb_bytes);  // c
-  if (log_n > 13) bytes += RangeAllocator::round(limb_bytes);  // two-pass scratch
+  if (polymul_scratch_words(1, log_n, NttShape{})) bytes += RangeAllocator::round(limb_bytes);  // two-pass scratch
   return bytes;
 }
 
@@ -244,7 +244,8 @@ bool yell_server::admit_into(Slot& s, std::vector<ReqPtr>* batch) {
     } else {
       r->d_c = r->req.c;
     }
-    r->d_s = (r->req.log_n > 13 && !is_ntt(r->req)) ? reinterpret_cast<uint64_t*>(p) : nullptr;
+    r->d_s = (polymul_scratch_words(1, r->req.log_n, NttShape{}) && !is_ntt(r->req)) ? reinterpret_cast<uint64_t*>(p)
+                                                                                  : nullptr;
     r->t_start = t;
     batch->push_back(r);
   }
