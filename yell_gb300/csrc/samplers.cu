@@ -51,57 +51,68 @@ __host__ __device__ __forceinline__ uint64_t rand_word(uint64_t seed, uint64_t k
 constexpr uint64_t kSeedPositions = 0x5ca1ab1e0ddba11ull;
 constexpr uint64_t kSeedSigns = 0x0b5e55edc0ffee5ull;
 
-// Four consecutive words per thread (one limb row, since N >= 8): one
-// modulus lookup and two 16-byte stores per four words.
+// A warp writes 128 consecutive words per step as two 512-byte stores: lane j
+// holds words 2j, 2j + 1 and 64 + 2j, 65 + 2j of the chunk.  The total is a
+// multiple of 8 words (N >= 8), so a pair never straddles two limbs.
 __global__ void k_sample_uniform(uint64_t* out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
                                  const DevMod* __restrict__ mods, uint64_t seed) {
-  const size_t quads = (((size_t)count * L) << log_n) >> 2;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < quads; t += (size_t)gridDim.x * blockDim.x) {
-    const size_t k = t << 2;
-    const uint32_t l = (uint32_t)(k >> log_n) % L;
-    const uint64_t p = __ldg(&mods[cm0 + l].p);
-    const uint64_t mask = (2ull << (63 - __clzll(p))) - 1ull;  // 2^(floor(log2 p) + 1) - 1
-    uint64_t v[4];
-    uint64_t z = seed + (k + 1) * 0x9E3779B97F4A7C15ull;  // counter of word k; + gamma per word
+  const size_t words = ((size_t)count * L) << log_n;
+  const uint32_t lane = threadIdx.x & 31u;
+  const size_t warp = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
+  const size_t warps = ((size_t)gridDim.x * blockDim.x) >> 5;
+  for (size_t c = warp << 7; c < words; c += warps << 7) {
 #pragma unroll
-    for (int j = 0; j < 4; ++j, z += 0x9E3779B97F4A7C15ull) {
-      v[j] = mix64(z) & mask;
-      if (v[j] >= p) v[j] -= p;
+    for (int h = 0; h < 2; ++h) {
+      const size_t k = c + ((size_t)h << 6) + (lane << 1);
+      if (k >= words) break;
+      const uint32_t l = (uint32_t)(k >> log_n) % L;
+      const uint64_t p = __ldg(&mods[cm0 + l].p);
+      const uint64_t mask = (2ull << (63 - __clzll(p))) - 1ull;  // 2^(floor(log2 p) + 1) - 1
+      const uint64_t z = seed + (k + 1) * 0x9E3779B97F4A7C15ull;  // counter of word k; + gamma per word
+      uint64_t v0 = mix64(z) & mask, v1 = mix64(z + 0x9E3779B97F4A7C15ull) & mask;
+      if (v0 >= p) v0 -= p;
+      if (v1 >= p) v1 -= p;
+      *reinterpret_cast<ulonglong2*>(out + k) = make_ulonglong2(v0, v1);
     }
-    reinterpret_cast<ulonglong2*>(out + k)[0] = make_ulonglong2(v[0], v[1]);
-    reinterpret_cast<ulonglong2*>(out + k)[1] = make_ulonglong2(v[2], v[3]);
   }
 }
 
-// mode 0: ZO with threshold rho; mode 1: gaussian through the cumulative table.
+// mode 0: ZO with threshold rho; mode 1: gaussian through the cumulative
+// table.  Two adjacent coefficients per thread (N >= 8 is even), so every
+// limb row is written with 16-byte stores.
+__device__ __forceinline__ int64_t shared_int(uint64_t r, int mode, uint32_t rho, const uint64_t* __restrict__ cdt,
+                                              uint32_t cdt_len, int32_t tail, uint64_t amplifier) {
+  if (mode == 0) {
+    const uint32_t byte = (uint32_t)(r & 0xFF);
+    return byte <= rho ? ((byte & 2) ? -1 : 1) : 0;
+  }
+  // first index with r < cdt[idx] (upper bound), clamped to the table
+  uint32_t lo = 0, hi = cdt_len;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (r < __ldg(&cdt[mid])) hi = mid;
+    else lo = mid + 1;
+  }
+  if (lo >= cdt_len) lo = cdt_len - 1;
+  return ((int64_t)lo - tail) * (int64_t)amplifier;
+}
+
 __global__ void k_sample_shared_int(uint64_t* out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
                                     const DevMod* __restrict__ mods, uint64_t seed, int mode, uint32_t rho,
                                     const uint64_t* __restrict__ cdt, uint32_t cdt_len, int32_t tail,
                                     uint64_t amplifier) {
-  const size_t coeffs = (size_t)count << log_n;
+  const size_t pairs = ((size_t)count << log_n) >> 1;
   const uint32_t nmask = (1u << log_n) - 1u;
-  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < coeffs; k += (size_t)gridDim.x * blockDim.x) {
-    const uint64_t r = rand_word(seed, k);
-    int64_t e;
-    if (mode == 0) {
-      const uint32_t byte = (uint32_t)(r & 0xFF);
-      e = byte <= rho ? ((byte & 2) ? -1 : 1) : 0;
-    } else {
-      // first index with r < cdt[idx] (upper bound), clamped to the table
-      uint32_t lo = 0, hi = cdt_len;
-      while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (r < __ldg(&cdt[mid])) hi = mid;
-        else lo = mid + 1;
-      }
-      if (lo >= cdt_len) lo = cdt_len - 1;
-      e = ((int64_t)lo - tail) * (int64_t)amplifier;
-    }
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < pairs; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = t << 1;
+    const int64_t e0 = shared_int(rand_word(seed, k), mode, rho, cdt, cdt_len, tail, amplifier);
+    const int64_t e1 = shared_int(rand_word(seed, k + 1), mode, rho, cdt, cdt_len, tail, amplifier);
     const size_t poly = k >> log_n;
     const uint32_t i = (uint32_t)k & nmask;
     for (uint32_t l = 0; l < L; ++l) {
       const uint64_t p = __ldg(&mods[cm0 + l].p);
-      out[(((poly * L) + l) << log_n) + i] = e < 0 ? p + (uint64_t)e : (uint64_t)e;
+      *reinterpret_cast<ulonglong2*>(out + (((poly * L) + l) << log_n) + i) =
+          make_ulonglong2(e0 < 0 ? p + (uint64_t)e0 : (uint64_t)e0, e1 < 0 ? p + (uint64_t)e1 : (uint64_t)e1);
     }
   }
 }
@@ -130,16 +141,21 @@ __host__ __device__ __forceinline__ uint32_t feistel(uint32_t x, uint32_t bits, 
 
 __global__ void k_sample_hwt(uint64_t* out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
                              const DevMod* __restrict__ mods, uint64_t seed, uint32_t h) {
-  const size_t coeffs = (size_t)count << log_n;
+  // two adjacent coefficients per thread: 16-byte stores per limb row
+  const size_t pairs = ((size_t)count << log_n) >> 1;
   const uint32_t nmask = (1u << log_n) - 1u;
-  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < coeffs; k += (size_t)gridDim.x * blockDim.x) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < pairs; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = t << 1;
     const size_t poly = k >> log_n;
     const uint32_t i = (uint32_t)k & nmask;
-    const bool take = feistel(i, log_n, rand_word(seed ^ kSeedPositions, poly)) < h;
-    const bool plus = (rand_word(seed ^ kSeedSigns, k) & 2) != 0;
+    const uint64_t key = rand_word(seed ^ kSeedPositions, poly);
+    const bool take0 = feistel(i, log_n, key) < h, take1 = feistel(i + 1, log_n, key) < h;
+    const bool plus0 = (rand_word(seed ^ kSeedSigns, k) & 2) != 0;
+    const bool plus1 = (rand_word(seed ^ kSeedSigns, k + 1) & 2) != 0;
     for (uint32_t l = 0; l < L; ++l) {
       const uint64_t p = __ldg(&mods[cm0 + l].p);
-      out[(((poly * L) + l) << log_n) + i] = take ? (plus ? 1ull : p - 1) : 0ull;
+      *reinterpret_cast<ulonglong2*>(out + (((poly * L) + l) << log_n) + i) =
+          make_ulonglong2(take0 ? (plus0 ? 1ull : p - 1) : 0ull, take1 ? (plus1 ? 1ull : p - 1) : 0ull);
     }
   }
 }
@@ -245,8 +261,8 @@ int yell_dev_sample_zo(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log
   int st = prepare(d_out, count, L, log_n, cm0, stream, &a);
   if (st != kOk) return st;
   LaunchScope ps("sample_zo", a.st);
-  k_sample_shared_int<<<grid_for((size_t)count << log_n), 256, 0, a.st>>>(d_out, count, L, log_n, cm0, a.mods,
-                                                                         seed, 0, rho, nullptr, 0, 0, 1);
+  k_sample_shared_int<<<grid_for(((size_t)count << log_n) >> 1), 256, 0, a.st>>>(
+      d_out, count, L, log_n, cm0, a.mods, seed, 0, rho, nullptr, 0, 0, 1);
   g_kernel_launches += 1;
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? kOk : fail_cuda(e, "sample_zo");
@@ -259,7 +275,8 @@ int yell_dev_sample_hwt(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t lo
   int st = prepare(d_out, count, L, log_n, cm0, stream, &a);
   if (st != kOk) return st;
   LaunchScope ps("sample_hwt", a.st);
-  k_sample_hwt<<<grid_for((size_t)count << log_n), 256, 0, a.st>>>(d_out, count, L, log_n, cm0, a.mods, seed, h);
+  k_sample_hwt<<<grid_for(((size_t)count << log_n) >> 1), 256, 0, a.st>>>(d_out, count, L, log_n, cm0, a.mods,
+                                                                          seed, h);
   g_kernel_launches += 1;
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? kOk : fail_cuda(e, "sample_hwt");
@@ -279,7 +296,7 @@ int yell_dev_sample_gaussian(uint64_t* d_out, uint32_t count, uint32_t L, uint32
   st = gaussian_table(a.ctx->device(), sigma, tail, &cdt, &len);
   if (st != kOk) return st;
   LaunchScope ps("sample_gaussian", a.st);
-  k_sample_shared_int<<<grid_for((size_t)count << log_n), 256, 0, a.st>>>(
+  k_sample_shared_int<<<grid_for(((size_t)count << log_n) >> 1), 256, 0, a.st>>>(
       d_out, count, L, log_n, cm0, a.mods, seed, 1, 0, cdt, len, (int32_t)tail, amplifier);
   g_kernel_launches += 1;
   const cudaError_t e = cudaGetLastError();
