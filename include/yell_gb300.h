@@ -15,7 +15,7 @@
  * (forward) or left in [0, 4p) (forward_lazy, the same lazy words as the
  * reference); backward outputs in natural order in [0, p).
  *
- * Degrees: N = 2^log_n with log_n in [3, 17] (yell_min_log_degree() ..
+ * Degrees: N = 2^log_n with log_n in [3, 20] (yell_min_log_degree() ..
  * yell_max_log_degree()).  The reference's inverse at N = 4 applies its last
  * layer twice (lib/ntt.cpp:174-187 followed by
  * include/yell/details/ntt.hpp:220-228) and is not an inverse, so 4 is
@@ -46,7 +46,7 @@ extern "C" {
 enum yell_status_code {
   YELL_OK = 0,
   YELL_ERR_INVALID_ARGUMENT = 1,   /* null pointer, zero count, bad enum */
-  YELL_ERR_UNSUPPORTED_DEGREE = 2, /* log_n outside [3, 17] */
+  YELL_ERR_UNSUPPORTED_DEGREE = 2, /* log_n outside [3, 20] */
   YELL_ERR_INVALID_MODULUS = 3,    /* cm >= yell_max_moduli() */
   YELL_ERR_CUDA = 4,               /* a CUDA call failed; see yell_last_error() */
   YELL_ERR_OUT_OF_MEMORY = 5,      /* device or pinned allocation refused */

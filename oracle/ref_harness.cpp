@@ -10,7 +10,7 @@
 // <gmp.h> and an MPFR sampler), so the element-wise entry points below call
 // the yell::ops functors exactly as the YELL_BINARY_OPERATOR loop does
 // (include/yell/ops.hpp:7-41).  N is a template parameter in the reference
-// (include/yell/ntt.hpp:6-7); the switch below instantiates 2^2 .. 2^17.
+// (include/yell/ntt.hpp:6-7); the switch below instantiates 2^2 .. 2^20.
 #include <cstdint>
 #include <cstring>
 #include <chrono>
@@ -67,6 +67,9 @@ void run_one(op_kind k, uint64_t* x, size_t cm) {
     case 15: CALL(32768); break;               \
     case 16: CALL(65536); break;               \
     case 17: CALL(131072); break;              \
+    case 18: CALL(262144); break;              \
+    case 19: CALL(524288); break;              \
+    case 20: CALL(1048576); break;             \
     default: return -1;                        \
   }
 

@@ -4,6 +4,7 @@
 // the add_product_of / forward_lazy path of example.cpp:36-57.  Prints "OK".
 #include <cstdio>
 #include <cstdint>
+#include <vector>
 #include "yell/poly.hpp"
 
 constexpr size_t Deg = 1024;
@@ -62,6 +63,19 @@ int main() {
     return 1;
   }
   if (mm(3, 5, 0) != 15) return 1;
+  // the largest degree of the reference (params::kMaxPolyDegree = 2^20): round trip
+  constexpr size_t Big = yell::params::kMaxPolyDegree;
+  yell::ntt<Big>::init_table(5);
+  std::vector<uint64_t> x(Big), x0;
+  uint64_t seed = 13;
+  for (auto& v : x) v = splitmix64(seed) % yell::params::P[5];
+  x0 = x;
+  yell::ntt<Big>::forward(x.data(), 5);
+  yell::ntt<Big>::backward(x.data(), 5);
+  if (x != x0) {
+    std::printf("MISMATCH round trip at N = 2^20\n");
+    return 1;
+  }
   std::printf("OK\n");
   return 0;
 }

@@ -71,7 +71,7 @@ def main() -> None:
             out[key + "_bwd"] = ref.backward(x2, log_n, cm)
 
     # digests of larger transforms: (log_n, cm, op, seed, bound multiple)
-    for log_n, cm in ((13, 2), (14, 1), (15, 7), (16, 31), (17, 3)):
+    for log_n, cm in ((13, 2), (14, 1), (15, 7), (16, 31), (17, 3), (18, 4), (19, 9), (20, 0)):
         p = int(out["P"][cm])
         x4 = seeded(3000 + log_n, 1 << log_n, 4 * p)
         x2 = seeded(4000 + log_n, 1 << log_n, 2 * p)

@@ -32,7 +32,7 @@ def test_signature_table_covers_header():
 def test_abi_and_ranges(ylib):
     assert ylib.yell_abi_version() == 1
     assert y.max_moduli() == 1000
-    assert (y.min_log_degree(), y.max_log_degree()) == (3, 17)
+    assert (y.min_log_degree(), y.max_log_degree()) == (3, 20)
     assert ylib.yell_prime(1000) == 0
 
 
@@ -58,7 +58,7 @@ def test_argument_errors_without_touching_cuda(ylib):
     buf = np.zeros(16, np.uint64)
     addr = buf.ctypes.data
     assert ylib.yell_ntt_forward(addr, 2, 0) == _capi.YELL_ERR_UNSUPPORTED_DEGREE
-    assert ylib.yell_ntt_forward(addr, 18, 0) == _capi.YELL_ERR_UNSUPPORTED_DEGREE
+    assert ylib.yell_ntt_forward(addr, 21, 0) == _capi.YELL_ERR_UNSUPPORTED_DEGREE
     assert ylib.yell_ntt_backward(addr, 4, 1000) == _capi.YELL_ERR_INVALID_MODULUS
     assert ylib.yell_ntt_forward(None, 4, 0) == _capi.YELL_ERR_INVALID_ARGUMENT
     assert ylib.yell_dev_ntt(addr + 8, 1, 1, 4, 0, 0, None) == _capi.YELL_ERR_INVALID_ARGUMENT
@@ -75,7 +75,7 @@ def test_polymul_scratch_sizes(ylib):
     assert y.polymul_scratch_words(16, 32, 12) == 0
     assert y.polymul_scratch_words(16, 32, 13) == 16 * 32 << 13  # two-pass variants at 2^13
     assert y.polymul_scratch_words(16, 32, 16) == 16 * 32 << 16
-    assert y.polymul_scratch_words(1, 1, 18) == 0
+    assert y.polymul_scratch_words(1, 1, 21) == 0
 
 
 def test_no_kernel_ran_on_cpu(ylib):

@@ -31,7 +31,7 @@ def _run(torch, mix, ops, cm0s, fn):
 
 
 def test_every_degree_matches_oracle(cuda, orc):
-    mix = [(d, 1 + d % 3) for d in range(3, 18)] + [(13, 4), (10, 2), (16, 1), (3, 5)]
+    mix = [(d, 1 + d % 3) for d in range(3, 21)] + [(13, 4), (10, 2), (16, 1), (3, 5)]
     cm0s = [i % 5 for i in range(len(mix))]
     ops = []
     for i, ((log_n, L), cm0) in enumerate(zip(mix, cm0s)):

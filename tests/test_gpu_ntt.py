@@ -13,7 +13,7 @@ from yell_gb300.inputs import splitmix64, uniform_polys
 
 pytestmark = pytest.mark.gpu
 
-ALL_LOG_N = list(range(3, 18))
+ALL_LOG_N = list(range(3, 21))  # the reference's degrees 2^3 .. kMaxPolyDegree = 2^20
 
 
 def _uniform(seed, log_n, cm, scale=1):
@@ -50,7 +50,7 @@ def test_backward_per_limb(cuda, orc, log_n, cm):
     assert int(got.max()) < y.prime(cm)
 
 
-@pytest.mark.parametrize("log_n", [3, 8, 13, 14, 16, 17])
+@pytest.mark.parametrize("log_n", [3, 8, 13, 14, 16, 17, 18, 20])
 def test_round_trip_identity(cuda, log_n):
     x = _uniform(400 + log_n, log_n, 3)
     f = y.ntt_forward(x, log_n, 3)
@@ -73,14 +73,14 @@ def test_edge_values(cuda, orc, log_n):
 
 
 def test_unsupported_degree_is_an_error(cuda):
-    for log_n in (0, 1, 2, 18):
+    for log_n in (0, 1, 2, 21):
         with pytest.raises(y.YellError) as ei:
             y.ntt_forward(np.zeros(1 << log_n, np.uint64), log_n, 0)
         assert ei.value.status == 2
 
 
 @pytest.mark.parametrize("log_n,count,L", [(3, 5, 3), (10, 3, 4), (12, 2, 3), (13, 3, 2),
-                                           (14, 2, 3), (16, 2, 2), (17, 1, 2)])
+                                           (14, 2, 3), (16, 2, 2), (17, 1, 2), (19, 1, 2), (20, 2, 1)])
 @pytest.mark.parametrize("direction", [0, 1, 2])
 def test_device_batch(cuda, orc, log_n, count, L, direction):
     torch = cuda

@@ -33,7 +33,7 @@ def test_config1_plain_method(cuda, orc):
     assert np.array_equal(got, orc.polymul(a[0], b[0], log_n, 0)[0])
 
 
-@pytest.mark.parametrize("log_n", list(range(3, 18)))
+@pytest.mark.parametrize("log_n", list(range(3, 21)))
 def test_polymul_all_degrees(cuda, orc, log_n):
     torch = cuda
     pairs, L, cm0 = 2, 3, 1

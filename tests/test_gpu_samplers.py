@@ -92,4 +92,4 @@ def test_sampler_errors(cuda):
     with pytest.raises(y.YellError):
         y.sample_gaussian(t, 1, 1, 10, tail=19, amplifier=1 << 60)
     with pytest.raises(y.YellError):
-        y.sample_uniform(t, 1, 1, 18)
+        y.sample_uniform(t, 1, 1, 21)  # above the largest degree: rejected before any launch

@@ -13,7 +13,7 @@ def _dev(torch, a):
     return torch.from_numpy(np.ascontiguousarray(a).view(np.int64).copy()).cuda()
 
 
-@pytest.mark.parametrize("log_n", list(range(3, 18)))
+@pytest.mark.parametrize("log_n", list(range(3, 21)))
 def test_all_variants_match_oracle(cuda, orc, log_n):
     torch = cuda
     names = y.variants(log_n)

@@ -90,6 +90,9 @@ __device__ __forceinline__ void dispatch(uint32_t kind, const QueueBucket& B, ui
     case 15: run_item<15>(kind, B, bid); break;
     case 16: run_item<16>(kind, B, bid); break;
     case 17: run_item<17>(kind, B, bid); break;
+    case 18: run_item<18>(kind, B, bid); break;
+    case 19: run_item<19>(kind, B, bid); break;
+    case 20: run_item<20>(kind, B, bid); break;
     default: break;
   }
 }

@@ -9,7 +9,7 @@
 namespace yell_gb300 {
 
 // Work item kinds.  Whole-limb degrees (N <= 2^12) are one item per CTA tile;
-// degrees 2^13 .. 2^17 run the two-pass polymul as three items per tile: the
+// degrees 2^13 .. 2^20 run the two-pass polymul as three items per tile: the
 // forward column pass of a and b, the fused row step, the inverse column pass.
 enum QueueItemKind : uint32_t { kItemWhole = 0, kItemColFwd = 1, kItemRows = 2, kItemColInv = 3 };
 
@@ -44,7 +44,7 @@ struct QueueLaunch {
 
 // Degrees served by the queue kernel and the column stages of its two-pass
 // degrees.
-constexpr uint32_t kQueueMinLogN = 3, kQueueMaxLogN = 17, kQueueFirstTwoPass = 13;
+constexpr uint32_t kQueueMinLogN = 3, kQueueMaxLogN = 20, kQueueFirstTwoPass = 13;
 constexpr uint32_t kQueueTileLog = 12;  // tile words of every item (2^11 at N = 8)
 uint32_t queue_k1(uint32_t log_n);
 

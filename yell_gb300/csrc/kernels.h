@@ -18,7 +18,7 @@ struct NttShape {
 };
 
 constexpr uint32_t kMinLogN = 3;
-constexpr uint32_t kMaxLogN = 17;
+constexpr uint32_t kMaxLogN = 20;
 
 uint32_t default_k1(uint32_t log_n);
 

@@ -22,7 +22,7 @@ using namespace yell_gb300;
 namespace {
 
 // 2^21 words = 16 MiB: scratch for up to 32 limbs at N = 2^16 (e.g. one
-// pair of 32-limb polys), 16 at 2^17, 64 at 2^15, 128 at 2^14, 256 at 2^13.  Every GPU
+// pair of 32-limb polys), 16 at 2^17, 2 at 2^20, 64 at 2^15, 128 at 2^14, 256 at 2^13.  Every GPU
 // that loads this module holds the array until the process exits.
 constexpr size_t kNoAllocScratchWords = size_t(1) << 21;
 static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocScratchWords];
