@@ -6,12 +6,15 @@
 // ZO_dist); the reference's gaussian<> wraps an MPFR-built FastGaussianNoise,
 // so the facade names the distribution instead (gaussian_dist).
 #pragma once
+#include <array>
 #include <atomic>
 #include <cassert>
 #include <cstdlib>
 #include <random>
 #include <cstring>
+#include <ostream>
 #include <stdexcept>
+#include <string>
 #include <utility>
 #include <vector>
 #include "yell/ntt.hpp"
@@ -184,6 +187,21 @@ class poly {
                  "add_product_of");
     return *this;
   }
+#ifndef YELL_USE_32BITS_MODULI
+  // details/poly.hpp:135-149: a * s computed as a * r + a * (s - r) with a
+  // fresh uniform r, so s never meets a in one product (NTT domain).
+  poly& mul_sensitive_poly(const poly& sensitive_poly) {
+    assert(nmoduli == sensitive_poly.nmoduli);
+    poly r0(nmoduli, uniform{});
+    poly r1 = sensitive_poly - r0;
+    r1 *= *this;
+    *this *= r0;
+    *this += r1;
+    r0.clear();
+    r1.clear();
+    return *this;
+  }
+#endif
   // details/poly.hpp:151-157
   void negate() { check_status(detail::poly_negate(_data.data(), (uint32_t)nmoduli, log_n), "negate"); }
 
@@ -237,7 +255,38 @@ class poly {
     for (size_t cm = 0; cm < nmoduli; ++cm) std::memset(_data[cm], 0, degree_ * sizeof(value_type));
   }
   size_t moduli_count() const { return nmoduli; }
+  // details/poly.hpp:357-368: every word below its modulus (debug builds only).
+  void check_vaild_range() const {
+#ifndef NDEBUG
+    for (size_t cm = 0; cm < nmoduli; ++cm)
+      for (size_t i = 0; i < degree_; ++i) assert(_data[cm][i] < params::P[cm]);
+#endif
+  }
 };
+
+// details/poly.hpp:336-354: {{w0ULL, w1ULL, ...}\n{...}}, one brace group per limb.
+template <size_t Degree>
+std::ostream& operator<<(std::ostream& os, poly<Degree> const& p) {
+  os << "{";
+  for (size_t cm = 0; cm < p.moduli_count(); ++cm) {
+    os << "{";
+    for (size_t i = 0; i < Degree; ++i) os << p(cm, i) << "ULL" << (i + 1 < Degree ? ", " : "}");
+    if (cm + 1 < p.moduli_count()) os << "\n";
+  }
+  return os << "}";
+}
+
+// poly.hpp:144-156: limb cm viewed as a std::array of N words.
+template <typename value_type, size_t degree>
+struct ArrayPointer {
+  using T = std::array<value_type, degree>*;
+  using cT = const T;
+};
+template <size_t degree>
+typename ArrayPointer<params::value_type, degree>::T recast_as_array(poly<degree>& op, size_t cm) {
+  assert(cm < op.moduli_count());
+  return reinterpret_cast<typename ArrayPointer<params::value_type, degree>::T>(op.ptr_at(cm));
+}
 
 namespace detail {
 template <size_t N, int (*FN)(W* const*, const W* const*, const W* const*, uint32_t, uint32_t)>

@@ -2,9 +2,12 @@
 // set(hwt_dist), set(ZO_dist), gmp::poly2mpz) compiled against the
 // yell_gb300 facade and run on the GPU.  Checks ranges, Hamming weight, the
 // same small integer in every limb, and that each lifted coefficient is
-// congruent to its residues.  Prints "OK".
+// congruent to its residues; then mul_sensitive_poly against the plain
+// product, the stream format and recast_as_array.  Prints "OK".
 #include <cstdio>
 #include <cstdint>
+#include <sstream>
+#include <string>
 #include "yell/gmp.hpp"
 #include "yell/poly.hpp"
 
@@ -69,6 +72,27 @@ int main() {
       for (size_t w = 1; w < W; ++w)
         if (xg[i * W + w] != 0) return fail("lift of a small integer (high words)");
     }
+  }
+  // details/poly.hpp:135-149: a * s through a random split equals a * s
+  {
+    yell::poly<Deg> a(NdM, yell::uniform{}), s(NdM, yell::uniform{});
+    yell::poly<Deg> want = a * s;
+    a.mul_sensitive_poly(s);
+    if (a != want) return fail("mul_sensitive_poly");
+    a.check_vaild_range();
+  }
+  // details/poly.hpp:336-354 stream format; poly.hpp:150-156 recast_as_array
+  {
+    yell::poly<8> t(2);
+    for (size_t cm = 0; cm < 2; ++cm)
+      for (size_t i = 0; i < 8; ++i) t(cm, i) = 10 * cm + i;
+    std::ostringstream os;
+    os << t;
+    if (os.str() != "{{0ULL, 1ULL, 2ULL, 3ULL, 4ULL, 5ULL, 6ULL, 7ULL}\n"
+                    "{10ULL, 11ULL, 12ULL, 13ULL, 14ULL, 15ULL, 16ULL, 17ULL}}")
+      return fail("stream format");
+    auto arr = yell::recast_as_array(t, 1);
+    if ((*arr)[3] != 13 || arr->size() != 8) return fail("recast_as_array");
   }
   std::printf("OK\n");
   return 0;
