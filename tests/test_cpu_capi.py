@@ -108,3 +108,15 @@ def test_cpp_facade_compiles(tmp_path):
            "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_cpp_facade_math_helpers(tmp_path):
+    """yell/utils/math.hpp (host helpers): compiled and run on the CPU."""
+    exe = tmp_path / "facade_math"
+    cmd = ["g++", "-std=c++17", "-O1", f"-I{ROOT}/include", f"-I{ROOT}/include/yell_gb300",
+           f"{ROOT}/tests/cpp/facade_math.cpp", f"-L{ROOT}/yell_gb300", "-lyell_gb300",
+           f"-Wl,-rpath,{ROOT}/yell_gb300", "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.strip() == "OK", r.stdout + r.stderr
