@@ -277,7 +277,12 @@ int BatchExecutor::run_queue(DeviceContext* ctx, const yell_polymul_desc* descs,
     buckets.push_back(b);
   }
   if (buckets.size() > (1u << 24)) return fail(kInvalidArgument, "batch: too many buckets");
-  // ---- queue: forward column passes, whole-limb tiles, row steps, inverse column passes
+  // ---- queue: forward column passes, whole-limb tiles, row steps, inverse
+  // column passes.  All resident CTAs run the same kind of item most of the
+  // time, so the SMs' instruction caches hold one body at a time.
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device());
+  const uint32_t resident = (uint32_t)std::max(sms, 1) * 2;
   std::vector<QueueItem> items;
   for (int phase = 0; phase < 4; ++phase)
     for (size_t bi = 0; bi < buckets.size(); ++bi) {
@@ -354,9 +359,7 @@ int BatchExecutor::run_queue(DeviceContext* ctx, const yell_polymul_desc* descs,
   ql.next = d_queue_ctl_ + 1;
   ql.done = d_queue_ctl_ + 2;
   ql.timeout_ns = timeout_ns;
-  int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device());
-  ql.grid = (uint32_t)std::min<size_t>(items.size(), (size_t)std::max(sms, 1) * 2);
+  ql.grid = (uint32_t)std::min<size_t>(items.size(), resident);
   const uint64_t l0 = g_kernel_launches.load();
   e = launch_batch_queue(ql, s);
   last_launches_ = g_kernel_launches.load() - l0;

@@ -25,7 +25,7 @@ static_assert(kQueueTileLog == (uint32_t)kTileLog, "queue tiles are the two-pass
 
 template <int LOGN>
 constexpr int k1_of() {
-  return LOGN == 13 ? 6 : (LOGN <= 15 ? 7 : (LOGN == 16 ? 9 : 8));
+  return LOGN == 13 ? 6 : (LOGN <= 15 ? 7 : 8);
 }
 
 __device__ __forceinline__ uint64_t global_ns() {
@@ -97,13 +97,20 @@ __device__ __forceinline__ void dispatch(uint32_t kind, const QueueBucket& B, ui
   }
 }
 
+// Each CTA takes its next ticket while it works on the current item, so the
+// atomic's round trip is hidden behind the item.  Still deadlock-free: the
+// smallest ticket taken and not finished is always some CTA's current item
+// (a prefetched ticket is larger than its CTA's current one), and it depends
+// only on smaller tickets, which are all finished.
 __global__ void __launch_bounds__(kQueueThreads, 2) k_batch_queue(QueueLaunch q) {
-  __shared__ uint32_t s_ticket;
-  for (;;) {
-    if (threadIdx.x == 0) s_ticket = atomicAdd(q.next, 1u);
-    __syncthreads();
-    const uint32_t t = s_ticket;
+  __shared__ uint32_t s_ticket[2];
+  if (threadIdx.x == 0) s_ticket[0] = atomicAdd(q.next, 1u);
+  __syncthreads();
+  for (uint32_t cur = 0;; cur ^= 1u) {
+    const uint32_t t = s_ticket[cur];
     if (t >= q.n_items) break;
+    uint32_t next = 0;
+    if (threadIdx.x == 0) next = atomicAdd(q.next, 1u);
     const QueueItem it = q.items[t];
     const uint32_t kind = it.bucket_kind & 0xFFu;
     const QueueBucket B = q.buckets[it.bucket_kind >> 8];
@@ -118,6 +125,8 @@ __global__ void __launch_bounds__(kQueueThreads, 2) k_batch_queue(QueueLaunch q)
       if (kind != kItemColInv) publish = cnt + (kind == kItemColFwd ? 0 : 1);
     }
     dispatch(kind, B, it.bid);
+    // s_ticket[cur ^ 1] was last read before the previous iteration's barrier
+    if (threadIdx.x == 0) s_ticket[cur ^ 1u] = next;
     __syncthreads();  // every thread's stores issued; the tiles are free again
     if (publish && threadIdx.x == 0) {
       __threadfence();
@@ -128,7 +137,7 @@ __global__ void __launch_bounds__(kQueueThreads, 2) k_batch_queue(QueueLaunch q)
 
 }  // namespace
 
-uint32_t queue_k1(uint32_t log_n) { return log_n == 13 ? 6u : (log_n <= 15 ? 7u : (log_n == 16 ? 9u : 8u)); }
+uint32_t queue_k1(uint32_t log_n) { return log_n == 13 ? 6u : (log_n <= 15 ? 7u : 8u); }
 
 size_t queue_smem_bytes() { return 2 * kTileSmemBytes; }
 
