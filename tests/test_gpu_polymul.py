@@ -87,14 +87,15 @@ def test_config3_full_size(cuda, orc):
     assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("log_n,pairs,L", [(10, 3, 2), (16, 3, 4)])
-def test_polymul_host_pipeline(cuda, orc, log_n, pairs, L):
-    ps = y.primes(L)
+# chunking of pairs across the pipeline slots, with odd limb counts and a nonzero first modulus
+@pytest.mark.parametrize("log_n,pairs,L,cm0", [(10, 3, 2, 0), (16, 3, 4, 0), (12, 2, 7, 5), (16, 5, 7, 11)])
+def test_polymul_host_pipeline(cuda, orc, log_n, pairs, L, cm0):
+    ps = y.primes(L, cm0)
     a = uniform_polys(40 + log_n, pairs, L, log_n, ps)
     b = uniform_polys(50 + log_n, pairs, L, log_n, ps)
-    got = y.polymul_host(a, b, log_n)
+    got = y.polymul_host(a, b, log_n, cm0=cm0)
     for i in range(pairs):
-        assert np.array_equal(got[i], orc.polymul(a[i], b[i], log_n, 0))
+        assert np.array_equal(got[i], orc.polymul(a[i], b[i], log_n, cm0))
 
 
 def test_polymul_host_pinned(cuda, orc):
