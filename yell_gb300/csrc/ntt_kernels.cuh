@@ -312,10 +312,13 @@ __device__ __forceinline__ void col_pass_body(ConstLimbSet src, LimbSet dst, con
 
 // The standalone column pass keeps its own copy of the body above: compiled
 // as one kernel it schedules better at k1 = 9 (1.131 vs 1.141 ms for the
-// N = 2^16, L = 32, 16-pair polymul on GB300) than the inlined body.
+// N = 2^16, L = 32, 16-pair polymul on GB300) than the inlined body.  The
+// inverse pass waits mostly on its strided column loads: capped at 64
+// registers (a few bytes spilled) it runs four CTAs per SM instead of three,
+// and that polymul takes 1.117 instead of 1.127 ms.
 template <class C, int LOGB, bool INV>
-__global__ void __launch_bounds__(C::THREADS) k_col_pass(ConstLimbSet src, LimbSet dst,
-                                                         const DevMod* __restrict__ mods) {
+__global__ void __launch_bounds__(C::THREADS, INV ? 4 : 1) k_col_pass(ConstLimbSet src, LimbSet dst,
+                                                                      const DevMod* __restrict__ mods) {
   extern __shared__ __align__(16) uint64_t smem[];
   constexpr int K = C::K, LB = C::LB, NR = C::NR;
   constexpr uint32_t log_n = K + LOGB;
