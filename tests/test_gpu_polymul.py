@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 import yell_gb300 as y
+from yell_gb300 import _capi
 from yell_gb300.inputs import gaussian_polys, uniform_polys
 
 pytestmark = pytest.mark.gpu
@@ -111,3 +112,30 @@ def test_polymul_host_pinned(cuda, orc):
         assert np.array_equal(pc.array[i], orc.polymul(pa.array[i], pb.array[i], log_n, 0))
     for buf in (pa, pb, pc):
         buf.free()
+
+
+def test_polymul_every_modulus_in_one_call(cuda, orc):
+    """All 1000 moduli of the table (params::kMaxNbModuli) as the limbs of one
+    poly at N = 2^10; the last modulus index is 999."""
+    torch = cuda
+    log_n, L = 10, 1000
+    ps = y.primes(L)
+    a = uniform_polys(1000, 1, L, log_n, ps)
+    b = uniform_polys(1001, 1, L, log_n, ps)
+    c = torch.empty(a.size, dtype=torch.int64, device="cuda")
+    y.dev_polymul(c, _dev(torch, a), _dev(torch, b), 1, L, log_n, 0)
+    torch.cuda.synchronize()
+    got = _host(c, a.shape)
+    assert np.array_equal(got[0], orc.polymul(a[0], b[0], log_n, 0))
+
+
+def test_modulus_range_boundaries(cuda, orc):
+    torch = cuda
+    log_n = 12
+    # room for every limb the rejected calls name, so no call could write past it
+    t = torch.zeros(1001 << log_n, dtype=torch.int64, device="cuda")
+    y.dev_ntt(t[: 1 << log_n], 1, 1, log_n, 999, 0)  # the last modulus alone is fine
+    for cm0, L in ((999, 2), (1000, 1), (0, 1001)):
+        with pytest.raises(y.YellError) as ei:
+            y.dev_ntt(t, 1, L, log_n, cm0, 0)
+        assert ei.value.status == _capi.YELL_ERR_INVALID_MODULUS, (cm0, L)

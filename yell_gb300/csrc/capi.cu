@@ -84,9 +84,19 @@ int host_ntt(uint64_t* const* limbs, uint32_t L, uint32_t log_n, uint32_t cm0, N
   const DevMod* mods;
   YELL_TRY(ctx->ensure_tables(log_n, cm0, L, &mods));
   const size_t n = (size_t)1 << log_n;
+  cudaStream_t st = ctx->stream();
+  if (n * L <= DeviceContext::kSmallCallWords && ntt_launch_count(log_n, ctx->shape) == 1) {
+    // small call: one whole-limb launch in place on the mapped host buffer
+    std::lock_guard<std::mutex> g(ctx->small.lock);
+    YELL_TRY(ctx->small.ensure());
+    for (uint32_t i = 0; i < L; ++i) std::memcpy(ctx->small.host + i * n, limbs[i], n * 8);
+    YELL_CUDA(launch_ntt(contiguous(ctx->small.dev, L, L, cm0), log_n, mods, dir, ctx->shape, st), "launch ntt");
+    YELL_CUDA(cudaStreamSynchronize(st), "synchronize");
+    for (uint32_t i = 0; i < L; ++i) std::memcpy(limbs[i], ctx->small.host + i * n, n * 8);
+    return kOk;
+  }
   std::lock_guard<std::mutex> g(ctx->staging.lock);
   YELL_TRY(ctx->staging.reserve(n * L));
-  cudaStream_t st = ctx->stream();
   uint64_t* d = ctx->staging.ptr;
   for (uint32_t i = 0; i < L; ++i)
     YELL_CUDA(cudaMemcpyAsync(d + i * n, limbs[i], n * 8, cudaMemcpyHostToDevice, st), "H2D limb");
@@ -111,9 +121,29 @@ int host_elementwise(EwOp op, uint64_t* const* dst, const uint64_t* const* a,
   YELL_TRY(ctx->ensure_tables(log_n, 0, L, &mods));
   const size_t n = (size_t)1 << log_n;
   const size_t w = n * L;
+  cudaStream_t st = ctx->stream();
+  if (w <= DeviceContext::kSmallCallWords) {
+    // small call: the kernel reads and writes the mapped host buffer
+    std::lock_guard<std::mutex> g(ctx->small.lock);
+    YELL_TRY(ctx->small.ensure());
+    uint64_t* ha = ctx->small.host;
+    uint64_t* hb = ha + w;
+    uint64_t* hd = hb + w;
+    for (uint32_t i = 0; i < L; ++i) {
+      std::memcpy(ha + i * n, a[i], n * 8);
+      if (op != EwOp::kNegate) std::memcpy(hb + i * n, b[i], n * 8);
+      if (op == EwOp::kMuladd) std::memcpy(hd + i * n, dst[i], n * 8);
+    }
+    uint64_t* va = ctx->small.dev;
+    YELL_CUDA(launch_elementwise(op, contiguous(va + 2 * w, L, L, 0), const_contiguous(va, L, L, 0),
+                                 const_contiguous(va + w, L, L, 0), log_n, mods, st),
+              "launch elementwise");
+    YELL_CUDA(cudaStreamSynchronize(st), "synchronize");
+    for (uint32_t i = 0; i < L; ++i) std::memcpy(dst[i], hd + i * n, n * 8);
+    return kOk;
+  }
   std::lock_guard<std::mutex> g(ctx->staging.lock);
   YELL_TRY(ctx->staging.reserve(3 * w));
-  cudaStream_t st = ctx->stream();
   uint64_t* da = ctx->staging.ptr;
   uint64_t* db = da + w;
   uint64_t* dd = db + w;
@@ -253,6 +283,23 @@ int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_
   const DevMod* mods;
   YELL_TRY(ctx->ensure_tables(log_n, cm0, L, &mods));
   const size_t pair_words = ((size_t)L) << log_n;
+  if ((size_t)pairs * pair_words <= DeviceContext::kSmallCallWords &&
+      polymul_launch_count(log_n, ctx->shape) == 1) {
+    // small call: one whole-limb launch on the mapped host buffer
+    const size_t w = (size_t)pairs * pair_words;
+    std::lock_guard<std::mutex> g(ctx->small.lock);
+    YELL_TRY(ctx->small.ensure());
+    std::memcpy(ctx->small.host, a, w * 8);
+    std::memcpy(ctx->small.host + w, b, w * 8);
+    uint64_t* va = ctx->small.dev;
+    cudaStream_t st = ctx->stream();
+    YELL_CUDA(launch_polymul(contiguous(va + 2 * w, pairs * L, L, cm0), const_contiguous(va, pairs * L, L, cm0),
+                             const_contiguous(va + w, pairs * L, L, cm0), log_n, mods, nullptr, ctx->shape, st),
+              "launch polymul");
+    YELL_CUDA(cudaStreamSynchronize(st), "synchronize");
+    std::memcpy(c, ctx->small.host + 2 * w, w * 8);
+    return kOk;
+  }
   // ~64 MiB of operands per chunk, at least one pair.
   const size_t target = (64ull << 20) / 8;
   uint32_t cp = (uint32_t)std::max<size_t>(1, target / (2 * pair_words));

@@ -142,6 +142,22 @@ int DeviceContext::Buffer::reserve(size_t w) {
   return kOk;
 }
 
+int DeviceContext::HostMapped::ensure() {
+  if (host) return kOk;
+  void* h = nullptr;
+  cudaError_t e = cudaHostAlloc(&h, 3 * kSmallCallWords * sizeof(uint64_t), cudaHostAllocMapped);
+  if (e != cudaSuccess) return fail_cuda(e, "cudaHostAlloc(small-call buffer)");
+  void* d = nullptr;
+  e = cudaHostGetDevicePointer(&d, h, 0);
+  if (e != cudaSuccess) {
+    cudaFreeHost(h);
+    return fail_cuda(e, "cudaHostGetDevicePointer(small-call buffer)");
+  }
+  host = static_cast<uint64_t*>(h);
+  dev = static_cast<uint64_t*>(d);
+  return kOk;
+}
+
 DeviceContext::DeviceContext(int device) : device_(device) {}
 
 int DeviceContext::init() {

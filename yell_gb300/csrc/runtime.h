@@ -86,6 +86,20 @@ class DeviceContext {
   Buffer scratch;   // polymul scratch for device-resident calls
   Buffer staging;   // host-pointer drop-ins: operands / results
 
+  // Pinned host memory mapped into this device's address space, for small
+  // host-pointer calls: the caller's words are copied in on the host and the
+  // kernel reads and writes them in place, so a call is one launch and one
+  // stream synchronisation instead of copy calls around the launch.  Three
+  // operands of kSmallCallWords words each; allocated on first use.
+  static constexpr size_t kSmallCallWords = size_t(1) << 15;
+  struct HostMapped {
+    std::mutex lock;
+    uint64_t* host = nullptr;  // host address
+    uint64_t* dev = nullptr;   // the same memory as the device sees it
+    int ensure();              // under lock
+  };
+  HostMapped small;
+
   // Pipelined host polymul, under `pipe_lock`: one stream each for H2D,
   // compute and D2H; kPipeSlots device buffer sets cycled by the chunks, with
   // per-slot events ordering reuse of a slot's buffers.
