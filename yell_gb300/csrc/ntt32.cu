@@ -12,6 +12,7 @@
 // and scaled last layer follow.  The butterflies, their order and their
 // twiddle indices are the reference's, so lazy words match it exactly.
 #include <algorithm>
+#include <cstring>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -526,6 +527,9 @@ __global__ void k32_elementwise(uint32_t* dst, const uint32_t* a, const uint32_t
 // ---- launch ----------------------------------------------------------------------
 // Degrees whose polymul runs on a CTA pair.
 constexpr int kMinPairLogN = 14;
+// Host-pointer calls up to this degree (single-CTA kernels) run in place on
+// the context's pinned, device-mapped host buffer.
+constexpr uint32_t kSmallCall32LogN = 13;
 
 template <int LOGN>
 cudaError_t set_attrs32() {
@@ -639,11 +643,25 @@ int host_ntt32(int kind, uint32_t* op, uint32_t log_n, uint32_t cm) {
   int st = prepare32(log_n, cm, 1, &ctx, &mods);
   if (st != kOk) return st;
   const size_t n = (size_t)1 << log_n;
+  cudaStream_t s = ctx->stream();
+  if (log_n <= kSmallCall32LogN) {
+    // small call: one single-CTA launch in place on the mapped host buffer
+    std::lock_guard<std::mutex> g(ctx->small.lock);
+    st = ctx->small.ensure();
+    if (st != kOk) return st;
+    uint32_t* h = reinterpret_cast<uint32_t*>(ctx->small.host);
+    std::memcpy(h, op, n * 4);
+    st = run32(kind, reinterpret_cast<uint32_t*>(ctx->small.dev), nullptr, nullptr, 1, 1, log_n, cm, s);
+    if (st != kOk) return st;
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail_cuda(e, "synchronize");
+    std::memcpy(op, h, n * 4);
+    return kOk;
+  }
   std::lock_guard<std::mutex> g(ctx->staging.lock);
   st = ctx->staging.reserve(n);
   if (st != kOk) return st;
   uint32_t* d = reinterpret_cast<uint32_t*>(ctx->staging.ptr);
-  cudaStream_t s = ctx->stream();
   cudaError_t e = cudaMemcpyAsync(d, op, n * 4, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return fail_cuda(e, "H2D");
   st = run32(kind, d, nullptr, nullptr, 1, 1, log_n, cm, s);
@@ -742,15 +760,38 @@ static int host_poly32(int kind, int op, uint32_t* const* dst, const uint32_t* c
   int st = prepare32(log_n, 0, L, &ctx, &mods);
   if (st != kOk) return st;
   const size_t n = (size_t)1 << log_n, w = n * L;
+  cudaStream_t s = ctx->stream();
+  const bool need_dst = kind != 3 || op == YELL_OP_MULADD;
+  if (log_n <= kSmallCall32LogN && w <= 2 * DeviceContext::kSmallCallWords) {
+    // small call: the kernel works on the mapped host buffer (three operands
+    // of w 32-bit words fit its 3 x kSmallCallWords 64-bit words)
+    std::lock_guard<std::mutex> g(ctx->small.lock);
+    st = ctx->small.ensure();
+    if (st != kOk) return st;
+    uint32_t* hd = reinterpret_cast<uint32_t*>(ctx->small.host);
+    uint32_t* ha = hd + w;
+    uint32_t* hb = ha + w;
+    for (uint32_t l = 0; l < L; ++l) {
+      if (need_dst) std::memcpy(hd + l * n, dst[l], n * 4);
+      if (kind == 3) std::memcpy(ha + l * n, a[l], n * 4);
+      if (binary) std::memcpy(hb + l * n, b[l], n * 4);
+    }
+    uint32_t* vd = reinterpret_cast<uint32_t*>(ctx->small.dev);
+    st = kind == 3 ? yell32_dev_elementwise(op, vd, vd + w, binary ? vd + 2 * w : nullptr, 1, L, log_n, 0, s)
+                   : run32(kind, vd, nullptr, nullptr, 1, L, log_n, 0, s);
+    if (st != kOk) return st;
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail_cuda(e, "synchronize");
+    for (uint32_t l = 0; l < L; ++l) std::memcpy(dst[l], hd + l * n, n * 4);
+    return kOk;
+  }
   std::lock_guard<std::mutex> g(ctx->staging.lock);
   st = ctx->staging.reserve((3 * w + 1) / 2);  // three uint32 operands in uint64 words
   if (st != kOk) return st;
   uint32_t* dd = reinterpret_cast<uint32_t*>(ctx->staging.ptr);
   uint32_t* da = dd + w;
   uint32_t* db = da + w;
-  cudaStream_t s = ctx->stream();
   cudaError_t e = cudaSuccess;
-  const bool need_dst = kind != 3 || op == YELL_OP_MULADD;
   for (uint32_t l = 0; l < L && e == cudaSuccess; ++l) {
     if (need_dst) e = cudaMemcpyAsync(dd + l * n, dst[l], n * 4, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && kind == 3) e = cudaMemcpyAsync(da + l * n, a[l], n * 4, cudaMemcpyHostToDevice, s);
