@@ -552,9 +552,17 @@ def run_rows(torch, y, stream, dc, reps: int = 5):
     m32.init_ntt_tables(log32, L)
     ms = timed(lambda: m32.dev_polymul(c32, a32, b32, PAIRS, L, log32, stream=stream))
     byts = 12 * n32 * L * PAIRS
+    # integer roofline: 3 NTTs of (N/2) log N butterflies per limb pair (2 CT, 1 GS)
+    bfly = 3 * L * PAIRS * (1 << (log32 - 1)) * log32
+    ct32, gs32 = m32.calibrate_butterflies()
+    ceiling32 = 3.0 / (2.0 / ct32 + 1.0 / gs32)
     out["polymul32"] = {"ms": ms, "limb_ntts_per_s": 3 * L * PAIRS / (ms * 1e-3),
                         "achieved_gbs": byts / (ms * 1e-3) / 1e9, "frac": byts / (ms * 1e-3) / 1e9 / hbm,
-                        "algorithmic_bytes": byts, "workload": "N=2^15, L=32, 16 pairs, 30-bit primes"}
+                        "algorithmic_bytes": byts, "workload": "N=2^15, L=32, 16 pairs, 30-bit primes",
+                        "integer": {"bfly_per_s": bfly / (ms * 1e-3), "ceiling_bfly_per_s": ceiling32,
+                                    "frac": bfly / (ms * 1e-3) / ceiling32,
+                                    "note": "ceiling = register-only 32-bit CT/GS butterflies, 2:1 mix "
+                                            "(yell32_calibrate_butterflies)"}}
     return out
 
 

@@ -383,6 +383,8 @@ int yell_autotune(uint32_t log_n, uint32_t L, uint32_t pairs, uint32_t* best, do
  * every SM of the current device and returns butterflies per second, the
  * ceiling the 64-bit modular arithmetic allows at the current clock. */
 int yell_calibrate_butterflies(double* ct_per_s, double* gs_per_s);
+/* The same for the 32-bit moduli mode's butterflies on 32-bit words. */
+int yell32_calibrate_butterflies(double* ct_per_s, double* gs_per_s);
 
 /* Waits for all work the library queued on its own stream of this device. */
 int yell_synchronize(void);

@@ -89,6 +89,7 @@ SIGNATURES = {
     "yell_dev_polymul_noalloc": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),
     "yell_dev_polymul_batch": (_int, [_vp, _u32, _vp]),
     "yell_calibrate_butterflies": (_int, [_vp, _vp]),
+    "yell32_calibrate_butterflies": (_int, [_vp, _vp]),
     "yell_negacyclic_forward_lazy": (_int, [_vp, _u64, _vp, _vp, _u64]),
     "yell_negacyclic_backward_lazy": (_int, [_vp, _u64, _vp, _vp, _u64]),
     "yell32_max_moduli": (_u32, []),

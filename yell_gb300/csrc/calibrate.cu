@@ -45,7 +45,93 @@ __global__ void __launch_bounds__(256) k_butterfly_ceiling(uint64_t* out, const 
   for (int i = 0; i < 16; ++i) out[(size_t)tid * 16 + i] = x[i];
 }
 
+// The same loop on 32-bit words with the 32-bit mode's butterflies (the
+// twiddles are arbitrary residues of a 30-bit modulus with their Shoup
+// companions; the rate does not depend on their values).
+template <bool GS>
+__global__ void __launch_bounds__(256) k_butterfly_ceiling32(uint32_t* out, const uint2* tw, uint32_t p, int iters) {
+  uint32_t x[16];
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int i = 0; i < 16; ++i) x[i] = (tid * 0x9E3779B9u + i * 0x85EBCA6Bu) % (2 * p);
+  const uint32_t p2 = 2 * p, np = 0u - p;
+  uint2 w[15];
+  for (int i = 0; i < 15; ++i) w[i] = tw[(tid + i) & 63];
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int d = 1 << (3 - k);
+#pragma unroll
+      for (int jj = 0; jj < (1 << k); ++jj)
+#pragma unroll
+        for (int q = 0; q < d; ++q) {
+          const int j = jj * 2 * d + q;
+          const uint2 ww = w[(1 << k) - 1 + jj];
+          if (GS)
+            gs_bfly(x[j], x[j + d], ww.x, ww.y, np, p2);
+          else
+            ct_bfly(x[j], x[j + d], ww.x, ww.y, np, p2);
+        }
+    }
+  }
+  for (int i = 0; i < 16; ++i) out[(size_t)tid * 16 + i] = x[i];
+}
+
 }  // namespace
+
+extern "C" int yell32_calibrate_butterflies(double* ct_per_s, double* gs_per_s) {
+  if (!ct_per_s || !gs_per_s) return fail(kInvalidArgument, "null output");
+  int st = kOk;
+  DeviceContext* ctx = DeviceContext::current(&st);
+  if (!ctx) return st;
+  int sms = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device());
+  if (e != cudaSuccess) return fail_cuda(e, "cudaDeviceGetAttribute");
+  const uint32_t p = yell32_prime(0);
+  uint2 htw[64];
+  uint64_t s = 0x243F6A8885A308D3ull;
+  for (uint2& t : htw) {
+    s = s * 6364136223846793005ull + 1442695040888963407ull;
+    t.x = (uint32_t)((s >> 20) % p);
+    t.y = (uint32_t)(((uint64_t)t.x << 32) / p);
+  }
+  const int blocks = sms * 8, threads = 256, iters = 400;
+  uint2* tw = nullptr;
+  uint32_t* out = nullptr;
+  e = cudaMalloc(&tw, sizeof(htw));
+  if (e == cudaSuccess) e = cudaMalloc(&out, (size_t)blocks * threads * 16 * sizeof(uint32_t));
+  cudaStream_t strm = ctx->stream();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tw, htw, sizeof(htw), cudaMemcpyHostToDevice, strm);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  const double bfly = (double)blocks * threads * iters * 32;
+  double rates[2] = {0, 0};
+  for (int gs = 0; gs < 2 && e == cudaSuccess; ++gs) {
+    float best = 1e30f;
+    for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {
+      cudaEventRecord(e0, strm);
+      if (gs)
+        k_butterfly_ceiling32<true><<<blocks, threads, 0, strm>>>(out, tw, p, iters);
+      else
+        k_butterfly_ceiling32<false><<<blocks, threads, 0, strm>>>(out, tw, p, iters);
+      g_kernel_launches += 1;
+      cudaEventRecord(e1, strm);
+      e = cudaEventSynchronize(e1);
+      float ms = 0;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0 && ms < best) best = ms;  // first run is the warm-up
+    }
+    rates[gs] = bfly / (best * 1e-3);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (tw) cudaFree(tw);
+  if (out) cudaFree(out);
+  if (e != cudaSuccess) return fail_cuda(e, "calibration run (32-bit)");
+  *ct_per_s = rates[0];
+  *gs_per_s = rates[1];
+  return kOk;
+}
 
 extern "C" int yell_calibrate_butterflies(double* ct_per_s, double* gs_per_s) {
   if (!ct_per_s || !gs_per_s) return fail(kInvalidArgument, "null output");

@@ -95,7 +95,16 @@ def dev_elementwise(op: int, dst, a, b, count: int, L: int, log_n: int, cm0: int
          count, L, log_n, cm0, _stream(stream))
 
 
-__all__ = ["max_moduli", "max_log_degree", "prime", "primes", "prime_pn", "primitive_root",
+def calibrate_butterflies() -> tuple[float, float]:
+    """Register-only rate of the 32-bit butterflies on this GPU: (CT per s, GS per s)."""
+    import ctypes
+
+    ct, gs = ctypes.c_double(), ctypes.c_double()
+    call("yell32_calibrate_butterflies", ctypes.addressof(ct), ctypes.addressof(gs))
+    return ct.value, gs.value
+
+
+__all__ = ["calibrate_butterflies", "max_moduli", "max_log_degree", "prime", "primes", "prime_pn", "primitive_root",
            "init_ntt_tables", "ntt_tables", "ntt_forward", "ntt_forward_lazy", "ntt_backward",
            "dev_ntt", "dev_polymul", "dev_elementwise", "YELL_FORWARD", "YELL_FORWARD_LAZY",
            "YELL_BACKWARD"]
