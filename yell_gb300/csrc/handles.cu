@@ -58,7 +58,7 @@ int yell_dev_poly_alloc(uint32_t L, uint32_t log_n, uint32_t cm0, yell_dev_poly*
   if (st != kOk) return st;
   st = check_moduli(cm0, L);
   if (st != kOk) return st;
-  DeviceContext* ctx;
+  DeviceContext* ctx = nullptr;
   st = context_for(-1, &ctx);
   if (st != kOk) return st;
   const DevMod* mods;
@@ -80,7 +80,7 @@ int yell_dev_poly_alloc(uint32_t L, uint32_t log_n, uint32_t cm0, yell_dev_poly*
 
 int yell_dev_poly_free(yell_dev_poly* p) {
   if (!p) return kOk;
-  DeviceContext* ctx;
+  DeviceContext* ctx = nullptr;
   int st = context_for(p->device, &ctx);
   if (st != kOk) return st;
   // pending work on the library stream may still use the buffer
@@ -101,7 +101,7 @@ int yell_dev_poly_info(const yell_dev_poly* p, uint64_t** d_data, uint32_t* L, u
 
 int yell_dev_poly_upload(yell_dev_poly* p, const uint64_t* const* limbs) {
   if (!p || !limbs) return fail(kInvalidArgument, "null handle or limb array");
-  DeviceContext* ctx;
+  DeviceContext* ctx = nullptr;
   int st = context_for(p->device, &ctx);
   if (st != kOk) return st;
   const size_t n = limb_words(p);
@@ -117,7 +117,7 @@ int yell_dev_poly_upload(yell_dev_poly* p, const uint64_t* const* limbs) {
 
 int yell_dev_poly_download(const yell_dev_poly* p, uint64_t* const* limbs) {
   if (!p || !limbs) return fail(kInvalidArgument, "null handle or limb array");
-  DeviceContext* ctx;
+  DeviceContext* ctx = nullptr;
   int st = context_for(p->device, &ctx);
   if (st != kOk) return st;
   const size_t n = limb_words(p);
@@ -133,7 +133,7 @@ int yell_dev_poly_download(const yell_dev_poly* p, uint64_t* const* limbs) {
 
 int yell_dev_poly_ntt(yell_dev_poly* p, int direction) {
   if (!p) return fail(kInvalidArgument, "null handle");
-  DeviceContext* ctx;
+  DeviceContext* ctx = nullptr;
   int st = context_for(p->device, &ctx);
   if (st != kOk) return st;
   return yell_dev_ntt(p->data, 1, p->L, p->log_n, p->cm0, direction, nullptr);
@@ -144,7 +144,7 @@ int yell_dev_poly_op(int op, yell_dev_poly* dst, const yell_dev_poly* a, const y
   int st = same_shape(dst, a);
   if (st == kOk && op != YELL_OP_NEGATE) st = same_shape(dst, b);
   if (st != kOk) return st;
-  DeviceContext* ctx;
+  DeviceContext* ctx = nullptr;
   st = context_for(dst->device, &ctx);
   if (st != kOk) return st;
   return yell_dev_elementwise(op, dst->data, a->data, op == YELL_OP_NEGATE ? nullptr : b->data, 1, dst->L,
@@ -157,7 +157,7 @@ int yell_dev_poly_mul(yell_dev_poly* c, const yell_dev_poly* a, const yell_dev_p
   int st = same_shape(c, a);
   if (st == kOk) st = same_shape(c, b);
   if (st != kOk) return st;
-  DeviceContext* ctx;
+  DeviceContext* ctx = nullptr;
   st = context_for(c->device, &ctx);
   if (st != kOk) return st;
   return yell_dev_polymul(c->data, a->data, b->data, 1, c->L, c->log_n, c->cm0, nullptr, 0, nullptr);
@@ -178,7 +178,7 @@ int yell_batch_submit(yell_dev_poly* const* c, const yell_dev_poly* const* a, co
     device = c[i]->device;
     descs[i] = yell_polymul_desc{c[i]->data, a[i]->data, b[i]->data, c[i]->log_n, c[i]->L, c[i]->cm0, 0};
   }
-  DeviceContext* ctx;
+  DeviceContext* ctx = nullptr;
   int st = context_for(device, &ctx);
   if (st != kOk) return st;
   st = yell_dev_polymul_batch(descs.data(), n, nullptr);

@@ -403,7 +403,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, 2)
   const uint32_t limb = blockIdx.x >> 1;    // grid = 2 x limbs, every CTA active
   const uint32_t tid = threadIdx.x;
   const DevMod32 m = load_mod(mods, ls.cm(limb));
-  const uint32_t p = m.p, p2 = p << 1, np = 0u - p;
+  const uint32_t p = m.p, p2 = p << 1;
   const uint2 w1 = __ldg(m.fwd + 1);
   const size_t lbase = (size_t)limb << log_n;
   const uint32_t bb = RB::base(tid);

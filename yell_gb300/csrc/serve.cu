@@ -95,7 +95,7 @@ struct yell_server {
   int init(const yell_server_config* c);
   void loop();
   void finish(Slot& s);
-  bool admit_into(Slot& s, std::vector<ReqPtr>* batch);
+  bool admit(std::vector<ReqPtr>* batch);
   int launch(Slot& s, std::vector<ReqPtr>& batch);
   void complete(const ReqPtr& r, int status, Clock::time_point t);
   void shutdown();
@@ -201,7 +201,7 @@ void yell_server::finish(Slot& s) {
 }
 
 // Takes queued requests in arrival order while the arena can hold them.
-bool yell_server::admit_into(Slot& s, std::vector<ReqPtr>* batch) {
+bool yell_server::admit(std::vector<ReqPtr>* batch) {
   std::lock_guard<std::mutex> g(mu);
   const Clock::time_point t = Clock::now();
   while (!pending.empty() && batch->size() < cfg.max_batch) {
@@ -334,7 +334,7 @@ void yell_server::loop() {
         Slot& s = *sp;
         if (s.busy) continue;
         std::vector<ReqPtr> batch;
-        if (!admit_into(s, &batch)) break;
+        if (!admit(&batch)) break;
         const int st = launch(s, batch);
         if (st != kOk) {
           // the batch failed to launch: fail its requests, keep serving
