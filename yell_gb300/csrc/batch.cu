@@ -14,6 +14,7 @@
 #include <array>
 
 #include "batch_queue.h"
+#include "profiler.h"
 #include <cstring>
 #include <memory>
 
@@ -122,6 +123,7 @@ cudaError_t BatchExecutor::launch_buckets(const std::vector<Bucket>& buckets, cu
 
 int BatchExecutor::run(DeviceContext* ctx, const yell_polymul_desc* descs, uint64_t* const* desc_scratch,
                        uint32_t n, cudaStream_t s, bool use_graph, bool fork) {
+  TraceRange trace("yell batch");
   // ---- buckets and their list layout -----------------------------------
   std::array<std::vector<uint32_t>, kDegrees> members;
   for (uint32_t i = 0; i < n; ++i) members[descs[i].log_n - kMinLogN].push_back(i);
@@ -240,6 +242,7 @@ int BatchExecutor::reserve_queue_ctl(size_t words) {
 
 int BatchExecutor::run_queue(DeviceContext* ctx, const yell_polymul_desc* descs, uint32_t n, cudaStream_t s,
                              uint64_t timeout_ns) {
+  TraceRange trace("yell batch queue");
   if (!queue_attrs_) {
     const cudaError_t e = queue_set_attributes();
     if (e != cudaSuccess) return fail_cuda(e, "queue kernel attributes");

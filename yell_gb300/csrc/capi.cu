@@ -274,6 +274,7 @@ void yell_host_free(void* p) {
 // and for the copy-out that read its product.
 int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_t pairs,
                       uint32_t L, uint32_t log_n, uint32_t cm0) {
+  TraceRange trace("yell polymul_host");
   if (!c || !a || !b) return fail(kInvalidArgument, "null pointer");
   if (pairs == 0) return fail(kInvalidArgument, "pairs is 0");
   YELL_TRY(check_degree(log_n));

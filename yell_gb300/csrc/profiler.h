@@ -4,12 +4,17 @@
 // by the launchers is bracketed by a pair of CUDA events recorded on the
 // launching stream; totals per kernel name are read back after stop.  When
 // disabled the scope objects cost one relaxed atomic load.
+//
+// Every launch scope and every batch / serving step is also an NVTX range
+// (header-only NVTX 3: a no-op unless a tool such as ncu or nsys is attached),
+// so a timeline shows the library's launches by name inside its steps.
 #pragma once
 #include <atomic>
 #include <cstdint>
 #include <string>
 #include <vector>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 namespace yell_gb300 {
 
@@ -28,10 +33,20 @@ int profile_stop();
 int profile_count();
 int profile_get(int i, std::string* name, uint64_t* launches, double* total_ms);
 
-// Brackets one kernel launch on `st` when profiling is on.
+// An NVTX range for the lifetime of the object.
+class TraceRange {
+ public:
+  explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+  ~TraceRange() { nvtxRangePop(); }
+  TraceRange(const TraceRange&) = delete;
+  TraceRange& operator=(const TraceRange&) = delete;
+};
+
+// Brackets one kernel launch on `st` when profiling is on (and always with an
+// NVTX range of the kernel's name).
 class LaunchScope {
  public:
-  LaunchScope(const char* name, cudaStream_t st) : name_(name), st_(st) {
+  LaunchScope(const char* name, cudaStream_t st) : name_(name), st_(st), range_(name) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (g_profiling.load(std::memory_order_relaxed) &&
         cudaStreamIsCapturing(st_, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
@@ -50,6 +65,7 @@ class LaunchScope {
  private:
   const char* name_;
   cudaStream_t st_;
+  TraceRange range_;
   cudaEvent_t start_ = nullptr, stop_ = nullptr;
 };
 

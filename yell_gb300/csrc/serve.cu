@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "batch.h"
+#include "profiler.h"
 #include "range_alloc.h"
 #include "runtime.h"
 #include "yell_gb300.h"
@@ -253,6 +254,7 @@ bool yell_server::admit(std::vector<ReqPtr>* batch) {
 }
 
 int yell_server::launch(Slot& s, std::vector<ReqPtr>& batch) {
+  TraceRange trace("yell serve step");
   const size_t n = batch.size();
   std::vector<yell_polymul_desc> descs;
   std::vector<uint64_t*> scratch;
