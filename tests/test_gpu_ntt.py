@@ -115,8 +115,9 @@ def test_device_limb_pointer_list(cuda, orc, log_n):
 
 
 def test_config2_forward_inverse_full_size(cuda, orc):
-    """N=2^14, L=8 (P[0..7]), batch 64, one launch each way: forward words
-    equal the reference's, and the inverse returns the input exactly."""
+    """N=2^14, L=8 (P[0..7]), batch 64, one call each way over all 512 limbs
+    (a column-pass and a row-pass launch): forward words equal the
+    reference's, and the inverse returns the input exactly."""
     torch = cuda
     log_n, L, count = 14, 8, 64
     x = uniform_polys(2, count, L, log_n, y.primes(L))
