@@ -554,6 +554,8 @@ __device__ __forceinline__ void polymul_rows_body(LimbSet ca, ConstLimbSet sbuf,
                                                   uint32_t bid) {
   extern __shared__ __align__(16) uint64_t smem[];
   constexpr int K = C::K, NR = C::NR;
+  // rows stay with their threads: warp barriers where a row fits one warp
+  constexpr bool WS = C::WARP_LOCAL;
   constexpr uint32_t log_n = K + K1;
   constexpr int TPL = log_n - kTileLog;
   uint64_t* sa = smem;
@@ -574,17 +576,17 @@ __device__ __forceinline__ void polymul_rows_body(LimbSet ca, ConstLimbSet sbuf,
   ct_stages2<R0::R, R0::E, 0>(xa, xb, m.fwd, K1 + R0::HI, R0::gr(b0, G), 0 - m.p, m.p << 1);
   smem_store<R0>(xa, sa, b0);
   smem_store<R0>(xb, sb, b0);
-  __syncthreads();
-  fwd_rounds<C, 1, NR - 1>(sa, tid, K1, G, m.fwd, m.p, true);
-  fwd_rounds<C, 1, NR - 1>(sb, tid, K1, G, m.fwd, m.p, true);
+  round_barrier<WS>();
+  fwd_rounds<C, 1, NR - 1, WS>(sa, tid, K1, G, m.fwd, m.p, true);
+  fwd_rounds<C, 1, NR - 1, WS>(sb, tid, K1, G, m.fwd, m.p, true);
   using RB = Round<C, NR - 1>;
   const uint32_t bb = RB::base(tid);
   smem_load<RB>(xa, sa, bb);
   smem_load<RB>(xb, sb, bb);
   fused_product<C, false>(xa, xb, bb, log_n, K1, G, m);
   smem_store<RB>(xa, sa, bb);
-  __syncthreads();
-  inv_rounds<C, NR - 2, 0, false>(sa, tid, log_n, 0, G, m, true);
+  round_barrier<WS>();
+  inv_rounds<C, NR - 2, 0, false, WS>(sa, tid, log_n, 0, G, m, true);
   smem_load<R0>(xa, sa, b0);
   gs_round<R0, false>(xa, log_n, R0::BETA, R0::gr(b0, G), m);
   gstore_rows<R0>(xa, pa, b0);
