@@ -462,6 +462,8 @@ __device__ __forceinline__ void polymul_whole_body(LimbSet c, ConstLimbSet a, Co
     __syncthreads();
     stage_out_limbs<C>(sa, c, limb0, log_n, mods, false);
   } else {
+    // no CTA-wide staging on this path: barriers over a limb's threads only
+    constexpr int BK = C::LOCAL_BARRIER;
     using R0 = Round<C, 0>;
     const uint32_t b0 = R0::base(tid);
     if (active) {
@@ -471,9 +473,9 @@ __device__ __forceinline__ void polymul_whole_body(LimbSet c, ConstLimbSet a, Co
       smem_store<R0>(xa, sa, b0);
       smem_store<R0>(xb, sb, b0);
     }
-    __syncthreads();
-    fwd_rounds<C, 1, NR - 1>(sa, tid, 0, 0, m.fwd, m.p, active);
-    fwd_rounds<C, 1, NR - 1>(sb, tid, 0, 0, m.fwd, m.p, active);
+    round_barrier<C, BK>(tid);
+    fwd_rounds<C, 1, NR - 1, BK>(sa, tid, 0, 0, m.fwd, m.p, active);
+    fwd_rounds<C, 1, NR - 1, BK>(sb, tid, 0, 0, m.fwd, m.p, active);
     using RB = Round<C, NR - 1>;
     const uint32_t bb = RB::base(tid);
     if (active) {
@@ -482,8 +484,8 @@ __device__ __forceinline__ void polymul_whole_body(LimbSet c, ConstLimbSet a, Co
       fused_product<C, false>(xa, xb, bb, log_n, 0, 0, m);
       smem_store<RB>(xa, sa, bb);
     }
-    __syncthreads();
-    inv_rounds<C, NR - 2, 0, true>(sa, tid, log_n, 0, 0, m, active);
+    round_barrier<C, BK>(tid);
+    inv_rounds<C, NR - 2, 0, true, BK>(sa, tid, log_n, 0, 0, m, active);
     if (active) {
       smem_load<R0>(xa, sa, b0);
       gs_round<R0, true>(xa, log_n, R0::BETA, R0::gr(b0, 0), m);
@@ -554,8 +556,8 @@ __device__ __forceinline__ void polymul_rows_body(LimbSet ca, ConstLimbSet sbuf,
                                                   uint32_t bid) {
   extern __shared__ __align__(16) uint64_t smem[];
   constexpr int K = C::K, NR = C::NR;
-  // rows stay with their threads: warp barriers where a row fits one warp
-  constexpr bool WS = C::WARP_LOCAL;
+  // rows stay with their threads: barriers over a row's threads only
+  constexpr int BK = C::LOCAL_BARRIER;
   constexpr uint32_t log_n = K + K1;
   constexpr int TPL = log_n - kTileLog;
   uint64_t* sa = smem;
@@ -576,17 +578,17 @@ __device__ __forceinline__ void polymul_rows_body(LimbSet ca, ConstLimbSet sbuf,
   ct_stages2<R0::R, R0::E, 0>(xa, xb, m.fwd, K1 + R0::HI, R0::gr(b0, G), 0 - m.p, m.p << 1);
   smem_store<R0>(xa, sa, b0);
   smem_store<R0>(xb, sb, b0);
-  round_barrier<WS>();
-  fwd_rounds<C, 1, NR - 1, WS>(sa, tid, K1, G, m.fwd, m.p, true);
-  fwd_rounds<C, 1, NR - 1, WS>(sb, tid, K1, G, m.fwd, m.p, true);
+  round_barrier<C, BK>(tid);
+  fwd_rounds<C, 1, NR - 1, BK>(sa, tid, K1, G, m.fwd, m.p, true);
+  fwd_rounds<C, 1, NR - 1, BK>(sb, tid, K1, G, m.fwd, m.p, true);
   using RB = Round<C, NR - 1>;
   const uint32_t bb = RB::base(tid);
   smem_load<RB>(xa, sa, bb);
   smem_load<RB>(xb, sb, bb);
   fused_product<C, false>(xa, xb, bb, log_n, K1, G, m);
   smem_store<RB>(xa, sa, bb);
-  round_barrier<WS>();
-  inv_rounds<C, NR - 2, 0, false, WS>(sa, tid, log_n, 0, G, m, true);
+  round_barrier<C, BK>(tid);
+  inv_rounds<C, NR - 2, 0, false, BK>(sa, tid, log_n, 0, G, m, true);
   smem_load<R0>(xa, sa, b0);
   gs_round<R0, false>(xa, log_n, R0::BETA, R0::gr(b0, G), m);
   gstore_rows<R0>(xa, pa, b0);

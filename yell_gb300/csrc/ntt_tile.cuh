@@ -69,9 +69,14 @@ struct TileCfg {
   // Tile bits above LB + K (sub-transform index) of thread tid.
   __device__ static __forceinline__ uint32_t sub(uint32_t tid) { return tid >> (LB + K - LOGE); }
   // A thread keeps its sub-transform in every round (the tid bits above the
-  // lowest K - LOGE select it), so with contiguous sub-transforms (LB = 0) of
-  // at most 32 threads every exchange between rounds stays inside one warp.
-  static constexpr bool WARP_LOCAL = LB == 0 && K - LOGE <= 5;
+  // lowest K - LOGE select it), so with contiguous sub-transforms (LB = 0)
+  // every exchange between rounds stays among the GROUP threads of one
+  // sub-transform.  The barrier between rounds for a caller that does no
+  // CTA-wide staging around them: 1 = the warp's (GROUP <= 32), 2 = a named
+  // barrier per sub-transform (at most 15 in the CTA), 0 = the CTA's.
+  static constexpr int GROUP = 1 << (K - LOGE);
+  static constexpr int LOCAL_BARRIER =
+      LB != 0 ? 0 : (GROUP <= 32 ? 1 : ((GROUP < THREADS && THREADS / GROUP <= 15) ? 2 : 0));
   static_assert(K >= LOGE, "transform narrower than a thread's word set");
   static_assert(T >= K + LB, "tile smaller than one sub-transform");
 };
@@ -405,37 +410,40 @@ __device__ __forceinline__ void inv_round_smem(W* s, uint32_t tid, uint32_t log_
   }
 }
 
-// Barrier between rounds: the warp's when WS (only for a tile whose
-// exchanges are warp-local and whose caller does no CTA-wide staging
-// around the rounds), else the CTA's.
-template <bool WS>
-__device__ __forceinline__ void round_barrier() {
-  if constexpr (WS)
+// Barrier between rounds of kind BK (TileCfg::LOCAL_BARRIER, or 0 for the
+// CTA's).  Named barrier 1 + g serves sub-transform g (barrier 0 is the
+// CTA's); every thread of the group takes it, active or not.
+template <class C, int BK>
+__device__ __forceinline__ void round_barrier(uint32_t tid) {
+  if constexpr (BK == 1) {
     __syncwarp();
-  else
+  } else if constexpr (BK == 2) {
+    asm volatile("bar.sync %0, %1;" ::"r"(1u + C::sub(tid)), "r"((uint32_t)C::GROUP) : "memory");
+  } else {
     __syncthreads();
+  }
 }
 
 // Forward rounds [I, I1) through shared memory, a barrier after each.
-template <class C, int I, int I1, bool WS = false, class W, class PW>
+template <class C, int I, int I1, int BK = 0, class W, class PW>
 __device__ __forceinline__ void fwd_rounds(W* s, uint32_t tid, uint32_t s_off, uint32_t G, const PW* tw, W p,
                                            bool active) {
   if constexpr (I < I1) {
     fwd_round_smem<C, I>(s, tid, s_off, G, tw, p, active);
-    round_barrier<WS>();
-    fwd_rounds<C, I + 1, I1, WS>(s, tid, s_off, G, tw, p, active);
+    round_barrier<C, BK>(tid);
+    fwd_rounds<C, I + 1, I1, BK>(s, tid, s_off, G, tw, p, active);
   }
 }
 
 // Inverse rounds from top-index I down to I1 (exclusive), bottom-up order.
 // The round at top-index 0 carries the scaled last layer when HAS_LAST.
-template <class C, int I, int I1, bool HAS_LAST, bool WS = false, class W, class M>
+template <class C, int I, int I1, bool HAS_LAST, int BK = 0, class W, class M>
 __device__ __forceinline__ void inv_rounds(W* s, uint32_t tid, uint32_t log_n, uint32_t sig_off, uint32_t G,
                                            const M& m, bool active) {
   if constexpr (I > I1) {
     inv_round_smem<C, I, HAS_LAST && I == 0>(s, tid, log_n, sig_off, G, m, active);
-    round_barrier<WS>();
-    inv_rounds<C, I - 1, I1, HAS_LAST, WS>(s, tid, log_n, sig_off, G, m, active);
+    round_barrier<C, BK>(tid);
+    inv_rounds<C, I - 1, I1, HAS_LAST, BK>(s, tid, log_n, sig_off, G, m, active);
   }
 }
 
