@@ -217,6 +217,9 @@ __global__ void __launch_bounds__(C::THREADS) k_ntt_whole(LimbSet ls, const DevM
   if constexpr (DIR != 2) {
     // forward: round 0 straight from HBM when it is not also the last round
     if constexpr (NR > 1) {
+      // barriers over a limb's threads between rounds; the CTA's only before
+      // the cooperative stage-out
+      constexpr int BK = C::LOCAL_BARRIER;
       using RG = Round<C, 0>;
       uint64_t x[1 << C::LOGE];
       const uint32_t b = RG::base(tid);
@@ -225,8 +228,9 @@ __global__ void __launch_bounds__(C::THREADS) k_ntt_whole(LimbSet ls, const DevM
         ct_round<RG>(x, m.fwd, RG::HI, RG::gr(b, 0), m.p);
         smem_store<RG>(x, smem, b);
       }
-      __syncthreads();
-      fwd_rounds<C, 1, NR>(smem, tid, 0, 0, m.fwd, m.p, active);
+      round_barrier<C, BK>(tid);
+      fwd_rounds<C, 1, NR - 1, BK>(smem, tid, 0, 0, m.fwd, m.p, active);
+      fwd_rounds<C, NR - 1, NR>(smem, tid, 0, 0, m.fwd, m.p, active);
     } else {
       stage_in_limbs<C>(smem, as_const(ls), limb0, ls.count, log_n);
       __syncthreads();
@@ -237,7 +241,8 @@ __global__ void __launch_bounds__(C::THREADS) k_ntt_whole(LimbSet ls, const DevM
     stage_in_limbs<C>(smem, as_const(ls), limb0, ls.count, log_n);
     __syncthreads();
     if constexpr (NR > 1) {
-      inv_rounds<C, NR - 1, 0, true>(smem, tid, log_n, 0, 0, m, active);
+      // after the cooperative stage-in, barriers over a limb's threads only
+      inv_rounds<C, NR - 1, 0, true, C::LOCAL_BARRIER>(smem, tid, log_n, 0, 0, m, active);
       using RG = Round<C, 0>;
       uint64_t x[1 << C::LOGE];
       const uint32_t b = RG::base(tid);
@@ -393,13 +398,17 @@ __global__ void __launch_bounds__(C::THREADS) k_row_pass(LimbSet ls, const DevMo
     gload_rows<R0>(x, data, b0);
     ct_round<R0>(x, m.fwd, K1 + R0::HI, R0::gr(b0, G), m.p);
     smem_store<R0>(x, smem, b0);
-    __syncthreads();
-    fwd_rounds<C, 1, NR>(smem, tid, K1, G, m.fwd, m.p, true);
+    // barriers over a row's threads between rounds; the CTA's only before
+    // the cooperative stage-out
+    round_barrier<C, C::LOCAL_BARRIER>(tid);
+    fwd_rounds<C, 1, NR - 1, C::LOCAL_BARRIER>(smem, tid, K1, G, m.fwd, m.p, true);
+    fwd_rounds<C, NR - 1, NR>(smem, tid, K1, G, m.fwd, m.p, true);
     stage_out_region<C>(smem, data, m.p, reduce != 0);
   } else {
     stage_in_region<C>(smem, data);
     __syncthreads();
-    inv_rounds<C, NR - 1, 0, false>(smem, tid, log_n, 0, G, m, true);
+    // after the cooperative stage-in, barriers over a row's threads only
+    inv_rounds<C, NR - 1, 0, false, C::LOCAL_BARRIER>(smem, tid, log_n, 0, G, m, true);
     using RT = Round<C, 0>;
     uint64_t x[1 << C::LOGE];
     const uint32_t bt = RT::base(tid);
