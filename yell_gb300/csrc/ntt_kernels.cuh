@@ -83,6 +83,13 @@ __device__ __forceinline__ void gload_rows(uint64_t* x, const uint64_t* g, uint3
         x[((2 * m) << R) | j] = v.x;
         x[((2 * m + 1) << R) | j] = v.y;
       }
+  } else if constexpr (RG::CONTIG) {
+#pragma unroll
+    for (int j = 0; j < (1 << R); j += 2) {
+      const ulonglong2 v = ld_pair_t<COH>(gb + j);
+      x[j] = v.x;
+      x[j + 1] = v.y;
+    }
   } else {
 #pragma unroll
     for (int ex = 0; ex < RG::E; ++ex)
@@ -101,6 +108,9 @@ __device__ __forceinline__ void gstore_rows(const uint64_t* x, uint64_t* g, uint
 #pragma unroll
       for (int j = 0; j < (1 << R); ++j)
         st_pair(gb + RG::off(2 * m, j), x[((2 * m) << R) | j], x[((2 * m + 1) << R) | j]);
+  } else if constexpr (RG::CONTIG) {
+#pragma unroll
+    for (int j = 0; j < (1 << R); j += 2) st_pair(gb + j, x[j], x[j + 1]);
   } else {
 #pragma unroll
     for (int ex = 0; ex < RG::E; ++ex)
@@ -200,6 +210,12 @@ __host__ __device__ ConstLimbSet as_const(const LimbSet& l) {
   return c;
 }
 
+// Whole-limb NTT tiles holding several limbs (sub-transforms of fewer
+// threads than the CTA, each with its own barrier) move the bottom round
+// between HBM and registers directly; one-limb tiles stage it coalesced.
+template <class C>
+constexpr bool kDirectBottom = C::LOCAL_BARRIER != 0 && C::GROUP < C::THREADS;
+
 // ===========================================================================
 // Whole-limb NTT.  DIR: 0 forward (reduced), 1 forward lazy, 2 backward.
 // ===========================================================================
@@ -217,8 +233,10 @@ __global__ void __launch_bounds__(C::THREADS) k_ntt_whole(LimbSet ls, const DevM
   if constexpr (DIR != 2) {
     // forward: round 0 straight from HBM when it is not also the last round
     if constexpr (NR > 1) {
-      // barriers over a limb's threads between rounds; the CTA's only before
-      // the cooperative stage-out
+      // barriers over a limb's threads between rounds; with one limb per CTA
+      // the CTA's before the cooperative (coalesced) stage-out, with several
+      // the bottom round goes to HBM straight from registers and the CTA
+      // barrier disappears (2^10: 16% faster)
       constexpr int BK = C::LOCAL_BARRIER;
       using RG = Round<C, 0>;
       uint64_t x[1 << C::LOGE];
@@ -230,6 +248,20 @@ __global__ void __launch_bounds__(C::THREADS) k_ntt_whole(LimbSet ls, const DevM
       }
       round_barrier<C, BK>(tid);
       fwd_rounds<C, 1, NR - 1, BK>(smem, tid, 0, 0, m.fwd, m.p, active);
+      if constexpr (kDirectBottom<C>) {
+        using RB = Round<C, NR - 1>;
+        const uint32_t bb = RB::base(tid);
+        if (active) {
+          smem_load<RB>(x, smem, bb);
+          ct_round<RB>(x, m.fwd, RB::HI, RB::gr(bb, 0), m.p);
+          if constexpr (DIR == 0) {
+#pragma unroll
+            for (int i = 0; i < (1 << C::LOGE); ++i) x[i] = fwd_correct(x[i], m.p, m.p << 1);
+          }
+          gstore_rows<RB>(x, ls.limb(my_limb, log_n), bb & umask);
+        }
+        return;
+      }
       fwd_rounds<C, NR - 1, NR>(smem, tid, 0, 0, m.fwd, m.p, active);
     } else {
       stage_in_limbs<C>(smem, as_const(ls), limb0, ls.count, log_n);
@@ -238,11 +270,25 @@ __global__ void __launch_bounds__(C::THREADS) k_ntt_whole(LimbSet ls, const DevM
     }
     stage_out_limbs<C>(smem, ls, limb0, log_n, mods, DIR == 0);
   } else {
-    stage_in_limbs<C>(smem, as_const(ls), limb0, ls.count, log_n);
-    __syncthreads();
     if constexpr (NR > 1) {
-      // after the cooperative stage-in, barriers over a limb's threads only
-      inv_rounds<C, NR - 1, 0, true, C::LOCAL_BARRIER>(smem, tid, log_n, 0, 0, m, active);
+      if constexpr (kDirectBottom<C>) {
+        // several limbs per CTA: the bottom round straight from HBM
+        using RB = Round<C, NR - 1>;
+        uint64_t xb[1 << C::LOGE];
+        const uint32_t bb = RB::base(tid);
+        if (active) {
+          gload_rows<RB>(xb, ls.limb(my_limb, log_n), bb & umask);
+          gs_round<RB, false>(xb, log_n, RB::BETA, RB::gr(bb, 0), m);
+          smem_store<RB>(xb, smem, bb);
+        }
+        round_barrier<C, C::LOCAL_BARRIER>(tid);
+        inv_rounds<C, NR - 2, 0, true, C::LOCAL_BARRIER>(smem, tid, log_n, 0, 0, m, active);
+      } else {
+        // after the cooperative stage-in, barriers over a limb's threads only
+        stage_in_limbs<C>(smem, as_const(ls), limb0, ls.count, log_n);
+        __syncthreads();
+        inv_rounds<C, NR - 1, 0, true, C::LOCAL_BARRIER>(smem, tid, log_n, 0, 0, m, active);
+      }
       using RG = Round<C, 0>;
       uint64_t x[1 << C::LOGE];
       const uint32_t b = RG::base(tid);
@@ -252,6 +298,8 @@ __global__ void __launch_bounds__(C::THREADS) k_ntt_whole(LimbSet ls, const DevM
         gstore_rows<RG>(x, ls.limb(my_limb, log_n), b & umask);
       }
     } else {
+      stage_in_limbs<C>(smem, as_const(ls), limb0, ls.count, log_n);
+      __syncthreads();
       inv_rounds<C, 0, -1, true>(smem, tid, log_n, 0, 0, m, active);
       stage_out_limbs<C>(smem, ls, limb0, log_n, mods, false);
     }

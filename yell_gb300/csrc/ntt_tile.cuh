@@ -94,6 +94,9 @@ struct Round {
   // Adjacent word pairs (ex = 2m, 2m+1) when the extra bits are the tile's
   // lowest bits: moved as one 16-byte access.
   static constexpr bool PAIRS = (LB == 0 && EB >= 1);
+  // The bottom round of a row-type tile: each thread's words are 2^R
+  // consecutive words, moved as 16-byte pairs.
+  static constexpr bool CONTIG = (LB == 0 && EB == 0 && BETA == 0 && R >= 1);
   static_assert(MID >= 0, "round plan broke the extra-bits-below rule");
 
   // Tile index of the thread's element (ex = 0, j = 0): thread id bits fill
