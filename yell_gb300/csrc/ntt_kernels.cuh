@@ -551,8 +551,11 @@ __device__ __forceinline__ void polymul_whole_body(LimbSet c, ConstLimbSet a, Co
   }
 }
 
+// Two 256-thread CTAs per SM (at most 128 registers, a few bytes spilled):
+// left to itself the compiler took 152-158 registers at the 2^12 tile, one
+// CTA per SM, and a 2^12 polymul ran 20% longer.
 template <class C>
-__global__ void __launch_bounds__(C::THREADS) k_polymul_whole(LimbSet c, ConstLimbSet a, ConstLimbSet b,
+__global__ void __launch_bounds__(C::THREADS, C::THREADS <= 256 ? 2 : 1) k_polymul_whole(LimbSet c, ConstLimbSet a, ConstLimbSet b,
                                                               const DevMod* __restrict__ mods) {
   polymul_whole_body<C>(c, a, b, mods, blockIdx.x);
 }
