@@ -219,8 +219,10 @@ constexpr bool kDirectBottom = C::LOCAL_BARRIER != 0 && C::GROUP < C::THREADS;
 // ===========================================================================
 // Whole-limb NTT.  DIR: 0 forward (reduced), 1 forward lazy, 2 backward.
 // ===========================================================================
+// Three 256-thread CTAs per SM (at most 85 registers, a few bytes spilled;
+// the compiler's own choice of up to 106 gave two): 2^12 NTTs 7% faster.
 template <class C, int DIR>
-__global__ void __launch_bounds__(C::THREADS) k_ntt_whole(LimbSet ls, const DevMod* __restrict__ mods) {
+__global__ void __launch_bounds__(C::THREADS, C::THREADS <= 256 ? 3 : 1) k_ntt_whole(LimbSet ls, const DevMod* __restrict__ mods) {
   extern __shared__ __align__(16) uint64_t smem[];
   constexpr int K = C::K, NR = C::NR;
   const uint32_t log_n = K;
@@ -368,9 +370,10 @@ __device__ __forceinline__ void col_pass_body(ConstLimbSet src, LimbSet dst, con
 // N = 2^16, L = 32, 16-pair polymul on GB300) than the inlined body.  The
 // inverse pass waits mostly on its strided column loads: capped at 64
 // registers (a few bytes spilled) it runs four CTAs per SM instead of three,
-// and that polymul takes 1.117 instead of 1.127 ms.
+// and that polymul takes 1.117 instead of 1.127 ms.  The forward pass (NTT
+// calls) fits three CTAs per SM at 80 registers without spilling.
 template <class C, int LOGB, bool INV>
-__global__ void __launch_bounds__(C::THREADS, INV ? 4 : 1) k_col_pass(ConstLimbSet src, LimbSet dst,
+__global__ void __launch_bounds__(C::THREADS, INV ? 4 : 3) k_col_pass(ConstLimbSet src, LimbSet dst,
                                                                       const DevMod* __restrict__ mods) {
   extern __shared__ __align__(16) uint64_t smem[];
   constexpr int K = C::K, LB = C::LB, NR = C::NR;
