@@ -386,7 +386,7 @@ __device__ __forceinline__ void pair_forward(uint32_t* x, const uint32_t* __rest
 }
 
 template <class C>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, 2)
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, C::THREADS <= 256 ? 3 : 2)
     k32_polymul_pair(uint32_t* c, const uint32_t* a, const uint32_t* b, Limbs32 ls,
                      const DevMod32* __restrict__ mods) {
   namespace cg = cooperative_groups;
@@ -453,7 +453,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, 2)
 // In-place NTT of one limb by a CTA pair (DIR: 0 forward, 1 forward lazy,
 // 2 backward), same split as k32_polymul_pair.
 template <class C, int DIR>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, 2)
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, C::THREADS <= 256 ? 3 : 2)
     k32_ntt_pair(uint32_t* data, Limbs32 ls, const DevMod32* __restrict__ mods) {
   namespace cg = cooperative_groups;
   extern __shared__ __align__(16) uint32_t smem32[];
