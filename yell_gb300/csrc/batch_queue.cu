@@ -137,8 +137,6 @@ __global__ void __launch_bounds__(kQueueThreads, 2) k_batch_queue(QueueLaunch q)
 
 }  // namespace
 
-uint32_t queue_k1(uint32_t log_n) { return log_n == 13 ? 6u : (log_n <= 15 ? 7u : 8u); }
-
 size_t queue_smem_bytes() { return 2 * kTileSmemBytes; }
 
 cudaError_t queue_set_attributes() {

@@ -42,11 +42,10 @@ struct QueueLaunch {
   uint32_t grid;
 };
 
-// Degrees served by the queue kernel and the column stages of its two-pass
-// degrees.
+// Degrees served by the queue kernel (the column stages of its two-pass
+// degrees are fixed in batch_queue.cu).
 constexpr uint32_t kQueueMinLogN = 3, kQueueMaxLogN = 20, kQueueFirstTwoPass = 13;
 constexpr uint32_t kQueueTileLog = 12;  // tile words of every item (2^11 at N = 8)
-uint32_t queue_k1(uint32_t log_n);
 
 // Dynamic shared memory of the queue kernel (two 4096-word tiles).
 size_t queue_smem_bytes();

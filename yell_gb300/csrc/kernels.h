@@ -20,8 +20,6 @@ struct NttShape {
 constexpr uint32_t kMinLogN = 3;
 constexpr uint32_t kMaxLogN = 20;
 
-uint32_t default_k1(uint32_t log_n);
-
 // Kernel launches made by this library (for the caller's accounting).
 extern std::atomic<uint64_t> g_kernel_launches;
 

@@ -125,8 +125,6 @@ void select_variant(int device, uint32_t log_n, uint32_t v) {
   g_selected[device][log_n].store((uint8_t)v, std::memory_order_relaxed);
 }
 
-uint32_t default_k1(uint32_t log_n) { return log_n <= 15 ? 7u : 8u; }
-
 cudaError_t init_kernel_attributes() {
   for (uint32_t n = kMinLogN; n <= kMaxLogN; ++n)
     for (const Variant& v : variants_of(n)) {
