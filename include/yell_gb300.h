@@ -18,7 +18,7 @@
  * Degrees: N = 2^log_n with log_n in [3, 20] (yell_min_log_degree() ..
  * yell_max_log_degree()).  The reference's inverse at N = 4 applies its last
  * layer twice (lib/ntt.cpp:174-187 followed by
- * include/yell/details/ntt.hpp:220-228) and is not an inverse, so 4 is
+ * include/yell/details/ntt.hpp:144-159) and is not an inverse, so 4 is
  * rejected with YELL_ERR_UNSUPPORTED_DEGREE.
  *
  * Three families of calls:
@@ -73,6 +73,10 @@ const char* yell_status_string(int status);
 const char* yell_last_error(void);
 /* Number of kernels this library launched so far in this process. */
 uint64_t yell_kernel_launches(void);
+/* Device, pinned-host and memory-pool allocations the library has made in
+ * this process (no counterpart in the reference): a caller that must not
+ * allocate can read it around a call. */
+uint64_t yell_allocations(void);
 
 /* ---- params: replaces yell::params (include/yell/params_64.hpp:19-38) --- */
 uint32_t yell_max_moduli(void);       /* kMaxNbModuli = 1000 (params_64.hpp:19) */
@@ -83,7 +87,7 @@ uint64_t yell_prime_pn(uint32_t cm);       /* params::Pn[cm] (:31)              
 uint64_t yell_primitive_root(uint32_t cm); /* params::primitive_roots[cm] (:34)      */
 
 /* ---- twiddle tables: replaces ntt<N>::init_table / init_ntt_tables -----
- * (include/yell/ntt.hpp:50-56, include/yell/details/ntt.hpp:97-173).  Tables
+ * (include/yell/ntt.hpp:50-56, include/yell/details/ntt.hpp:28-104).  Tables
  * live on the current device for the life of the process, like the
  * reference's per-N singleton.  Other calls build them on first use; calling
  * these first keeps table construction out of later timed or captured work. */
@@ -92,12 +96,12 @@ int yell_init_ntt_tables(uint32_t log_n, uint32_t K); /* cm = 0 .. K-1 */
 int yell_init_ntt_tables_range(uint32_t log_n, uint32_t cm0, uint32_t L); /* cm0 .. cm0+L-1 */
 /* Host copy of one table: out4n = phiTbl, shoupPhiTbl, invphiTbl,
  * shoupInvphiTbl (N words each, bit-reversed); scalars4 = invDegree,
- * shoupInvDegree, invphiInvDegree, shoupInvphiInvDegree (ntt.hpp:35-43). */
+ * shoupInvDegree, invphiInvDegree, shoupInvphiInvDegree (include/yell/ntt.hpp:35-43). */
 int yell_ntt_tables(uint32_t log_n, uint32_t cm, uint64_t* out4n, uint64_t* scalars4);
 
 /* ---- drop-in, one limb in host memory, in place -------------------------
  * Replace yell::ntt<N>::forward / forward_lazy / backward(T* op, size_t cm)
- * (include/yell/ntt.hpp:59-65; details/ntt.hpp:175-235). */
+ * (include/yell/ntt.hpp:59-65; include/yell/details/ntt.hpp:106-166). */
 int yell_ntt_forward(uint64_t* op, uint32_t log_n, uint32_t cm);
 int yell_ntt_forward_lazy(uint64_t* op, uint32_t log_n, uint32_t cm);
 int yell_ntt_backward(uint64_t* op, uint32_t log_n, uint32_t cm);
@@ -161,8 +165,12 @@ int yell_dev_elementwise(int op, uint64_t* d_dst, const uint64_t* d_a, const uin
                          uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0, void* stream);
 /* Fused polymul of `pairs` pairs; d_c may not alias d_a or d_b.  Degrees
  * with a two-pass polymul (N >= 2^13) need scratch of
- * yell_polymul_scratch_words() words; pass NULL to use the library's
- * per-device scratch (grown on demand, serialised by a lock per device). */
+ * yell_polymul_scratch_words() words; pass NULL to have the library take it
+ * stream-ordered from its per-device memory pool on `stream` and give it back
+ * there after the kernels, so the call returns without waiting for the GPU
+ * either way.  pairs * L must fit one launch (YELL_ERR_INVALID_ARGUMENT
+ * otherwise, in particular for any product >= 2^32); scratch_words() returns
+ * 0 for such sizes. */
 size_t yell_polymul_scratch_words(uint32_t pairs, uint32_t L, uint32_t log_n);
 int yell_dev_polymul(uint64_t* d_c, const uint64_t* d_a, const uint64_t* d_b, uint32_t pairs,
                      uint32_t L, uint32_t log_n, uint32_t cm0, uint64_t* d_scratch,
@@ -399,9 +407,10 @@ int yell_synchronize(void);
  * 2^21 / N limbs = pairs * L per call, e.g. 32 limbs at N = 2^16); larger
  * calls return YELL_ERR_INVALID_ARGUMENT, except at 2^13, where they run the
  * whole-limb polymul, which needs no scratch.  The twiddle tables must already be
- * resident (yell_init_ntt_tables_range), since building them allocates.
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture.  All calls share the one array: calls
+ * resident (yell_init_ntt_tables_range), since building them allocates; the
+ * first table build on a device also brings the array up and looks up its
+ * device address, so the array's memory is taken then and no call of this
+ * function allocates or does set-up.  All calls share the one array: calls
  * whose GPU work overlaps (other streams, other host threads) race on it, so
  * order them on one stream.  The array needs no clearing: each call writes
  * the scratch it reads. */

@@ -68,19 +68,19 @@ class ntt {
 
  public:
   static constexpr size_t degree = degree_;
-  // ntt.hpp:50: builds the table of modulus cm (on the GPU, kept for the process).
+  // include/yell/ntt.hpp:50: builds the table of modulus cm (on the GPU, kept for the process).
   static void init_table(size_t cm) { check_status(detail::ntt_init_table(log_n, (uint32_t)cm), "init_table"); }
-  // ntt.hpp:53-56
+  // include/yell/ntt.hpp:53-56
   static void init_ntt_tables(size_t K) {
     check_status(detail::ntt_init_tables(log_n, (uint32_t)K), "init_ntt_tables");
   }
-  // ntt.hpp:59: in place, bit-reversed output in [0, p).
+  // include/yell/ntt.hpp:59: in place, bit-reversed output in [0, p).
   static void forward(T* op, size_t cm) { check_status(detail::ntt_forward(op, log_n, (uint32_t)cm), "forward"); }
-  // ntt.hpp:62: in place, output in [0, 4p).
+  // include/yell/ntt.hpp:62: in place, output in [0, 4p).
   static void forward_lazy(T* op, size_t cm) {
     check_status(detail::ntt_forward_lazy(op, log_n, (uint32_t)cm), "forward_lazy");
   }
-  // ntt.hpp:65: in place, natural-order output in [0, p).
+  // include/yell/ntt.hpp:65: in place, natural-order output in [0, p).
   static void backward(T* op, size_t cm) { check_status(detail::ntt_backward(op, log_n, (uint32_t)cm), "backward"); }
 };
 

@@ -276,7 +276,7 @@ std::ostream& operator<<(std::ostream& os, poly<Degree> const& p) {
   return os << "}";
 }
 
-// poly.hpp:144-156: limb cm viewed as a std::array of N words.
+// include/yell/poly.hpp:144-161: limb cm viewed as a std::array of N words.
 template <typename value_type, size_t degree>
 struct ArrayPointer {
   using T = std::array<value_type, degree>*;

@@ -1,5 +1,5 @@
-// Drop-in for yell/utils/math.hpp (include/yell/utils/math.hpp:5-43 and
-// lib/math.cpp:5-29): the host helpers the reference uses to build tables.
+// Drop-in for yell/utils/math.hpp (include/yell/utils/math.hpp:6-47 and
+// lib/math.cpp:5-27): the host helpers the reference uses to build tables.
 // Header-only; same results, written as plain loops.
 #pragma once
 #include <cstddef>

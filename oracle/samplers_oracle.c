@@ -7,12 +7,12 @@
  * include/yell/details/poly.hpp:195-330), driven by the counter-based stream
  * the GPU samplers use instead of the reference's unseeded Salsa20:
  * random word k of stream s = splitmix64(s + (k + 1) * 0x9E3779B97F4A7C15).
- *   uniform  poly.hpp:200-229  mask to the bit length of p, subtract p once
- *   ZO       poly.hpp:262-275  byte r: r <= rho ? (r & 2 ? p - 1 : 1) : 0
- *   HWT      poly.hpp:282-325  exactly h coefficients +-1 ((rnd & 2) ? 1 : p - 1),
+ *   uniform  include/yell/details/poly.hpp:200-228  mask to the bit length of p, subtract p once
+ *   ZO       include/yell/details/poly.hpp:267-280  byte r: r <= rho ? (r & 2 ? p - 1 : 1) : 0
+ *   HWT      include/yell/details/poly.hpp:287-330  exactly h coefficients +-1 ((rnd & 2) ? 1 : p - 1),
  *                              positions = the indices a keyed Feistel permutation
  *                              maps below h (a pseudorandom h-subset)
- *   gaussian poly.hpp:238-258  e * amplifier, e < 0 ? p + e : e, every limb
+ *   gaussian include/yell/details/poly.hpp:236-260  e * amplifier, e < 0 ? p + e : e, every limb
  * The gaussian integer e is the index of the first cumulative threshold above
  * one random word, thresholds floor(2^64 * CDF) of exp(-e^2 / 2 sigma^2)
  * on |e| <= tail (the stated distribution of lib/prng/FastGaussianNoise.cpp,

@@ -14,7 +14,7 @@
  *   - addmod/submod/mulmod/mulmod_shoup/muladd : include/yell/ops.hpp:46-158
  *   - twiddles     : include/yell/details/ntt.hpp:97-146
  *   - CT/GS butterflies, lazy NTT loops : lib/ntt.cpp:48-210
- *   - forward / forward_lazy / backward : include/yell/details/ntt.hpp:175-235
+ *   - forward / forward_lazy / backward : include/yell/details/ntt.hpp:106-166
  *   - negate       : include/yell/details/poly.hpp:151-157
  *   - add_product_of : include/yell/details/poly.hpp:118-132
  * plus an independent schoolbook negacyclic product in unsigned __int128.
@@ -245,7 +245,7 @@ void orc_mulmod_shoup_n(uint64_t* dst, const uint64_t* a, uint64_t y, size_t n, 
 /* Twiddle tables: include/yell/details/ntt.hpp:97-146.                      */
 /* ------------------------------------------------------------------------ */
 
-/* include/yell/utils/math.hpp:43-56: in-place bit-reversal permutation. */
+/* include/yell/utils/math.hpp:29-43: in-place bit-reversal permutation. */
 static void revbin_permute(uint64_t* a, size_t n) {
   if (n <= 2) return;
   for (size_t i = 1, j = 0; i < n; ++i) {
@@ -284,17 +284,17 @@ static void tables_build(orc_tables* t, uint32_t log_n, uint32_t cm) {
   t->phi_s = t->phi + n;
   t->iphi = t->phi + 2 * n;
   t->iphi_s = t->phi + 3 * n;
-  /* ntt.hpp:108-112: square the 2^21-th root (20 - log2 N) times. */
+  /* include/yell/details/ntt.hpp:39-43: square the 2^21-th root (20 - log2 N) times. */
   uint64_t phi = orc_primitive_root(cm);
   for (uint32_t i = 0; i < ORC_LOG_MAX_DEGREE - log_n; ++i) phi = mulmod(phi, phi, p, pn);
-  /* ntt.hpp:116-122 */
+  /* include/yell/details/ntt.hpp:47-53 */
   uint64_t temp = 1;
   for (size_t i = 0; i < n; ++i) {
     t->phi[i] = temp;
     t->phi_s[i] = shoupify(temp, p);
     temp = mulmod(temp, phi, p, pn);
   }
-  /* ntt.hpp:127-134: phi^N * phi^(N-1) = phi^-1. */
+  /* include/yell/details/ntt.hpp:57-65: phi^N * phi^(N-1) = phi^-1. */
   uint64_t invphi = mulmod(temp, t->phi[n - 1], p, pn);
   temp = 1;
   for (size_t i = 0; i < n; ++i) {
@@ -302,12 +302,12 @@ static void tables_build(orc_tables* t, uint32_t log_n, uint32_t cm) {
     t->iphi_s[i] = shoupify(temp, p);
     temp = mulmod(temp, invphi, p, pn);
   }
-  /* ntt.hpp:137-140 */
+  /* include/yell/details/ntt.hpp:67-71 */
   revbin_permute(t->phi, n);
   revbin_permute(t->phi_s, n);
   revbin_permute(t->iphi, n);
   revbin_permute(t->iphi_s, n);
-  /* ntt.hpp:142-145 */
+  /* include/yell/details/ntt.hpp:73-76 */
   t->inv_n = inv_mod_prime((uint64_t)n, p, pn);
   t->inv_n_iphi = mulmod(t->inv_n, t->iphi[1], p, pn);
   t->inv_n_s = shoupify(t->inv_n, p);
@@ -416,12 +416,12 @@ int orc_negacyclic_backward_lazy(uint64_t* x, uint64_t degree, const uint64_t* w
   return 0;
 }
 
-/* details/ntt.hpp:194-203 */
+/* include/yell/details/ntt.hpp:125-134 */
 static void forward_lazy_t(uint64_t* x, const orc_tables* t) {
   forward_lazy_loop(x, (size_t)1 << t->log_n, t->phi, t->phi_s, t->p);
 }
 
-/* details/ntt.hpp:175-192: lazy forward, then v -= 2p*[v>=2p]; v -= p*[v>=p]. */
+/* include/yell/details/ntt.hpp:106-123: lazy forward, then v -= 2p*[v>=2p]; v -= p*[v>=p]. */
 static void forward_t(uint64_t* x, const orc_tables* t) {
   size_t n = (size_t)1 << t->log_n;
   uint64_t p = t->p, p2 = p << 1;
@@ -434,7 +434,7 @@ static void forward_t(uint64_t* x, const orc_tables* t) {
   }
 }
 
-/* details/ntt.hpp:205-235: lazy GS stages, then the fused last layer. */
+/* include/yell/details/ntt.hpp:136-166: lazy GS stages, then the fused last layer. */
 static void backward_t(uint64_t* x, const orc_tables* t) {
   size_t n = (size_t)1 << t->log_n;
   uint64_t p = t->p, p2 = p << 1;

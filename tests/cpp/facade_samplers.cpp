@@ -81,7 +81,7 @@ int main() {
     if (a != want) return fail("mul_sensitive_poly");
     a.check_vaild_range();
   }
-  // details/poly.hpp:336-354 stream format; poly.hpp:150-156 recast_as_array
+  // include/yell/details/poly.hpp:336-354 stream format; include/yell/poly.hpp:150-161 recast_as_array
   {
     yell::poly<8> t(2);
     for (size_t cm = 0; cm < 2; ++cm)

@@ -71,6 +71,28 @@ def test_argument_errors_without_touching_cuda(ylib):
     assert ylib.yell_status_string(2) == b"unsupported degree"
 
 
+def test_limb_count_overflow_rejected(ylib):
+    """pairs * L (or count * L) beyond what one launch covers, in particular
+    any product >= 2^32, is refused before any CUDA call; no entry point may
+    wrap the product and run a truncated batch."""
+    fake = [0x10000, 0x20000, 0x30000]  # aligned, never dereferenced: the check comes first
+    big = 1 << 31
+    E = _capi.YELL_ERR_INVALID_ARGUMENT
+    assert ylib.yell_dev_polymul(*fake, big, 2, 16, 0, None, 0, None) == E
+    assert b"limbs" in ylib.yell_last_error()
+    assert ylib.yell_dev_polymul(*fake, (1 << 32) - 1, 1000, 10, 0, None, 0, None) == E
+    assert ylib.yell_dev_polymul_noalloc(*fake, big, 2, 16, 0, None) == E
+    assert ylib.yell_dev_ntt(fake[0], big, 4, 12, 0, 0, None) == E
+    assert ylib.yell_dev_elementwise(0, *fake, big, 2, 12, 0, None) == E
+    assert ylib.yell_dev_sample_uniform(fake[0], big, 2, 12, 0, 1, None) == E
+    assert ylib.yell_dev_crt_lift(fake[0], fake[1], big, 2, 12, 0, None) == E
+    # 2^20: one call takes at most (2^31 - 1) >> 8 limbs (4096-word tiles in a grid)
+    assert ylib.yell_dev_polymul(*fake, 1 << 23, 1, 20, 0, None, 0, None) == E
+    assert y.polymul_scratch_words(big, 2, 16) == 0
+    assert y.polymul_scratch_words(1 << 23, 1, 20) == 0
+    assert y.polymul_scratch_words((1 << 23) - 1, 1, 20) == ((1 << 23) - 1) << 20
+
+
 def test_polymul_scratch_sizes(ylib):
     assert y.polymul_scratch_words(16, 32, 12) == 0
     assert y.polymul_scratch_words(16, 32, 13) == 16 * 32 << 13  # two-pass variants at 2^13

@@ -71,6 +71,39 @@ def test_polymul_caller_scratch(cuda, orc):
         y.dev_polymul(c, _dev(torch, a), _dev(torch, b), pairs, L, log_n, 0, scratch=small)
 
 
+def test_polymul_library_scratch_does_not_block(cuda, orc):
+    """Without caller scratch the two-pass polymul takes its scratch
+    stream-ordered from the library's pool: the call returns while the GPU is
+    still busy with it (the stream has work left), and the result equals the
+    caller-scratch path word for word."""
+    torch = cuda
+    log_n, pairs, L = 16, 8, 32
+    ps = y.primes(L)
+    a = uniform_polys(41, pairs, L, log_n, ps)
+    b = uniform_polys(42, pairs, L, log_n, ps)
+    da, db = _dev(torch, a), _dev(torch, b)
+    want = torch.empty(a.size, dtype=torch.int64, device="cuda")
+    scratch = torch.empty(y.polymul_scratch_words(pairs, L, log_n), dtype=torch.int64, device="cuda")
+    stream = torch.cuda.Stream()
+    c = torch.empty(a.size, dtype=torch.int64, device="cuda")
+    with torch.cuda.stream(stream):
+        y.dev_polymul(want, da, db, pairs, L, log_n, 0, scratch=scratch, stream=stream.cuda_stream)
+        y.dev_polymul(c, da, db, pairs, L, log_n, 0, stream=stream.cuda_stream)  # warm the pool
+    stream.synchronize()
+    allocs = y.allocations()
+    with torch.cuda.stream(stream):
+        for _ in range(4):  # several ms of work queued before the checked call
+            y.dev_polymul(want, da, db, pairs, L, log_n, 0, scratch=scratch, stream=stream.cuda_stream)
+        c.fill_(-1)
+        y.dev_polymul(c, da, db, pairs, L, log_n, 0, stream=stream.cuda_stream)
+        busy = not stream.query()
+    stream.synchronize()
+    assert busy, "yell_dev_polymul without scratch waited for the GPU"
+    assert torch.equal(c, want)
+    got = _host(c, a.shape)
+    assert np.array_equal(got[0], orc.polymul(a[0], b[0], log_n, 0))
+
+
 def test_config3_full_size(cuda, orc):
     """N=2^16, L=32 (P[0..31]), 16 pairs, A uniform, B centred discrete
     Gaussian (sigma 3.2, |e| <= 19) mapped per limb: every word of the fused

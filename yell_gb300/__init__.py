@@ -23,7 +23,7 @@ __all__ = [
     "init_ntt_tables", "ntt_tables", "ntt_forward", "ntt_forward_lazy", "ntt_backward",
     "poly_forward", "poly_forward_lazy", "poly_backward", "poly_mulmod", "poly_addmod",
     "poly_submod", "poly_add_product_of", "poly_negate", "polymul_host", "dev_ntt",
-    "dev_ntt_limbs", "dev_elementwise", "dev_polymul", "polymul_scratch_words", "kernel_launches",
+    "dev_ntt_limbs", "dev_elementwise", "dev_polymul", "polymul_scratch_words", "kernel_launches", "allocations",
     "Poly", "PinnedBuffer", "sample_uniform", "sample_zo", "sample_hwt", "sample_gaussian",
     "crt_words", "dev_crt_lift", "poly_to_bigint", "words_to_ints", "DevPoly", "BatchTicket",
     "batch_submit", "dev_polymul_batch_queue", "batch_queue_status", "batch_queue_wait_check",
@@ -71,6 +71,11 @@ def primes(L: int, cm0: int = 0) -> np.ndarray:
 
 def kernel_launches() -> int:
     return int(load().yell_kernel_launches())
+
+
+def allocations() -> int:
+    """Device, pinned-host and pool allocations the library made so far."""
+    return int(load().yell_allocations())
 
 
 # --- tables -----------------------------------------------------------------

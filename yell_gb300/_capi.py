@@ -52,6 +52,7 @@ SIGNATURES = {
     "yell_status_string": (ctypes.c_char_p, [_int]),
     "yell_last_error": (ctypes.c_char_p, []),
     "yell_kernel_launches": (_u64, []),
+    "yell_allocations": (_u64, []),
     "yell_max_moduli": (_u32, []),
     "yell_min_log_degree": (_u32, []),
     "yell_max_log_degree": (_u32, []),

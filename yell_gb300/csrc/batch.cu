@@ -65,9 +65,9 @@ int BatchExecutor::reserve_lists(size_t bytes) {
   h_lists_ = nullptr;
   lists_bytes_ = 0;
   const size_t want = std::max<size_t>(bytes, 1 << 16) * 2;
-  cudaError_t e = cudaMalloc(&d_lists_, want);
+  cudaError_t e = lib_malloc(&d_lists_, want);
   if (e != cudaSuccess) return fail_cuda(e, "cudaMalloc(batch lists)");
-  e = cudaMallocHost(&h_lists_, want);
+  e = lib_malloc_host(&h_lists_, want);
   if (e != cudaSuccess) return fail_cuda(e, "cudaMallocHost(batch lists)");
   lists_bytes_ = want;
   return kOk;
@@ -79,7 +79,7 @@ int BatchExecutor::reserve_scratch(size_t words) {
   if (d_scratch_) cudaFree(d_scratch_);
   d_scratch_ = nullptr;
   scratch_words_ = 0;
-  cudaError_t e = cudaMalloc(&d_scratch_, words * sizeof(uint64_t));
+  cudaError_t e = lib_malloc(&d_scratch_, words * sizeof(uint64_t));
   if (e != cudaSuccess) return fail_cuda(e, "cudaMalloc(batch scratch)");
   scratch_words_ = words;
   return kOk;
@@ -232,7 +232,7 @@ int BatchExecutor::reserve_queue_ctl(size_t words) {
     queue_ctl_words_ = 0;
   }
   const size_t want = std::max<size_t>(words, 4096) * 2;
-  cudaError_t e = cudaMalloc(&d_queue_ctl_, want * sizeof(uint32_t));
+  cudaError_t e = lib_malloc(&d_queue_ctl_, want * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMemset(d_queue_ctl_, 0, want * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMemcpy(d_queue_ctl_, &status, 4, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return fail_cuda(e, "cudaMalloc(queue control)");
@@ -458,6 +458,23 @@ int validate(const yell_polymul_desc& d) {
   return check_moduli(d.cm0, d.L);
 }
 
+// Every entry valid, and the limbs of each degree (one bucket, one launch
+// sequence) within what one launch covers.
+int validate_batch(const yell_polymul_desc* descs, uint32_t n) {
+  uint64_t limbs[kMaxLogN + 1] = {};
+  for (uint32_t i = 0; i < n; ++i) {
+    const int st = validate(descs[i]);
+    if (st != kOk) return st;
+    limbs[descs[i].log_n] += descs[i].L;
+  }
+  for (uint32_t k = kMinLogN; k <= kMaxLogN; ++k) {
+    if (!limbs[k]) continue;
+    const int st = check_limbs(limbs[k], 1, k, nullptr);
+    if (st != kOk) return st;
+  }
+  return kOk;
+}
+
 struct DeviceBatch {
   std::mutex mu;
   BatchExecutor exec;
@@ -488,11 +505,8 @@ DeviceBatch* device_batch(int dev, int* st) {
 
 extern "C" int yell_dev_polymul_batch(const yell_polymul_desc* descs, uint32_t n, void* stream) {
   if (!descs || n == 0) return fail(kInvalidArgument, "empty batch");
-  for (uint32_t i = 0; i < n; ++i) {
-    const int st = validate(descs[i]);
-    if (st != kOk) return st;
-  }
-  int st = kOk;
+  int st = validate_batch(descs, n);
+  if (st != kOk) return st;
   DeviceContext* ctx = DeviceContext::current(&st);
   if (!ctx) return st;
   // tables first (this may allocate and synchronise)
@@ -523,11 +537,8 @@ extern "C" int yell_dev_polymul_batch(const yell_polymul_desc* descs, uint32_t n
 
 extern "C" int yell_dev_polymul_batch_queue(const yell_polymul_desc* descs, uint32_t n, void* stream) {
   if (!descs || n == 0) return fail(kInvalidArgument, "empty batch");
-  for (uint32_t i = 0; i < n; ++i) {
-    const int st = validate(descs[i]);
-    if (st != kOk) return st;
-  }
-  int st = kOk;
+  int st = validate_batch(descs, n);
+  if (st != kOk) return st;
   DeviceContext* ctx = DeviceContext::current(&st);
   if (!ctx) return st;
   for (uint32_t i = 0; i < n; ++i) {

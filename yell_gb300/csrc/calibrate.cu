@@ -97,8 +97,8 @@ extern "C" int yell32_calibrate_butterflies(double* ct_per_s, double* gs_per_s) 
   const int blocks = sms * 8, threads = 256, iters = 400;
   uint2* tw = nullptr;
   uint32_t* out = nullptr;
-  e = cudaMalloc(&tw, sizeof(htw));
-  if (e == cudaSuccess) e = cudaMalloc(&out, (size_t)blocks * threads * 16 * sizeof(uint32_t));
+  e = lib_malloc(&tw, sizeof(htw));
+  if (e == cudaSuccess) e = lib_malloc(&out, (size_t)blocks * threads * 16 * sizeof(uint32_t));
   cudaStream_t strm = ctx->stream();
   if (e == cudaSuccess) e = cudaMemcpyAsync(tw, htw, sizeof(htw), cudaMemcpyHostToDevice, strm);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -149,7 +149,7 @@ extern "C" int yell_calibrate_butterflies(double* ct_per_s, double* gs_per_s) {
   if (e != cudaSuccess) return fail_cuda(e, "cudaMemcpy(DevMod)");
   const int blocks = sms * 8, threads = 256, iters = 200;
   uint64_t* out = nullptr;
-  e = cudaMalloc(&out, (size_t)blocks * threads * 16 * sizeof(uint64_t));
+  e = lib_malloc(&out, (size_t)blocks * threads * 16 * sizeof(uint64_t));
   if (e != cudaSuccess) return fail_cuda(e, "cudaMalloc(calibration)");
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);

@@ -189,6 +189,8 @@ const char* yell_status_string(int status) {
 const char* yell_last_error(void) { return last_error(); }
 uint64_t yell_kernel_launches(void) { return g_kernel_launches.load(); }
 
+uint64_t yell_allocations(void) { return g_allocations.load(); }
+
 uint32_t yell_max_moduli(void) { return kMaxModuli; }
 uint32_t yell_min_log_degree(void) { return kMinLogN; }
 uint32_t yell_max_log_degree(void) { return kMaxLogN; }
@@ -259,7 +261,7 @@ int yell_poly_negate(uint64_t* const* limbs, uint32_t L, uint32_t log_n) {
 
 void* yell_host_alloc(size_t bytes) {
   void* p = nullptr;
-  if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+  if (lib_malloc_host(&p, bytes) != cudaSuccess) return nullptr;
   return p;
 }
 
@@ -279,6 +281,7 @@ int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_
   if (pairs == 0) return fail(kInvalidArgument, "pairs is 0");
   YELL_TRY(check_degree(log_n));
   YELL_TRY(check_moduli(cm0, L));
+  YELL_TRY(check_limbs(pairs, L, log_n, nullptr));
   DeviceContext* ctx;
   YELL_TRY(get_ctx(&ctx));
   const DevMod* mods;
@@ -351,11 +354,13 @@ int yell_dev_ntt(uint64_t* d_polys, uint32_t count, uint32_t L, uint32_t log_n, 
   YELL_TRY(check_aligned(d_polys, "d_polys"));
   YELL_TRY(check_degree(log_n));
   YELL_TRY(check_moduli(cm0, L));
+  uint32_t limbs;
+  YELL_TRY(check_limbs(count, L, log_n, &limbs));
   DeviceContext* ctx;
   YELL_TRY(get_ctx(&ctx));
   const DevMod* mods;
   YELL_TRY(ctx->ensure_tables(log_n, cm0, L, &mods));
-  YELL_CUDA(launch_ntt(contiguous(d_polys, count * L, L, cm0), log_n, mods, to_dir(direction),
+  YELL_CUDA(launch_ntt(contiguous(d_polys, limbs, L, cm0), log_n, mods, to_dir(direction),
                        ctx->shape, pick_stream(ctx, stream)),
             "launch ntt");
   return kOk;
@@ -407,22 +412,26 @@ int yell_dev_elementwise(int op, uint64_t* d_dst, const uint64_t* d_a, const uin
   if (d_b) YELL_TRY(check_aligned(d_b, "d_b"));
   YELL_TRY(check_degree(log_n));
   YELL_TRY(check_moduli(cm0, L));
+  uint32_t limbs;
+  YELL_TRY(check_limbs(count, L, log_n, &limbs));
   DeviceContext* ctx;
   YELL_TRY(get_ctx(&ctx));
   const DevMod* mods;
   YELL_TRY(ctx->ensure_tables(log_n, cm0, L, &mods));
-  YELL_CUDA(launch_elementwise(static_cast<EwOp>(op), contiguous(d_dst, count * L, L, cm0),
-                               const_contiguous(d_a, count * L, L, cm0),
-                               const_contiguous(d_b ? d_b : d_a, count * L, L, cm0), log_n, mods,
+  YELL_CUDA(launch_elementwise(static_cast<EwOp>(op), contiguous(d_dst, limbs, L, cm0),
+                               const_contiguous(d_a, limbs, L, cm0),
+                               const_contiguous(d_b ? d_b : d_a, limbs, L, cm0), log_n, mods,
                                pick_stream(ctx, stream)),
             "launch elementwise");
   return kOk;
 }
 
 size_t yell_polymul_scratch_words(uint32_t pairs, uint32_t L, uint32_t log_n) {
-  if (log_n < kMinLogN || log_n > kMaxLogN) return 0;
+  uint32_t limbs;
+  if (log_n < kMinLogN || log_n > kMaxLogN || L == 0 || L > kMaxModuli) return 0;
+  if (check_limbs(pairs, L, log_n, &limbs) != kOk) return 0;
   NttShape shape;
-  return polymul_scratch_words(pairs * L, log_n, shape);
+  return polymul_scratch_words(limbs, log_n, shape);
 }
 
 int yell_dev_polymul(uint64_t* d_c, const uint64_t* d_a, const uint64_t* d_b, uint32_t pairs,
@@ -436,11 +445,12 @@ int yell_dev_polymul(uint64_t* d_c, const uint64_t* d_a, const uint64_t* d_b, ui
   if (d_scratch) YELL_TRY(check_aligned(d_scratch, "d_scratch"));
   YELL_TRY(check_degree(log_n));
   YELL_TRY(check_moduli(cm0, L));
+  uint32_t count;
+  YELL_TRY(check_limbs(pairs, L, log_n, &count));
   DeviceContext* ctx;
   YELL_TRY(get_ctx(&ctx));
   const DevMod* mods;
   YELL_TRY(ctx->ensure_tables(log_n, cm0, L, &mods));
-  const uint32_t count = pairs * L;
   const size_t need = polymul_scratch_words(count, log_n, ctx->shape);
   cudaStream_t st = pick_stream(ctx, stream);
   if (need == 0 || d_scratch) {
@@ -453,15 +463,15 @@ int yell_dev_polymul(uint64_t* d_c, const uint64_t* d_a, const uint64_t* d_b, ui
               "launch polymul");
     return kOk;
   }
-  // Library scratch: the lock is held until the work using it completes.
-  std::lock_guard<std::mutex> g(ctx->scratch.lock);
-  YELL_TRY(ctx->scratch.reserve(need));
-  YELL_CUDA(launch_polymul(contiguous(d_c, count, L, cm0), const_contiguous(d_a, count, L, cm0),
-                           const_contiguous(d_b, count, L, cm0), log_n, mods, ctx->scratch.ptr,
-                           ctx->shape, st),
-            "launch polymul");
-  YELL_CUDA(cudaStreamSynchronize(st), "synchronize");
-  return kOk;
+  // Library scratch, stream-ordered: allocated and freed on `st` around the
+  // launches, so the call does not wait for the GPU.
+  uint64_t* scratch = nullptr;
+  YELL_TRY(ctx->scratch_alloc_async(need, st, &scratch));
+  const cudaError_t le = launch_polymul(contiguous(d_c, count, L, cm0), const_contiguous(d_a, count, L, cm0),
+                                        const_contiguous(d_b, count, L, cm0), log_n, mods, scratch, ctx->shape, st);
+  const int fs = ctx->scratch_free_async(scratch, st);
+  if (le != cudaSuccess) return fail_cuda(le, "launch polymul");
+  return fs;
 }
 
 int yell_profile_start(void) { return profile_start() == 0 ? kOk : fail(kCudaError, "profile start"); }

@@ -13,15 +13,15 @@ namespace yell_gb300 {
 
 // Per-(log_n, cm) constants resident on the device.  fwd/inv point at N
 // {w, w'} pairs in the reference's bit-reversed order
-// (include/yell/details/ntt.hpp:114-140): fwd = phiTbl/shoupPhiTbl,
+// (include/yell/details/ntt.hpp:45-71): fwd = phiTbl/shoupPhiTbl,
 // inv = invphiTbl/shoupInvphiTbl.
 struct alignas(16) DevMod {
   const ulonglong2* fwd;
   const ulonglong2* inv;
   uint64_t p;
   uint64_t pn;               // low word of floor(2^128/p) (params_64.hpp:29-31)
-  uint64_t inv_n, inv_n_s;   // N^-1 and its Shoup form (ntt.hpp:142-144)
-  uint64_t inv_n_iphi, inv_n_iphi_s;  // N^-1 * invphiTbl[1] and Shoup form (ntt.hpp:143-145)
+  uint64_t inv_n, inv_n_s;   // N^-1 and its Shoup form (include/yell/details/ntt.hpp:73,75)
+  uint64_t inv_n_iphi, inv_n_iphi_s;  // N^-1 * invphiTbl[1] and Shoup form (include/yell/details/ntt.hpp:74,76)
 };
 
 // Which limbs a launch touches.  Limb k of the launch lives at
@@ -178,14 +178,14 @@ __device__ __forceinline__ uint64_t mulmod_shoup(uint64_t x, uint64_t y, uint64_
 }
 
 // Last inverse layer with the N^-1 scaling fused in,
-// include/yell/details/ntt.hpp:220-228.
+// include/yell/details/ntt.hpp:144-159.
 __device__ __forceinline__ void gs_last(uint64_t& x0, uint64_t& x1, const DevMod& m) {
   const uint64_t u = x0, v = x1;
   x0 = mulmod_shoup(u + v, m.inv_n, m.inv_n_s, m.p);
   x1 = mulmod_shoup(u - v + (m.p << 1), m.inv_n_iphi, m.inv_n_iphi_s, m.p);
 }
 
-// Final correction of ntt<N>::forward, include/yell/details/ntt.hpp:179-187:
+// Final correction of ntt<N>::forward, include/yell/details/ntt.hpp:111-118:
 // v -= 2p if v >= 2p; v -= p if v >= p.
 __device__ __forceinline__ uint64_t fwd_correct(uint64_t v, uint64_t p, uint64_t p2) {
   return csub(csub(v, p2), p);

@@ -113,9 +113,9 @@ int build_crt_tables(uint32_t cm0, uint32_t L, CrtTables* t) {
     mods[j].c = (uint64_t)(((u128)1 << 125) / q);
     for (size_t w = 0; w < m.size(); ++w) cof[(size_t)j * W + w] = m[w];
   }
-  cudaError_t e = cudaMalloc(&t->mods, L * sizeof(CrtConst));
-  if (e == cudaSuccess) e = cudaMalloc(&t->cofactors, cof.size() * 8);
-  if (e == cudaSuccess) e = cudaMalloc(&t->q, (size_t)W * 8);
+  cudaError_t e = lib_malloc(&t->mods, L * sizeof(CrtConst));
+  if (e == cudaSuccess) e = lib_malloc(&t->cofactors, cof.size() * 8);
+  if (e == cudaSuccess) e = lib_malloc(&t->q, (size_t)W * 8);
   if (e == cudaSuccess) e = cudaMemcpy(t->mods, mods.data(), L * sizeof(CrtConst), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(t->cofactors, cof.data(), cof.size() * 8, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(t->q, Q.data(), (size_t)W * 8, cudaMemcpyHostToDevice);
@@ -355,6 +355,8 @@ int yell_dev_crt_lift(uint64_t* d_out, const uint64_t* d_in, uint32_t count, uin
                       uint32_t cm0, void* stream) {
   if (!d_out || !d_in || count == 0) return fail(kInvalidArgument, "null pointer or zero count");
   int st = check_crt_args(L, log_n, cm0);
+  if (st != kOk) return st;
+  st = check_limbs(count, L, log_n, nullptr);
   if (st != kOk) return st;
   DeviceContext* ctx = DeviceContext::current(&st);
   if (!ctx) return st;

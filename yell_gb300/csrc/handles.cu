@@ -69,7 +69,7 @@ int yell_dev_poly_alloc(uint32_t L, uint32_t log_n, uint32_t cm0, yell_dev_poly*
   p->log_n = log_n;
   p->cm0 = cm0;
   p->device = ctx->device();
-  const cudaError_t e = cudaMalloc(&p->data, ((size_t)L << log_n) * sizeof(uint64_t));
+  const cudaError_t e = lib_malloc(&p->data, ((size_t)L << log_n) * sizeof(uint64_t));
   if (e != cudaSuccess) {
     delete p;
     return e == cudaErrorMemoryAllocation ? fail(kOutOfMemory, "cudaMalloc(poly)") : fail_cuda(e, "cudaMalloc(poly)");

@@ -23,6 +23,41 @@ constexpr uint32_t kMaxLogN = 20;
 // Kernel launches made by this library (for the caller's accounting).
 extern std::atomic<uint64_t> g_kernel_launches;
 
+// Device and pinned-host allocations made by this library.  Every allocation
+// goes through these wrappers, so the count covers all of them.
+extern std::atomic<uint64_t> g_allocations;
+template <class T>
+cudaError_t lib_malloc(T** p, size_t bytes) {
+  void* v = nullptr;
+  const cudaError_t e = cudaMalloc(&v, bytes);
+  if (e == cudaSuccess) {
+    *p = static_cast<T*>(v);
+    g_allocations += 1;
+  }
+  return e;
+}
+template <class T>
+cudaError_t lib_malloc_host(T** p, size_t bytes, unsigned flags = cudaHostAllocDefault) {
+  void* v = nullptr;
+  const cudaError_t e = cudaHostAlloc(&v, bytes, flags);
+  if (e == cudaSuccess) {
+    *p = static_cast<T*>(v);
+    g_allocations += 1;
+  }
+  return e;
+}
+// Stream-ordered allocation from a memory pool (counted like the others).
+template <class T>
+cudaError_t lib_malloc_async(T** p, size_t bytes, cudaMemPool_t pool, cudaStream_t st) {
+  void* v = nullptr;
+  const cudaError_t e = cudaMallocFromPoolAsync(&v, bytes, pool, st);
+  if (e == cudaSuccess) {
+    *p = static_cast<T*>(v);
+    g_allocations += 1;
+  }
+  return e;
+}
+
 // In-place NTT over every limb of `ls`.  mods: the DevMod array of this
 // degree, indexed by modulus index.
 cudaError_t launch_ntt(const LimbSet& ls, uint32_t log_n, const DevMod* mods, NttDir dir,

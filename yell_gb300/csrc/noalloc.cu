@@ -33,21 +33,30 @@ static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocScratchWords
 std::mutex g_addr_mu;
 uint64_t* g_addr[64] = {};
 
-int scratch_address(int dev, uint64_t** out) {
+int aligned16(const void* p) { return reinterpret_cast<uintptr_t>(p) % 16 == 0; }
+
+}  // namespace
+
+// The lookup loads the module that holds the array, which is when the array
+// takes its device memory.  DeviceContext::ensure_tables_list calls this the
+// first time it builds tables on a device, so the memory is taken while
+// tables are being allocated anyway, never inside yell_dev_polymul_noalloc.
+int yell_gb300::noalloc_prepare(int dev) {
   std::lock_guard<std::mutex> g(g_addr_mu);
+  if (dev < 0 || dev >= 64) return fail(kInvalidArgument, "device index out of range");
   if (!g_addr[dev]) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return fail_cuda(e, "cudaGetSymbolAddress(noalloc scratch)");
     g_addr[dev] = static_cast<uint64_t*>(p);
   }
-  *out = g_addr[dev];
   return kOk;
 }
 
-int aligned16(const void* p) { return reinterpret_cast<uintptr_t>(p) % 16 == 0; }
-
-}  // namespace
+uint64_t* yell_gb300::noalloc_scratch(int dev) {
+  std::lock_guard<std::mutex> g(g_addr_mu);
+  return (dev >= 0 && dev < 64) ? g_addr[dev] : nullptr;
+}
 
 extern "C" int yell_dev_polymul_noalloc(uint64_t* d_c, const uint64_t* d_a, const uint64_t* d_b,
                                         uint32_t pairs, uint32_t L, uint32_t log_n, uint32_t cm0,
@@ -60,10 +69,12 @@ extern "C" int yell_dev_polymul_noalloc(uint64_t* d_c, const uint64_t* d_a, cons
   if (st != kOk) return st;
   st = check_moduli(cm0, L);
   if (st != kOk) return st;
-  const size_t count = (size_t)pairs * L;
+  uint32_t count = 0;
+  st = check_limbs(pairs, L, log_n, &count);
+  if (st != kOk) return st;
   DeviceContext* ctx = DeviceContext::current(&st);
   if (!ctx) return st;
-  size_t need = polymul_scratch_words((uint32_t)count, log_n, ctx->shape);
+  size_t need = polymul_scratch_words(count, log_n, ctx->shape);
   if (need > kNoAllocScratchWords && polymul_scratch_optional(log_n)) need = 0;  // scratch-free variant
   if (need > kNoAllocScratchWords)
     return fail(kInvalidArgument,
@@ -77,21 +88,22 @@ extern "C" int yell_dev_polymul_noalloc(uint64_t* d_c, const uint64_t* d_a, cons
     return fail(kInvalidArgument, "twiddle tables for degree 2^" + std::to_string(log_n) + ", moduli " +
                                       std::to_string(cm0) + ".." + std::to_string(cm0 + L - 1) +
                                       " are not resident: call yell_init_ntt_tables_range first");
+  // The array was brought up when the tables were built (noalloc_prepare).
   uint64_t* scratch = nullptr;
   if (need) {
-    st = scratch_address(ctx->device(), &scratch);
-    if (st != kOk) return st;
+    scratch = noalloc_scratch(ctx->device());
+    if (!scratch) return fail(kCudaError, "fixed scratch array of this device was not brought up");
   }
   LimbSet c;
   c.base = d_c;
   c.ptrs = nullptr;
   c.cms = nullptr;
-  c.count = (uint32_t)count;
+  c.count = count;
   c.L = L;
   c.cm0 = cm0;
   c.pad_ = 0;
-  ConstLimbSet a{d_a, nullptr, nullptr, (uint32_t)count, L, cm0, 0};
-  ConstLimbSet b{d_b, nullptr, nullptr, (uint32_t)count, L, cm0, 0};
+  ConstLimbSet a{d_a, nullptr, nullptr, count, L, cm0, 0};
+  ConstLimbSet b{d_b, nullptr, nullptr, count, L, cm0, 0};
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream();
   const cudaError_t e = launch_polymul(c, a, b, log_n, mods, scratch, ctx->shape, s);
   if (e != cudaSuccess) return fail_cuda(e, "launch polymul (noalloc)");

@@ -155,7 +155,7 @@ int ensure32(int device, uint32_t log_n, uint32_t cm0, uint32_t L, const DevMod3
   if (built.empty()) built.assign(kMaxModuli32, 0);
   cudaError_t e;
   if (!t.mods[log_n]) {
-    e = cudaMalloc(&t.mods[log_n], kMaxModuli32 * sizeof(DevMod32));
+    e = lib_malloc(&t.mods[log_n], kMaxModuli32 * sizeof(DevMod32));
     if (e != cudaSuccess) {
       t.mods[log_n] = nullptr;
       return fail_cuda(e, "cudaMalloc(DevMod32 table)");
@@ -176,7 +176,7 @@ int ensure32(int device, uint32_t log_n, uint32_t cm0, uint32_t L, const DevMod3
       packed[2 * (size_t)n + 2 * k + 1] = host[3 * n + k];
     }
     uint32_t* d = nullptr;
-    e = cudaMalloc(&d, packed.size() * sizeof(uint32_t));
+    e = lib_malloc(&d, packed.size() * sizeof(uint32_t));
     if (e != cudaSuccess) return fail_cuda(e, "cudaMalloc(twiddles32)");
     e = cudaMemcpy(d, packed.data(), packed.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return fail_cuda(e, "upload twiddles32");
@@ -621,7 +621,9 @@ int run32(int kind, uint32_t* c, const uint32_t* a, const uint32_t* b, uint32_t 
           uint32_t cm0, void* stream) {
   DeviceContext* ctx;
   const DevMod32* mods;
-  int st = prepare32(log_n, cm0, L, &ctx, &mods);
+  int st = check_limbs(count, L, log_n, nullptr);
+  if (st != kOk) return st;
+  st = prepare32(log_n, cm0, L, &ctx, &mods);
   if (st != kOk) return st;
   if ((st = aligned16(c, "output")) != kOk) return st;
   if (a && (st = aligned16(a, "a")) != kOk) return st;
@@ -723,7 +725,9 @@ int yell32_dev_elementwise(int op, uint32_t* d_dst, const uint32_t* d_a, const u
   if (op < YELL_OP_MULMOD || op > YELL_OP_NEGATE) return fail(kInvalidArgument, "bad op");
   DeviceContext* ctx;
   const DevMod32* mods;
-  int st = prepare32(log_n, cm0, L, &ctx, &mods);
+  int st = check_limbs(count, L, log_n, nullptr);
+  if (st != kOk) return st;
+  st = prepare32(log_n, cm0, L, &ctx, &mods);
   if (st != kOk) return st;
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream();
   const size_t total = ((size_t)count * L) << log_n;
@@ -744,7 +748,7 @@ int yell32_dev_elementwise(int op, uint32_t* d_dst, const uint32_t* d_a, const u
 
 // ---- host-memory poly<N> drop-ins (limb pointer arrays, moduli 0 .. L-1) ----
 // The reference's poly<N> members in 32-bit mode (details/poly.hpp:118-186 and
-// the operators of poly.hpp:163-168): limbs staged through device memory,
+// the operators of include/yell/poly.hpp:163-168): limbs staged through device memory,
 // one launch over all limbs, copied back; synchronous.
 
 static int host_poly32(int kind, int op, uint32_t* const* dst, const uint32_t* const* a, const uint32_t* const* b,

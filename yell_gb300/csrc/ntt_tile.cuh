@@ -300,7 +300,7 @@ __device__ __forceinline__ void ct_stages2(W* x, W* y, const PW* __restrict__ tw
 // Inverse sub-stage k pairs (j, j + 2^k) with twiddle
 // w[2^(log_n-1-sigma_first-k) + (gr << (R-1-k)) + (j >> (k+1))].  With
 // LAST, the round's final sub-stage is the reference's last layer with the
-// N^-1 scaling fused (include/yell/details/ntt.hpp:220-228).
+// N^-1 scaling fused (include/yell/details/ntt.hpp:144-159).
 // top = log_n - 1 - sigma_first, so sub-stage k uses m = 2^(top - k).
 template <int R, int E, bool LAST, int k, class W, class PW, class M>
 __device__ __forceinline__ void gs_stages(W* x, const PW* __restrict__ itw, uint32_t top, uint32_t gr,

@@ -50,6 +50,7 @@ inline uint32_t bit_reverse(uint32_t x, uint32_t bits) {
 }  // namespace
 
 std::atomic<uint64_t> g_kernel_launches{0};
+std::atomic<uint64_t> g_allocations{0};
 
 const PrimeEntry& prime_entry(uint32_t cm) { return kPrimes[cm]; }
 
@@ -83,16 +84,31 @@ int check_moduli(uint32_t cm0, uint32_t L) {
   return kOk;
 }
 
+int check_limbs(uint64_t count, uint32_t L, uint32_t log_n, uint32_t* limbs) {
+  if (count == 0) return fail(kInvalidArgument, "zero polys or pairs");
+  const uint64_t total = count * (uint64_t)L;  // count < 2^32, L <= kMaxModuli: no wrap
+  // One launch covers every limb: the grid (limbs, or 4096-word tiles of
+  // larger limbs) must stay below 2^31 blocks.
+  const uint32_t shift = log_n > 12 ? log_n - 12 : 0;
+  const uint64_t max_limbs = ((uint64_t(1) << 31) - 1) >> shift;
+  if (total > max_limbs)
+    return fail(kInvalidArgument, std::to_string(count) + " x " + std::to_string(L) + " = " +
+                                      std::to_string(total) + " limbs of degree 2^" + std::to_string(log_n) +
+                                      " exceed the " + std::to_string(max_limbs) + " one call can take");
+  if (limbs) *limbs = (uint32_t)total;
+  return kOk;
+}
+
 // The values are the reference's (include/yell/details/ntt.hpp:97-146); they
 // are canonical residues, so exact u128 arithmetic reproduces them.
 void build_host_tables(uint32_t log_n, uint32_t cm, uint64_t* out4n, uint64_t* sc4) {
   const PrimeEntry& pe = kPrimes[cm];
   const uint64_t p = pe.p;
   const uint32_t n = 1u << log_n;
-  // ntt.hpp:108-112: psi = root^(2^(20 - log_n)), a primitive 2N-th root.
+  // include/yell/details/ntt.hpp:39-43: psi = root^(2^(20 - log_n)), a primitive 2N-th root.
   uint64_t psi = pe.root;
   for (uint32_t i = 0; i < kLogMaxDegree - log_n; ++i) psi = mulmod_exact(psi, psi, p);
-  // ntt.hpp:127: invphi = psi^N * psi^(N-1) = psi^(2N-1).
+  // include/yell/details/ntt.hpp:57-58: invphi = psi^N * psi^(N-1) = psi^(2N-1).
   const uint64_t ipsi = powmod(psi, 2ull * n - 1, p);
   uint64_t* phi = out4n;
   uint64_t* phi_s = out4n + n;
@@ -100,7 +116,7 @@ void build_host_tables(uint32_t log_n, uint32_t cm, uint64_t* out4n, uint64_t* s
   uint64_t* iphi_s = out4n + 3 * (size_t)n;
   uint64_t a = 1, b = 1;
   for (uint32_t i = 0; i < n; ++i) {
-    // ntt.hpp:116-140: powers, Shoup forms, then bit-reversed order.
+    // include/yell/details/ntt.hpp:45-71: powers, Shoup forms, then bit-reversed order.
     const uint32_t r = bit_reverse(i, log_n);
     phi[r] = a;
     phi_s[r] = shoupify(a, p);
@@ -109,7 +125,7 @@ void build_host_tables(uint32_t log_n, uint32_t cm, uint64_t* out4n, uint64_t* s
     a = mulmod_exact(a, psi, p);
     b = mulmod_exact(b, ipsi, p);
   }
-  // ntt.hpp:142-145
+  // include/yell/details/ntt.hpp:73-76
   const uint64_t inv_n = powmod(n % p, p - 2, p);
   const uint64_t inv_n_iphi = mulmod_exact(inv_n, iphi[1], p);
   sc4[0] = inv_n;
@@ -133,7 +149,7 @@ int DeviceContext::Buffer::reserve(size_t w) {
     words = 0;
     if (e != cudaSuccess) return fail_cuda(e, "cudaFree(buffer)");
   }
-  cudaError_t e = cudaMalloc(&ptr, w * sizeof(uint64_t));
+  cudaError_t e = lib_malloc(&ptr, w * sizeof(uint64_t));
   if (e != cudaSuccess) {
     ptr = nullptr;
     return fail_cuda(e, "cudaMalloc(buffer)");
@@ -145,7 +161,7 @@ int DeviceContext::Buffer::reserve(size_t w) {
 int DeviceContext::HostMapped::ensure() {
   if (host) return kOk;
   void* h = nullptr;
-  cudaError_t e = cudaHostAlloc(&h, 3 * kSmallCallWords * sizeof(uint64_t), cudaHostAllocMapped);
+  cudaError_t e = lib_malloc_host(&h, 3 * kSmallCallWords * sizeof(uint64_t), cudaHostAllocMapped);
   if (e != cudaSuccess) return fail_cuda(e, "cudaHostAlloc(small-call buffer)");
   void* d = nullptr;
   e = cudaHostGetDevicePointer(&d, h, 0);
@@ -159,6 +175,20 @@ int DeviceContext::HostMapped::ensure() {
 }
 
 DeviceContext::DeviceContext(int device) : device_(device) {}
+
+int DeviceContext::scratch_alloc_async(size_t words, cudaStream_t st, uint64_t** out) {
+  const cudaError_t e = lib_malloc_async(out, words * sizeof(uint64_t), pool_, st);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    return fail_cuda(e, "cudaMallocFromPoolAsync(polymul scratch)");
+  }
+  return kOk;
+}
+
+int DeviceContext::scratch_free_async(uint64_t* p, cudaStream_t st) {
+  const cudaError_t e = cudaFreeAsync(p, st);
+  return e == cudaSuccess ? kOk : fail_cuda(e, "cudaFreeAsync(polymul scratch)");
+}
 
 int DeviceContext::init() {
   cudaError_t e = cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking);
@@ -174,6 +204,15 @@ int DeviceContext::init() {
       if (e != cudaSuccess) return fail_cuda(e, "cudaEventCreate(pipe)");
     }
   }
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device_;
+  e = cudaMemPoolCreate(&pool_, &props);
+  if (e != cudaSuccess) return fail_cuda(e, "cudaMemPoolCreate");
+  uint64_t keep = ~uint64_t(0);
+  e = cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep);
+  if (e != cudaSuccess) return fail_cuda(e, "cudaMemPoolSetAttribute");
   e = init_kernel_attributes();
   if (e != cudaSuccess) return fail_cuda(e, "cudaFuncSetAttribute");
   load_tuning(device_);
@@ -241,9 +280,13 @@ int DeviceContext::ensure_tables_list(uint32_t log_n, const uint32_t* cms, uint3
     return kOk;
   }
   for (uint32_t cm : missing) built[cm] = 0;
+  // Tables are built only here, and yell_dev_polymul_noalloc requires them:
+  // bring up its fixed scratch array now, while allocating is allowed.
+  const int nst = noalloc_prepare(device_);
+  if (nst != kOk) return nst;
   cudaError_t e;
   if (!d_mods_[log_n]) {
-    e = cudaMalloc(&d_mods_[log_n], kMaxModuli * sizeof(DevMod));
+    e = lib_malloc(&d_mods_[log_n], kMaxModuli * sizeof(DevMod));
     if (e != cudaSuccess) {
       d_mods_[log_n] = nullptr;
       return fail_cuda(e, "cudaMalloc(DevMod table)");
@@ -282,7 +325,7 @@ int DeviceContext::ensure_tables_list(uint32_t log_n, const uint32_t* cms, uint3
       packed[2 * (size_t)nwords + 2 * (size_t)k + 1] = t[3 * (size_t)nwords + k];
     }
     void* dtab = nullptr;
-    e = cudaMalloc(&dtab, packed.size() * sizeof(uint64_t));
+    e = lib_malloc(&dtab, packed.size() * sizeof(uint64_t));
     if (e != cudaSuccess) return fail_cuda(e, "cudaMalloc(twiddle table)");
     table_allocs_.push_back(dtab);
     e = cudaMemcpy(dtab, packed.data(), packed.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);

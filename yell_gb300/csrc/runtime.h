@@ -48,9 +48,20 @@ void load_tuning(int device);
 // Argument checks shared by the entry points.
 int check_degree(uint32_t log_n);
 int check_moduli(uint32_t cm0, uint32_t L);
+// count polys (or pairs) of L limbs each: rejects a zero count and a limb
+// total of one call that would not fit its launch grid (in particular any
+// count * L >= 2^32).  On success *limbs = count * L (when limbs != nullptr).
+int check_limbs(uint64_t count, uint32_t L, uint32_t log_n, uint32_t* limbs);
+
+// Looks up, once per device, the device address of the fixed scratch array
+// of yell_dev_polymul_noalloc (which loads the module holding it, so the
+// array is in device memory from then on).  Called with that device current.
+int noalloc_prepare(int device);
+// The address noalloc_prepare found for `device`, or nullptr.
+uint64_t* noalloc_scratch(int device);
 
 // Builds the reference's tables for (log_n, cm) on the host
-// (include/yell/details/ntt.hpp:97-146): out4n = phi, phi', invphi, invphi'
+// (include/yell/details/ntt.hpp:28-77): out4n = phi, phi', invphi, invphi'
 // (N words each, bit-reversed); sc4 = N^-1, (N^-1)', N^-1*invphi[1], its '.
 void build_host_tables(uint32_t log_n, uint32_t cm, uint64_t* out4n, uint64_t* sc4);
 
@@ -83,8 +94,17 @@ class DeviceContext {
     int reserve(size_t words);  // under lock
     ~Buffer();
   };
-  Buffer scratch;   // polymul scratch for device-resident calls
   Buffer staging;   // host-pointer drop-ins: operands / results
+
+  // Stream-ordered scratch for device-resident calls made without caller
+  // scratch: taken from this context's memory pool on the caller's stream
+  // and given back on that stream after the kernels that use it, so the call
+  // returns before its work completes and concurrent calls on different
+  // streams each get their own.  The pool keeps freed memory for reuse (no
+  // release threshold), so after the first call of a size no memory is
+  // obtained from the driver.
+  int scratch_alloc_async(size_t words, cudaStream_t st, uint64_t** out);
+  int scratch_free_async(uint64_t* p, cudaStream_t st);
 
   // Pinned host memory mapped into this device's address space, for small
   // host-pointer calls: the caller's words are copied in on the host and the
@@ -117,6 +137,7 @@ class DeviceContext {
 
   int device_;
   cudaStream_t stream_ = nullptr;
+  cudaMemPool_t pool_ = nullptr;
   mutable std::mutex tables_mu_;
   DevMod* d_mods_[kMaxLogN + 1] = {};
   std::vector<uint8_t> built_[kMaxLogN + 1];

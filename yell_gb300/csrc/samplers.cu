@@ -6,15 +6,15 @@
 // sample is a pure function of (seed, position) and can be regenerated on the
 // host; the transformation of random words into coefficients follows the
 // reference's algorithm for each distribution:
-//   uniform  (poly.hpp:200-229): per limb, w & (2^(floor(log2 p)+1) - 1), minus p
+//   uniform  (include/yell/details/poly.hpp:200-228): per limb, w & (2^(floor(log2 p)+1) - 1), minus p
 //            once if still >= p; independent words for every limb.
-//   ZO(rho)  (poly.hpp:262-275): one random byte r per coefficient, shared by all
+//   ZO(rho)  (include/yell/details/poly.hpp:267-280): one random byte r per coefficient, shared by all
 //            limbs: r <= rho ? (r & 2 ? p - 1 : 1) : 0.
-//   HWT(h)   (poly.hpp:282-325): exactly h coefficients set to +-1 (same positions
+//   HWT(h)   (include/yell/details/poly.hpp:287-330): exactly h coefficients set to +-1 (same positions
 //            and signs in every limb), the positions a pseudorandom h-subset (a
 //            keyed permutation of the indices, below); sign bit 1 of a random
 //            word: set -> +1, clear -> p - 1.
-//   gaussian (poly.hpp:238-258): a centred integer e per coefficient, shared by all
+//   gaussian (include/yell/details/poly.hpp:236-260): a centred integer e per coefficient, shared by all
 //            limbs, times an amplifier, mapped e < 0 ? p + e : e.  e comes from a
 //            cumulative table of 64-bit thresholds (search of one random word), not
 //            the reference's FastGaussianNoise lookup tables: the same truncated
@@ -201,7 +201,7 @@ int gaussian_table(int device, double sigma, uint32_t tail, const uint64_t** out
   if (it == tables.end()) {
     const std::vector<uint64_t> cdt = gaussian_cdt(sigma, (int)tail);
     uint64_t* d = nullptr;
-    cudaError_t e = cudaMalloc(&d, cdt.size() * sizeof(uint64_t));
+    cudaError_t e = lib_malloc(&d, cdt.size() * sizeof(uint64_t));
     if (e != cudaSuccess) return fail_cuda(e, "cudaMalloc(gaussian table)");
     e = cudaMemcpy(d, cdt.data(), cdt.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
@@ -228,6 +228,8 @@ int prepare(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log_n, uint32_
   int st = check_degree(log_n);
   if (st != kOk) return st;
   st = check_moduli(cm0, L);
+  if (st != kOk) return st;
+  st = check_limbs(count, L, log_n, nullptr);
   if (st != kOk) return st;
   a->ctx = DeviceContext::current(&st);
   if (!a->ctx) return st;

@@ -152,7 +152,7 @@ int yell_server::init(const yell_server_config* c) {
     if (cfg.hbm_budget_bytes) return fail(kOutOfMemory, "HBM budget exceeds the free device memory");
     budget = free_b > 2 * margin ? free_b - 2 * margin : free_b / 2;
   }
-  e = cudaMalloc(&arena, budget);
+  e = lib_malloc(&arena, budget);
   if (e != cudaSuccess) return fail_cuda(e, "cudaMalloc(server arena)");
   pool.reset(budget);
   cfg.hbm_budget_bytes = budget;

@@ -127,7 +127,7 @@ int yell_autotune(uint32_t log_n, uint32_t L, uint32_t pairs, uint32_t* best, do
   const size_t words = count << log_n;
   const size_t sw = polymul_scratch_words((uint32_t)count, log_n, NttShape{});
   uint64_t* buf = nullptr;
-  cudaError_t e = cudaMalloc(&buf, (3 * words + sw + 2) * sizeof(uint64_t));
+  cudaError_t e = lib_malloc(&buf, (3 * words + sw + 2) * sizeof(uint64_t));
   if (e != cudaSuccess) return fail_cuda(e, "cudaMalloc(autotune)");
   cudaStream_t s = ctx->stream();
   // Any words will do: the arithmetic is branch-free, so timing does not depend on them.
