@@ -218,9 +218,39 @@ def rows_cpu_baseline(dc_host) -> dict:
     return out
 
 
+def init_host_group(world: int):
+    """gloo process group over the ranks (None for one rank)."""
+    if world <= 1:
+        return None
+    import datetime
+
+    import torch.distributed as dist
+
+    dist.init_process_group("gloo", timeout=datetime.timedelta(minutes=10))
+    return dist
+
+
+def host_max(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args, rank: int, world: int) -> int:
-    if rank != 0:
-        return 0
+    dist = init_host_group(world)
+    try:
+        return run_reference_rank0(args, world) if rank == 0 else 0
+    finally:
+        if dist is not None:
+            dist.barrier()  # the other ranks do no work; they wait for rank 0's line
+            dist.destroy_process_group()
+
+
+def run_reference_rank0(args, world: int) -> int:
     import oracle
 
     oracle_dir = os.path.join(ROOT, "oracle")
@@ -265,11 +295,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
     import yell_gb300 as y
 
     torch.cuda.set_device(local_rank)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    # Replicas: no collective on the data path.  The ranks only meet on the
+    # host (barriers around the timed region, the max of their times), so a
+    # gloo group on host tensors is all they need.
+    dist = init_host_group(world)
 
     def barrier():
         if dist is not None:
@@ -277,11 +306,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
         torch.cuda.synchronize()
 
     def max_over_ranks(v: float) -> float:
-        if dist is None:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return host_max(dist, v)
 
     pairs = args.pairs
     a, b = make_inputs(rank, pairs)
@@ -359,22 +384,16 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
                 "pipeline": {"algorithmic_bytes_per_step": 24 * N * L * pairs,
                              "achieved": 24 * N * L * pairs / (ms_per_step * 1e-3) / 1e9,
                              "frac": 24 * N * L * pairs / (ms_per_step * 1e-3) / 1e9 / hbm}}
-    # ---- integer roofline: butterflies against the calibrated ceiling -----
-    ct_rate, gs_rate = y.calibrate_butterflies()
-    ceiling = (2 * ct_rate + gs_rate) / 3  # two forward NTTs per inverse
-    bfly_step = 3 * L * pairs * (N // 2) * LOG_N
-    rows_bfly = 3 * L * pairs * (N // 2) * (LOG_N - 8)  # forward rows of a and b, inverse rows
-    integer_roofline = {
-        "bound": "imad (64-bit modmul from 32-bit IMAD)",
-        "ceiling_ct_bfly_per_s": ct_rate, "ceiling_gs_bfly_per_s": gs_rate,
-        "pipeline_bfly_per_s": bfly_step / (ms_per_step * 1e-3),
-        "pipeline_frac": bfly_step / (ms_per_step * 1e-3) / ceiling,
-        "rows_kernel_bfly_per_s": rows_bfly / (kernels["polymul_rows"][1] / kernels["polymul_rows"][0] * 1e-3)
-        if "polymul_rows" in kernels else None,
-        "note": "ceiling = register-only CT/GS butterflies on every SM (yell_calibrate_butterflies)"}
-    if integer_roofline["rows_kernel_bfly_per_s"]:
-        integer_roofline["rows_kernel_frac"] = integer_roofline["rows_kernel_bfly_per_s"] / ceiling
-    roofline["integer"] = integer_roofline
+    roofline["traffic_kind"] = traffic_kind(dom)
+    roofline["integer"] = integer_roofline(y, kernels, ms_per_step, pairs, y.variants(LOG_N)[tuned_variant])
+    k1 = roofline["integer"]["k1"]
+    if k1 is not None:
+        # distinct twiddle pairs {w, w'} (16 B) one launch reads, once per prime: the row
+        # step reads the forward and inverse tables above index 2^k1, the column passes
+        # the 2^k1 - 1 entries below it; not part of the algorithmic bytes
+        tw = {"polymul_rows": 2 * 16 * (N - (1 << k1)) * L, "polymul_col_fwd": 16 * ((1 << k1) - 1) * L,
+              "polymul_col_inv": 16 * ((1 << k1) - 1) * L}
+        roofline["twiddle_bytes_per_launch"] = tw.get(dom)
     if args.device_only:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT,
@@ -440,6 +459,9 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
            "path": "yell_polymul_host from pinned host buffers"}
     for buf in (pa, pb, pc):
         buf.free()
+    if not args.no_facade:
+        e2e["facade"] = run_e2e_facade(y, a, b, dc.cpu().numpy().view(np.uint64).reshape(a.shape))
+        barrier()
 
     # ---- CPU baseline (rank 0 at N=1 only) --------------------------------
     cpu = None
@@ -492,6 +514,56 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+def run_e2e_facade(y, a, b, want, steps: int = 2) -> dict:
+    """The drop-in path a YELL user hits: for each pair, a.forward();
+    b.forward(); c = a * b; c.backward() through yell_poly_forward /
+    yell_poly_mulmod / yell_poly_backward, on the reference's data layout:
+    every limb its own pageable host allocation (poly<N> allocates each limb
+    separately).  Each call copies its limbs to the device and back and waits,
+    as the reference's calls return with the work done.  The first pass runs
+    on fresh copies and is checked against the fused device result."""
+    import ctypes
+
+    lib = y.load()
+    pairs = a.shape[0]
+    ptrs = ctypes.c_void_p * L
+
+    def limbs(x):
+        return [[np.array(x[p, l], copy=True) for l in range(L)] for p in range(pairs)]
+
+    A, B = limbs(a), limbs(b)
+    C = [[np.empty(N, np.uint64) for _ in range(L)] for _ in range(pairs)]
+    keep = [[ptrs(*[v.ctypes.data for v in X[p]]) for p in range(pairs)] for X in (A, B, C)]
+    pa, pb, pc = ([ctypes.addressof(t) for t in arrs] for arrs in keep)
+
+    def ok(st):
+        if st != 0:
+            raise RuntimeError(lib.yell_last_error().decode())
+
+    def step():
+        for p in range(pairs):
+            ok(lib.yell_poly_forward(pa[p], L, LOG_N))
+            ok(lib.yell_poly_forward(pb[p], L, LOG_N))
+            ok(lib.yell_poly_mulmod(pc[p], pa[p], pb[p], L, LOG_N))
+            ok(lib.yell_poly_backward(pc[p], L, LOG_N))
+
+    step()
+    got = np.stack([np.stack(C[p]) for p in range(pairs)])
+    if not np.array_equal(got, want):
+        raise RuntimeError("facade path differs from the fused polymul")
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    secs = (time.perf_counter() - t0) / steps
+    limb = N * 8
+    h2d = pairs * L * limb * 5  # forward a, forward b, mulmod reads a and b, backward
+    d2h = pairs * L * limb * 4
+    return {"value": 3 * L * pairs / secs, "unit": UNIT, "ms_per_step": 1e3 * secs,
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": steps,
+            "path": "yell_poly_forward x2, yell_poly_mulmod, yell_poly_backward per pair on per-limb "
+                    "pageable host allocations (the reference's poly<N> layout and call pattern)"}
 
 
 def run_rows(torch, y, stream, dc, reps: int = 10, groups: int = 3):
@@ -556,16 +628,19 @@ def run_rows(torch, y, stream, dc, reps: int = 10, groups: int = 3):
     ms = timed(lambda: m32.dev_polymul(c32, a32, b32, PAIRS, L, log32, stream=stream))
     byts = 12 * n32 * L * PAIRS
     # integer roofline: 3 NTTs of (N/2) log N butterflies per limb pair (2 CT, 1 GS)
-    bfly = 3 * L * PAIRS * (1 << (log32 - 1)) * log32
+    n_ct32 = 2 * L * PAIRS * (1 << (log32 - 1)) * log32
+    n_gs32 = n_ct32 // 2
     ct32, gs32 = m32.calibrate_butterflies()
-    ceiling32 = 3.0 / (2.0 / ct32 + 1.0 / gs32)
+    floor_s = integer_ceiling_s(n_ct32, n_gs32, ct32, gs32)
     out["polymul32"] = {"ms": ms, "limb_ntts_per_s": 3 * L * PAIRS / (ms * 1e-3),
                         "achieved_gbs": byts / (ms * 1e-3) / 1e9, "frac": byts / (ms * 1e-3) / 1e9 / hbm,
                         "algorithmic_bytes": byts, "workload": "N=2^15, L=32, 16 pairs, 30-bit primes",
-                        "integer": {"bfly_per_s": bfly / (ms * 1e-3), "ceiling_bfly_per_s": ceiling32,
-                                    "frac": bfly / (ms * 1e-3) / ceiling32,
-                                    "note": "ceiling = register-only 32-bit CT/GS butterflies, 2:1 mix "
-                                            "(yell32_calibrate_butterflies)"}}
+                        "integer": {"bfly_per_s": (n_ct32 + n_gs32) / (ms * 1e-3),
+                                    "ceiling_ct_bfly_per_s": ct32, "ceiling_gs_bfly_per_s": gs32,
+                                    "frac": floor_s / (ms * 1e-3),
+                                    "formula": "frac = (n_ct / ct_rate + n_gs / gs_rate) / measured time",
+                                    "note": "ceiling = register-only 32-bit CT/GS butterflies "
+                                            "(yell32_calibrate_butterflies); Barrett products not counted"}}
     return out
 
 
@@ -657,11 +732,59 @@ def run_serving(torch, y, uneven, duration_s: float):
     return out
 
 
+def integer_ceiling_s(n_ct: float, n_gs: float, ct_rate: float, gs_rate: float) -> float:
+    """Shortest time the calibrated butterfly rates allow for n_ct CT and n_gs
+    GS butterflies (each kind at its own register-only rate).  Used for every
+    kernel and for both word sizes, so the fractions are comparable."""
+    return n_ct / ct_rate + n_gs / gs_rate
+
+
+def integer_roofline(y, kernels: dict, ms_per_step: float, pairs: int, variant_name: str) -> dict:
+    """Butterflies of the fused polymul step and of each of its kernels against
+    the register-only ceiling (yell_calibrate_butterflies).  Stage counts
+    follow the launch variant: k1 column stages, log N - k1 row stages; the
+    forward NTTs of a and b are CT butterflies, the inverse GS (its scaled last
+    layer counted as one GS stage).  The Barrett products (N L pairs of them)
+    and the final reductions are not counted, so each fraction understates the
+    kernel's use of the multiplier slightly."""
+    import re
+
+    ct_rate, gs_rate = y.calibrate_butterflies()
+    m = re.search(r"k1=(\d+)", variant_name)
+    k1 = int(m.group(1)) if m else None
+    half = L * pairs * (N // 2)  # butterflies per stage over the batch
+    out = {"bound": "imad (64-bit modmul from 32-bit IMAD)",
+           "ceiling_ct_bfly_per_s": ct_rate, "ceiling_gs_bfly_per_s": gs_rate,
+           "formula": "frac = (n_ct / ct_rate + n_gs / gs_rate) / measured time",
+           "variant": variant_name, "k1": k1,
+           "note": "ceiling = register-only CT/GS butterflies on every SM; Barrett products not counted"}
+    n_ct, n_gs = 2 * half * LOG_N, half * LOG_N
+    out["pipeline_bfly_per_s"] = (n_ct + n_gs) / (ms_per_step * 1e-3)
+    out["pipeline_frac"] = integer_ceiling_s(n_ct, n_gs, ct_rate, gs_rate) / (ms_per_step * 1e-3)
+    if k1 is not None:
+        rows = LOG_N - k1
+        work = {"polymul_col_fwd": (2 * half * k1, 0), "polymul_rows": (2 * half * rows, half * rows),
+                "polymul_col_inv": (0, half * k1)}
+        out["row_stages"], out["column_stages"] = rows, k1
+        for name, (c, g) in work.items():
+            if name not in kernels:
+                continue
+            launches, total_ms = kernels[name]
+            t = total_ms / launches * 1e-3
+            out[name] = {"ct_bfly": c, "gs_bfly": g, "launch_ms": t * 1e3,
+                         "bfly_per_s": (c + g) / t, "frac": integer_ceiling_s(c, g, ct_rate, gs_rate) / t}
+        if "polymul_rows" in out:
+            out["rows_kernel_frac"] = out["polymul_rows"]["frac"]
+    return out
+
+
+NCU_TRAFFIC = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+
+
 def read_ncu_traffic(kernel: str):
     """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     try:
-        with open(path) as f:
+        with open(NCU_TRAFFIC) as f:
             for line in f:
                 parts = line.split()
                 if len(parts) >= 2 and parts[0] == kernel:
@@ -669,6 +792,16 @@ def read_ncu_traffic(kernel: str):
     except OSError:
         pass
     return None
+
+
+def traffic_kind(kernel: str) -> str | None:
+    """What roofline.traffic is: the header line of the committed ncu summary."""
+    try:
+        with open(NCU_TRAFFIC) as f:
+            kinds = [ln[1:].strip() for ln in f if ln.startswith("#")]
+        return " ".join(kinds) if read_ncu_traffic(kernel) is not None else None
+    except OSError:
+        return None
 
 
 def main() -> int:
@@ -691,13 +824,41 @@ def main() -> int:
                     help="time only the device-resident batch (for profiler captures)")
     ap.add_argument("--pairs", type=int, default=PAIRS,
                     help="pairs per batch (profiling of a smaller case; default 16)")
+    ap.add_argument("--no-facade", action="store_true",
+                    help="skip the end-to-end figure through the per-limb host drop-in calls")
     args = ap.parse_args()
+    if args.gpus < 1:
+        ap.error("--gpus must be at least 1")
+    if "WORLD_SIZE" not in os.environ and args.gpus > 1:
+        # not under torchrun: start the N ranks here, one process per GPU
+        return spawn_ranks(args.gpus, sys.argv[1:])
     rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus == 1 else 1)))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world != args.gpus:
+        print(f"bench.py: --gpus {args.gpus} but WORLD_SIZE {world}", file=sys.stderr)
+        return 2
     if args.impl == "reference":
         return run_reference(args, rank, world)
     return run_ours(args, rank, world, local_rank)
+
+
+def spawn_ranks(n: int, argv: list[str]) -> int:
+    """Runs this script as n ranks (RANK / LOCAL_RANK / WORLD_SIZE /
+    MASTER_ADDR / MASTER_PORT set as torchrun sets them), one per GPU, and
+    returns the first non-zero exit code.  Rank 0 prints the JSON line."""
+    import socket
+
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(n),
+                   LOCAL_WORLD_SIZE=str(n), MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, os.path.abspath(__file__), *argv], env=env))
+    codes = [p.wait() for p in procs]
+    return next((c for c in codes if c != 0), 0)
 
 
 if __name__ == "__main__":

@@ -339,14 +339,22 @@ int yell_batch_release(yell_batch* t);
 /* ---- seeded device samplers: replace poly<N>::set(uniform / ZO_dist / hwt_dist /
  * gaussian) (include/yell/details/poly.hpp:195-330) -------------------------
  * Fill `count` polys (count, L, N) on the device.  The reference's samplers
- * are unseeded; these draw random word k of a stream as
- * splitmix64(seed + (k + 1) * 0x9E3779B97F4A7C15) and turn words into
- * coefficients with the reference's rule for each distribution (uniform: mask
- * to 2^(floor(log2 p)+1) then subtract p once; ZO: one byte r per coefficient,
- * r <= rho ? (r & 2 ? -1 : 1) : 0; HWT: exactly h coefficients +-1; gaussian:
- * a centred integer |e| <= tail by a cumulative table, times `amplifier` as
- * in the reference's gaussian{prng, amp}; tail <= 1024, tail*amplifier < 2^61).  ZO, HWT and gaussian
- * coefficients are the same integers in every limb, mapped e < 0 ? p + e : e. */
+ * draw bytes from an unseeded stream (yell::fastrandombytes); these draw from
+ * a seeded one, word k = splitmix64(seed + (k + 1) * 0x9E3779B97F4A7C15),
+ * bytes little-endian, and make of it exactly what the reference's set(...)
+ * makes of the same stream: uniform (one word per coefficient, limb after
+ * limb, poly after poly: mask to 2^(floor(log2 p)+1) then subtract p once),
+ * ZO (one byte r per coefficient, poly after poly: r <= rho ? (r & 2 ? -1 : 1)
+ * : 0), HWT (poly j on the stream seeded with word j of this seed's stream:
+ * the reference's reservoir sampling with rejection, sorted positions signed
+ * +-1 by the words after the draws).  gaussian: a centred integer |e| <= tail
+ * by inversion of word k against the cumulative table of
+ * yell_gaussian_table, times `amplifier` as in the reference's
+ * gaussian{prng, amp} (tail <= 1024, tail*amplifier < 2^61); its distribution
+ * is the reference's FastGaussianNoise's to within 2^-63 per value, its draws
+ * are not.  ZO, HWT and gaussian coefficients are the same integers in every
+ * limb, mapped e < 0 ? p + e : e.  HWT takes scratch stream-ordered from the
+ * library's per-device pool. */
 int yell_dev_sample_uniform(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
                             uint64_t seed, void* stream);
 int yell_dev_sample_zo(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
@@ -355,6 +363,12 @@ int yell_dev_sample_hwt(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t lo
                         uint32_t h, uint64_t seed, void* stream);
 int yell_dev_sample_gaussian(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
                              double sigma, uint32_t tail, uint64_t amplifier, uint64_t seed, void* stream);
+/* The cumulative table of yell_dev_sample_gaussian for (sigma, tail) on the
+ * host: out[i] = floor(2^64 * P(e <= i - tail)) for i < 2 * tail, out[2 * tail]
+ * = 2^64 - 1 (cap >= 2 * tail + 1).  It stands in for the barrier table the
+ * reference's FastGaussianNoise builds with MPFR
+ * (include/yell/prng/FastGaussianNoise.hpp:302-374). */
+int yell_gaussian_table(double sigma, uint32_t tail, uint64_t* out, uint32_t cap);
 
 /* ---- RNS -> big-integer lifting: replaces gmp::poly2mpz
  * (include/yell/gmp.hpp:42-70, tables lib/gmp.cpp:6-51) ----------------------

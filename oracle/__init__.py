@@ -43,6 +43,7 @@ def build(ref_dir: str | None = None) -> None:
     ref = ref_dir or os.environ.get("YELL_REFERENCE_DIR", "/root/reference")
     if os.path.isdir(os.path.join(ref, "lib")):
         subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={ref}"], check=True)
+        subprocess.run(["make", "-s", "-C", _HERE, "ref_samplers", f"REF={ref}"], check=True)
 
 
 def _bind(lib, prefix: str):
@@ -312,6 +313,71 @@ class Oracle:
         out = self._polys(count, L, log_n)
         self.lib.orc_sample_gaussian(_ptr(out), count, L, log_n, cm0, _ptr(cdt), len(cdt), tail,
                                      amplifier, seed)
+        return out
+
+
+def ref_samplers_available() -> bool:
+    return os.path.exists(os.path.join(_HERE, "_ref", "libyellref_samplers.so"))
+
+
+class RefSamplers:
+    """The reference's own samplers, Gaussian sampler and CRT lifting
+    (yell/poly.hpp set(...), FastGaussianNoise, gmp::poly2mpz) run on the
+    counter stream by ref_samplers_harness.cpp; only where it was built."""
+
+    def __init__(self):
+        lib = ctypes.CDLL(os.path.join(_HERE, "_ref", "libyellref_samplers.so"))
+        u32, u64, i = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+        for name, args in (("refs_sample_uniform", [_U64P, u32, u32, u32, u64]),
+                           ("refs_sample_zo", [_U64P, u32, u32, u32, u32, u64]),
+                           ("refs_sample_hwt", [_U64P, u32, u32, u32, u32, u64]),
+                           ("refs_poly2mpz", [_U64P, _U64P, u32, u32, u32]),
+                           ("refs_gaussian_barriers", [ctypes.c_double, u32, u32, _U32P, _U64P, u32]),
+                           ("refs_gaussian_sample", [ctypes.c_double, u32, u32, u64,
+                                                     ctypes.POINTER(ctypes.c_int64), u64])):
+            fn = getattr(lib, name)
+            fn.restype = i
+            fn.argtypes = args
+        self.lib = lib
+
+    def _polys(self, count, L, log_n):
+        return np.zeros((count, L, 1 << log_n), dtype=np.uint64)
+
+    def sample_uniform(self, count, L, log_n, seed):
+        out = self._polys(count, L, log_n)
+        assert self.lib.refs_sample_uniform(_ptr(out), count, L, log_n, seed) == 0
+        return out
+
+    def sample_zo(self, count, L, log_n, rho, seed):
+        out = self._polys(count, L, log_n)
+        assert self.lib.refs_sample_zo(_ptr(out), count, L, log_n, rho, seed) == 0
+        return out
+
+    def sample_hwt(self, count, L, log_n, h, seed):
+        out = self._polys(count, L, log_n)
+        assert self.lib.refs_sample_hwt(_ptr(out), count, L, log_n, h, seed) == 0
+        return out
+
+    def poly2mpz(self, limbs, log_n, W):
+        """limbs: (L, N) residues of moduli 0..L-1 -> (N, W) little-endian words."""
+        limbs = np.ascontiguousarray(limbs, dtype=np.uint64)
+        out = np.zeros((1 << log_n, W), dtype=np.uint64)
+        rc = self.lib.refs_poly2mpz(_ptr(out), _ptr(limbs), limbs.shape[0], log_n, W)
+        if rc != 0:
+            raise ValueError(f"poly2mpz: {rc}")
+        return out
+
+    def gaussian_barriers(self, sigma=3.2, security=128, samples=1 << 14):
+        """(top 64 bits of each barrier, (barriers, bit precision, words))."""
+        info = (ctypes.c_uint32 * 3)()
+        top = np.zeros(4096, dtype=np.uint64)
+        assert self.lib.refs_gaussian_barriers(sigma, security, samples, info, _ptr(top), top.size) == 0
+        return top[:info[0]].copy(), tuple(info)
+
+    def gaussian_sample(self, n, seed, sigma=3.2, security=128, samples=1 << 14):
+        out = np.zeros(n, dtype=np.int64)
+        assert self.lib.refs_gaussian_sample(sigma, security, samples, seed,
+                                             out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), n) == 0
         return out
 
 

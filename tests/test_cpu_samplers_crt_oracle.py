@@ -1,10 +1,10 @@
 """Oracle checks for the sampler and CRT-lifting rows (CPU only).
 
-The sampler oracle is pinned to the reference's stated distributions
-(include/yell/details/poly.hpp:195-330, include/yell/poly.hpp:27-41) and the
-CRT oracle to the CRT itself: its output x must satisfy x = r_j mod q_j and
-0 <= x < Q, which determines x uniquely (the reference's libgmp headers are not
-installed here, so lib/gmp.cpp cannot be compiled as a second reference).
+Distribution checks of the sampler oracle against the reference's stated
+laws (include/yell/details/poly.hpp:195-330, include/yell/poly.hpp:27-41),
+and of the CRT oracle against the CRT itself: its output x must satisfy
+x = r_j mod q_j and 0 <= x < Q, which determines x uniquely.  Word-for-word
+pins to the reference's own code are in test_cpu_samplers_ref_pin.py.
 """
 import math
 
@@ -107,16 +107,24 @@ def test_crt_oracle_is_the_crt(orc, L):
 
 
 def test_hwt_positions_uniform(orc):
-    """Positions of the keyed-permutation HWT sampler: each index nonzero with
-    probability h/N and pairs with probability h(h-1)/(N(N-1)), as for a
-    uniform h-subset (chi-square and pair-frequency bounds)."""
+    """Positions of the reservoir HWT sampler follow the reference's law.
+
+    The reference draws the replacement index for item k uniformly from
+    [0, k) (include/yell/details/poly.hpp:296-315), not [0, k] as reservoir
+    sampling over k + 1 items would, so the set is not a uniform h-subset:
+    item k >= h is kept with probability (h/k) * prod_{m>k} (1 - 1/m) =
+    h/(N-1) and each of the first h items with (h-1)/(N-1).  Chi-square
+    against that law; pairs co-occur h(h-1)/(N(N-1)) of the time on average,
+    as for any fixed-size subset."""
     log_n, h, cnt = 6, 5, 20000
     n = 1 << log_n
     nz = orc.sample_hwt(cnt, 1, log_n, h=h, seed=21)[:, 0] != 0
     counts = nz.sum(0)
-    e = cnt * h / n
+    e = cnt * np.where(np.arange(n) < h, (h - 1) / (n - 1), h / (n - 1))
     chi2 = float(((counts - e) ** 2 / e).sum())
     assert chi2 < 2.0 * (n - 1)  # dof 63: mean 63, sd ~11
+    e_uniform = cnt * h / n
+    assert float(((counts - e_uniform) ** 2 / e_uniform).sum()) > 3.0 * (n - 1)  # the bias is real
     z = nz.astype(np.float64)
     co = z.T @ z
     exp = cnt * h * (h - 1) / (n * (n - 1))

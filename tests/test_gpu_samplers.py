@@ -36,9 +36,9 @@ def test_zo_matches_oracle(cuda, orc, rho, log_n):
     assert np.array_equal(_host(t, count, L, log_n), orc.sample_zo(count, L, log_n, 2, rho, 17))
 
 
-@pytest.mark.parametrize("log_n,h", [(3, 1), (3, 8), (10, 64), (12, 4096), (14, 192), (17, 1)])
+@pytest.mark.parametrize("log_n,h", [(3, 1), (3, 8), (10, 64), (12, 4096), (14, 192), (17, 1), (20, 1000)])
 def test_hwt_matches_oracle(cuda, orc, log_n, h):
-    count, L = 3, 2
+    count, L = (3, 2) if log_n < 20 else (2, 1)
     t = _empty(cuda, count, L, log_n)
     y.sample_hwt(t, count, L, log_n, h, cm0=1, seed=h + log_n)
     cuda.cuda.synchronize()
@@ -46,6 +46,45 @@ def test_hwt_matches_oracle(cuda, orc, log_n, h):
     assert np.array_equal(got, orc.sample_hwt(count, L, log_n, h, 1, h + log_n))
     for i in range(count):
         assert np.count_nonzero(got[i, 0]) == h
+
+
+@pytest.mark.parametrize("log_n,h", [(3, 8), (10, 64), (12, 4096), (13, 7)])
+def test_hwt_draw_order_path(cuda, orc, monkeypatch, log_n, h):
+    """The one-thread reservoir in draw order (taken when a draw is rejected,
+    forced here) gives the same polys as the parallel draws."""
+    count, L = 2, 2
+    monkeypatch.setenv("YELL_GB300_HWT_SEQUENTIAL", "1")
+    t = _empty(cuda, count, L, log_n)
+    y.sample_hwt(t, count, L, log_n, h, seed=5 + h)
+    cuda.cuda.synchronize()
+    assert np.array_equal(_host(t, count, L, log_n), orc.sample_hwt(count, L, log_n, h, 0, 5 + h))
+
+
+def test_samplers_match_reference_fixture(cuda):
+    """GPU output against the reference's own set(uniform / ZO_dist /
+    hwt_dist) on the same stream (tests/golden/yell_ref_samplers.npz)."""
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "yell_ref_samplers.npz"))
+    checked = 0
+    for kind in ("uniform", "zo", "hwt"):
+        i = 0
+        while f"{kind}_{i}" in g:
+            want = g[f"{kind}_{i}"]
+            args = [int(v) for v in g[f"{kind}_{i}_args"]]
+            count, L, log_n = args[:3]
+            t = _empty(cuda, count, L, log_n)
+            if kind == "uniform":
+                y.sample_uniform(t, count, L, log_n, seed=args[3])
+            elif kind == "zo":
+                y.sample_zo(t, count, L, log_n, rho=args[3], seed=args[4])
+            else:
+                y.sample_hwt(t, count, L, log_n, args[3], seed=args[4])
+            cuda.cuda.synchronize()
+            assert np.array_equal(_host(t, count, L, log_n), want), (kind, i)
+            checked += 1
+            i += 1
+    assert checked == 17
 
 
 @pytest.mark.parametrize("sigma,tail,amp", [(3.2, 19, 1), (3.2, 19, 1 << 20), (0.5, 4, 1), (40.0, 1024, 3)])

@@ -296,6 +296,13 @@ def sample_gaussian(t, count: int, L: int, log_n: int, cm0: int = 0, sigma: floa
          _stream(stream))
 
 
+def gaussian_table(sigma: float = 3.2, tail: int = 19) -> np.ndarray:
+    """The Gaussian sampler's cumulative 64-bit thresholds (2 * tail + 1)."""
+    out = np.zeros(2 * tail + 1, dtype=np.uint64)
+    call("yell_gaussian_table", sigma, tail, out.ctypes.data, out.size)
+    return out
+
+
 def crt_words(L: int, cm0: int = 0) -> int:
     """64-bit words of prod q_j over moduli cm0 .. cm0+L-1 (words per lifted coefficient)."""
     w = ctypes.c_uint32()

@@ -135,6 +135,7 @@ SIGNATURES = {
     "yell_dev_sample_zo": (_int, [_vp, _u32, _u32, _u32, _u32, _u32, _u64, _vp]),
     "yell_dev_sample_hwt": (_int, [_vp, _u32, _u32, _u32, _u32, _u32, _u64, _vp]),
     "yell_dev_sample_gaussian": (_int, [_vp, _u32, _u32, _u32, _u32, ctypes.c_double, _u32, _u64, _u64, _vp]),
+    "yell_gaussian_table": (_int, [ctypes.c_double, _u32, _vp, _u32]),
     "yell_variant_count": (_int, [_u32, _vp]),
     "yell_variant_name": (_int, [_u32, _u32, ctypes.c_char_p, _sz]),
     "yell_set_variant": (_int, [_u32, _u32]),
