@@ -23,9 +23,11 @@ namespace {
 constexpr int kQueueThreads = 256;
 static_assert(kQueueTileLog == (uint32_t)kTileLog, "queue tiles are the two-pass tiles");
 
+// Column stages of the queue's two-pass items: rows of at most 512 words
+// (one warp's) from 2^16 up, so the row step needs only warp barriers.
 template <int LOGN>
 constexpr int k1_of() {
-  return LOGN == 13 ? 6 : (LOGN <= 15 ? 7 : 8);
+  return LOGN == 13 ? 6 : (LOGN <= 15 ? 7 : LOGN - 9);
 }
 
 __device__ __forceinline__ uint64_t global_ns() {
@@ -73,26 +75,39 @@ __device__ __forceinline__ void run_item(uint32_t kind, const QueueBucket& B, ui
   }
 }
 
-__device__ __forceinline__ void dispatch(uint32_t kind, const QueueBucket& B, uint32_t bid) {
-  switch (B.log_n) {
-    case 3: run_item<3>(kind, B, bid); break;
-    case 4: run_item<4>(kind, B, bid); break;
-    case 5: run_item<5>(kind, B, bid); break;
-    case 6: run_item<6>(kind, B, bid); break;
-    case 7: run_item<7>(kind, B, bid); break;
-    case 8: run_item<8>(kind, B, bid); break;
-    case 9: run_item<9>(kind, B, bid); break;
-    case 10: run_item<10>(kind, B, bid); break;
-    case 11: run_item<11>(kind, B, bid); break;
-    case 12: run_item<12>(kind, B, bid); break;
-    case 13: run_item<13>(kind, B, bid); break;
-    case 14: run_item<14>(kind, B, bid); break;
-    case 15: run_item<15>(kind, B, bid); break;
-    case 16: run_item<16>(kind, B, bid); break;
-    case 17: run_item<17>(kind, B, bid); break;
-    case 18: run_item<18>(kind, B, bid); break;
-    case 19: run_item<19>(kind, B, bid); break;
-    case 20: run_item<20>(kind, B, bid); break;
+// One function per degree, not inlined: each body gets its own register
+// allocation within the kernel's 128 registers.  Inlined into one switch, the
+// bodies shared one allocation and the kernel spilled 448 bytes per thread;
+// separately each spills at most 16.  The bucket is read inside the callee,
+// so nothing large crosses the call.
+template <int LOGN>
+__device__ __noinline__ void run_item_of(uint32_t kind, const QueueBucket* __restrict__ buckets, uint32_t bucket,
+                                         uint32_t bid) {
+  const QueueBucket B = buckets[bucket];
+  run_item<LOGN>(kind, B, bid);
+}
+
+__device__ __forceinline__ void dispatch(uint32_t kind, const QueueBucket* buckets, uint32_t bucket, uint32_t log_n,
+                                         uint32_t bid) {
+  switch (log_n) {
+    case 3: run_item_of<3>(kind, buckets, bucket, bid); break;
+    case 4: run_item_of<4>(kind, buckets, bucket, bid); break;
+    case 5: run_item_of<5>(kind, buckets, bucket, bid); break;
+    case 6: run_item_of<6>(kind, buckets, bucket, bid); break;
+    case 7: run_item_of<7>(kind, buckets, bucket, bid); break;
+    case 8: run_item_of<8>(kind, buckets, bucket, bid); break;
+    case 9: run_item_of<9>(kind, buckets, bucket, bid); break;
+    case 10: run_item_of<10>(kind, buckets, bucket, bid); break;
+    case 11: run_item_of<11>(kind, buckets, bucket, bid); break;
+    case 12: run_item_of<12>(kind, buckets, bucket, bid); break;
+    case 13: run_item_of<13>(kind, buckets, bucket, bid); break;
+    case 14: run_item_of<14>(kind, buckets, bucket, bid); break;
+    case 15: run_item_of<15>(kind, buckets, bucket, bid); break;
+    case 16: run_item_of<16>(kind, buckets, bucket, bid); break;
+    case 17: run_item_of<17>(kind, buckets, bucket, bid); break;
+    case 18: run_item_of<18>(kind, buckets, bucket, bid); break;
+    case 19: run_item_of<19>(kind, buckets, bucket, bid); break;
+    case 20: run_item_of<20>(kind, buckets, bucket, bid); break;
     default: break;
   }
 }
@@ -124,7 +139,7 @@ __global__ void __launch_bounds__(kQueueThreads, 2) k_batch_queue(QueueLaunch q)
       }
       if (kind != kItemColInv) publish = cnt + (kind == kItemColFwd ? 0 : 1);
     }
-    dispatch(kind, B, it.bid);
+    dispatch(kind, q.buckets, it.bucket_kind >> 8, B.log_n, it.bid);
     // s_ticket[cur ^ 1] was last read before the previous iteration's barrier
     if (threadIdx.x == 0) s_ticket[cur ^ 1u] = next;
     __syncthreads();  // every thread's stores issued; the tiles are free again

@@ -345,6 +345,26 @@ struct PairCfg32 {
   static constexpr size_t kSmem = Smem<uint32_t>::words(1u << H) * sizeof(uint32_t);
 };
 
+// The stages inside a half limb of 2^H words, as two tiles of the engine:
+// the top 5 (pair distances 2^(H-1) .. 2^(H-5)) as one round across the CTA
+// (CA: columns of stride 2^(H-5)), the other H - 5 in rows of 2^(H-5) words
+// (CB), each row held by 2^(H-10) threads of one warp, so the rounds inside a
+// row need only warp barriers.  The rounds are the same (5, H - 10, 5)
+// stages as one tile over the half would run, with one CTA barrier less per
+// transform.  The bottom round gives each thread 32 consecutive words, as
+// before.
+template <int H>
+struct HalfSplit {
+  using CA = TileCfg<H, 5, H - 5, 5>;
+  using CB = TileCfg<H, H - 5, 0, 5>;
+  static constexpr int KB = H - 5;
+  static_assert(CA::THREADS == CB::THREADS && CB::LOCAL_BARRIER == 1, "rows must stay inside a warp");
+  // Row index within the whole limb (the sub-transform group of CB's top stage).
+  __device__ static __forceinline__ uint32_t row_group(uint32_t r, uint32_t tid) {
+    return (r << (H - KB)) + CB::sub(tid);
+  }
+};
+
 // Forward NTT of one half limb of `src` (the limb's first word) into the
 // bottom-round registers x of this thread: stage 0 while loading, stages
 // 1 .. log N - 1 in shared memory, the last round in registers.
@@ -379,10 +399,16 @@ __device__ __forceinline__ void pair_forward(uint32_t* x, const uint32_t* __rest
   // an in-place transform may overwrite src only once both CTAs have read it
   if constexpr (CLUSTER_SYNC) cooperative_groups::this_cluster().sync();
   else __syncthreads();
-  fwd_rounds<C, 0, NR - 1>(smem32, tid, 1, r, m.fwd, p, true);
-  const uint32_t bb = RB::base(tid);
-  smem_load<RB>(x, smem32, bb);
-  ct_round<RB>(x, m.fwd, 1u + RB::HI, RB::gr(bb, r), p);
+  using S = HalfSplit<H>;
+  using CB = typename S::CB;
+  using RBB = Round<CB, CB::NR - 1>;
+  static_assert(RBB::R == RB::R && RBB::BETA == 0 && RBB::EB == 0, "same bottom round as one tile over the half");
+  fwd_rounds<typename S::CA, 0, 1>(smem32, tid, 1, r, m.fwd, p, true);  // stages 1..5, CTA barrier
+  const uint32_t G = S::row_group(r, tid);
+  fwd_rounds<CB, 0, CB::NR - 1, CB::LOCAL_BARRIER>(smem32, tid, 6, G, m.fwd, p, true);
+  const uint32_t bb = RBB::base(tid);
+  smem_load<RBB>(x, smem32, bb);
+  ct_round<RBB>(x, m.fwd, 6u + RBB::HI, RBB::gr(bb, G), p);
 }
 
 template <class C>
@@ -424,10 +450,19 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, C::THREA
     x[i + 2] = mulmod_barrett(ah.z, fwd_correct(x[i + 2], p, p2), p, m.pn);
     x[i + 3] = mulmod_barrett(ah.w, fwd_correct(x[i + 3], p, p2), p, m.pn);
   }
-  gs_round<RB, false>(x, log_n, (uint32_t)RB::BETA, RB::gr(bb, r), m);
-  smem_store<RB>(x, smem32, bb);
-  __syncthreads();
-  inv_rounds<C, NR - 2, -1, false>(smem32, tid, log_n, 0, r, m, true);
+  {
+    // inverse stages inside the half: rows (warp barriers), then the top 5
+    // across the CTA; the same bottom-round words as RB
+    using S = HalfSplit<H>;
+    using CB = typename S::CB;
+    using RBB = Round<CB, CB::NR - 1>;
+    const uint32_t G = S::row_group(r, tid);
+    gs_round<RBB, false>(x, log_n, (uint32_t)RBB::BETA, RBB::gr(bb, G), m);
+    smem_store<RBB>(x, smem32, bb);
+    round_barrier<CB, CB::LOCAL_BARRIER>(tid);
+    inv_rounds<CB, CB::NR - 2, -1, false>(smem32, tid, log_n, 0, G, m, true);  // CTA barrier after
+    inv_rounds<typename S::CA, 0, -1, false>(smem32, tid, log_n, S::KB, r, m, true);
+  }
   // last layer across the pair: u = word i (rank 0), w = word i + N/2 (rank 1)
   cluster.sync();
   const uint32_t* peer = cluster.map_shared_rank(smem32, (int)(r ^ 1u));
@@ -487,7 +522,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, C::THREA
       *reinterpret_cast<uint4*>(smem32 + Smem<uint32_t>::idx(v)) = __ldg(reinterpret_cast<const uint4*>(own + v));
     }
     __syncthreads();
-    inv_rounds<C, NR - 1, -1, false>(smem32, tid, log_n, 0, r, m, true);
+    {
+      using S = HalfSplit<H>;
+      using CB = typename S::CB;
+      const uint32_t G = S::row_group(r, tid);
+      inv_rounds<CB, CB::NR - 1, 0, false, CB::LOCAL_BARRIER>(smem32, tid, log_n, 0, G, m, true);
+      inv_rounds<CB, 0, -1, false>(smem32, tid, log_n, 0, G, m, true);  // CTA barrier after
+      inv_rounds<typename S::CA, 0, -1, false>(smem32, tid, log_n, S::KB, r, m, true);
+    }
     cluster.sync();
     const uint32_t* peer = cluster.map_shared_rank(smem32, (int)(r ^ 1u));
     uint32_t* dst = base + r * half;

@@ -96,6 +96,7 @@ void build_table() {
   add_two_pass_variants_a(g_table);
   add_two_pass_variants_b(g_table);
   add_two_pass_variants_c(g_table);
+  add_two_pass_variants_d(g_table);
 }
 
 int current_device() {

@@ -372,9 +372,14 @@ __device__ __forceinline__ void col_pass_body(ConstLimbSet src, LimbSet dst, con
 // registers (a few bytes spilled) it runs four CTAs per SM instead of three,
 // and that polymul takes 1.117 instead of 1.127 ms.  The forward pass (NTT
 // calls) fits three CTAs per SM at 80 registers without spilling.
+// Minimum resident CTAs for a launch-bounds target of `threads` per SM.
+constexpr int min_blocks(int threads_per_sm, int cta_threads) {
+  return threads_per_sm / cta_threads > 1 ? threads_per_sm / cta_threads : 1;
+}
+
 template <class C, int LOGB, bool INV>
-__global__ void __launch_bounds__(C::THREADS, INV ? 4 : 3) k_col_pass(ConstLimbSet src, LimbSet dst,
-                                                                      const DevMod* __restrict__ mods) {
+__global__ void __launch_bounds__(C::THREADS, min_blocks(INV ? 1024 : 768, C::THREADS))
+    k_col_pass(ConstLimbSet src, LimbSet dst, const DevMod* __restrict__ mods) {
   extern __shared__ __align__(16) uint64_t smem[];
   constexpr int K = C::K, LB = C::LB, NR = C::NR;
   constexpr uint32_t log_n = K + LOGB;
@@ -607,8 +612,8 @@ __device__ __forceinline__ void col_pass2_body(ConstLimbSet a, ConstLimbSet b, L
 }
 
 template <class C, int LOGB>
-__global__ void __launch_bounds__(C::THREADS, 2) k_col_pass2(ConstLimbSet a, ConstLimbSet b, LimbSet ca,
-                                                             LimbSet cb, const DevMod* __restrict__ mods) {
+__global__ void __launch_bounds__(C::THREADS, min_blocks(512, C::THREADS))
+    k_col_pass2(ConstLimbSet a, ConstLimbSet b, LimbSet ca, LimbSet cb, const DevMod* __restrict__ mods) {
   col_pass2_body<C, LOGB>(a, b, ca, cb, mods, blockIdx.x);
 }
 
@@ -658,8 +663,8 @@ __device__ __forceinline__ void polymul_rows_body(LimbSet ca, ConstLimbSet sbuf,
 }
 
 template <class C, int K1>
-__global__ void __launch_bounds__(C::THREADS, 2) k_polymul_rows(LimbSet ca, ConstLimbSet sbuf,
-                                                                const DevMod* __restrict__ mods) {
+__global__ void __launch_bounds__(C::THREADS, min_blocks(512, C::THREADS))
+    k_polymul_rows(LimbSet ca, ConstLimbSet sbuf, const DevMod* __restrict__ mods) {
   polymul_rows_body<C, K1>(ca, sbuf, mods, blockIdx.x);
 }
 
@@ -675,10 +680,12 @@ cudaError_t set_smem(KernelT kernel, size_t bytes) {
 // Whole-limb tile: 2^T words (T >= log_n); 16 words per thread (8 at N = 8).
 template <int LOGN, int T>
 using WholeCfg = TileCfg<T, LOGN, 0, (LOGN >= 4 ? 4 : 3)>;
-template <int LOGN, int K1>
-using ColCfg = TileCfg<kTileLog, K1, kTileLog - K1, 4>;
-template <int LOGN, int K1>
-using RowCfg = TileCfg<kTileLog, LOGN - K1, 0, 4>;
+// Two-pass tiles: 4096 words, 2^LOGE words per thread per round (radix-2^LOGE
+// rounds): LOGE = 4 is 256 threads, LOGE = 3 is 512 threads per tile.
+template <int LOGN, int K1, int LOGE = 4>
+using ColCfg = TileCfg<kTileLog, K1, kTileLog - K1, LOGE>;
+template <int LOGN, int K1, int LOGE = 4>
+using RowCfg = TileCfg<kTileLog, LOGN - K1, 0, LOGE>;
 
 constexpr size_t tile_bytes(int T) { return tile_smem_words(1u << T) * sizeof(uint64_t); }
 constexpr size_t kTileSmemBytes = tile_bytes(kTileLog);
@@ -722,11 +729,11 @@ cudaError_t set_attrs_whole() {
   return set_smem(k_polymul_whole<C>, 2 * s);
 }
 
-template <int LOGN, int K1>
+template <int LOGN, int K1, int LC = 4, int LR = 4>
 cudaError_t launch_two_pass_ntt(const LimbSet& ls, const DevMod* mods, NttDir dir, cudaStream_t st) {
   constexpr int LOGB = LOGN - K1;
-  using CC = ColCfg<LOGN, K1>;
-  using RC = RowCfg<LOGN, K1>;
+  using CC = ColCfg<LOGN, K1, LC>;
+  using RC = RowCfg<LOGN, K1, LR>;
   const uint32_t tiles = ls.count << (LOGN - kTileLog);
   const ConstLimbSet cls = as_const(ls);
   if (dir == NttDir::kBackward) {
@@ -749,13 +756,13 @@ cudaError_t launch_two_pass_ntt(const LimbSet& ls, const DevMod* mods, NttDir di
   return cudaGetLastError();
 }
 
-template <int LOGN, int K1>
+template <int LOGN, int K1, int LC = 4, int LR = 4>
 cudaError_t launch_two_pass_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
                                     const DevMod* mods, uint64_t* scratch, uint64_t* const* scratch_ptrs,
                                     cudaStream_t st) {
   constexpr int LOGB = LOGN - K1;
-  using CC = ColCfg<LOGN, K1>;
-  using RC = RowCfg<LOGN, K1>;
+  using CC = ColCfg<LOGN, K1, LC>;
+  using RC = RowCfg<LOGN, K1, LR>;
   const uint32_t tiles = c.count << (LOGN - kTileLog);
   LimbSet sl = c;
   sl.base = scratch_ptrs ? nullptr : scratch;
@@ -776,11 +783,11 @@ cudaError_t launch_two_pass_polymul(const LimbSet& c, const ConstLimbSet& a, con
   return cudaGetLastError();
 }
 
-template <int LOGN, int K1>
+template <int LOGN, int K1, int LC = 4, int LR = 4>
 cudaError_t set_attrs_two_pass() {
   constexpr int LOGB = LOGN - K1;
-  using CC = ColCfg<LOGN, K1>;
-  using RC = RowCfg<LOGN, K1>;
+  using CC = ColCfg<LOGN, K1, LC>;
+  using RC = RowCfg<LOGN, K1, LR>;
   cudaError_t e;
   if ((e = set_smem(k_col_pass<CC, LOGB, false>, kTileSmemBytes)) != cudaSuccess) return e;
   if ((e = set_smem(k_col_pass<CC, LOGB, true>, kTileSmemBytes)) != cudaSuccess) return e;
@@ -803,13 +810,19 @@ Variant whole_variant() {
   return v;
 }
 
-template <int LOGN, int K1>
+// Named "two-pass k1=K1 (...)"; variants whose column or row tiles use other
+// than 16 words per thread name both word counts.
+template <int LOGN, int K1, int LC = 4, int LR = 4>
 Variant two_pass_variant() {
   Variant v;
-  std::snprintf(v.name, sizeof(v.name), "two-pass k1=%d (columns of 2^%d, rows of 2^%d)", K1, K1, LOGN - K1);
-  v.ntt = &launch_two_pass_ntt<LOGN, K1>;
-  v.polymul = &launch_two_pass_polymul<LOGN, K1>;
-  v.set_attrs = &set_attrs_two_pass<LOGN, K1>;
+  if (LC == 4 && LR == 4)
+    std::snprintf(v.name, sizeof(v.name), "two-pass k1=%d (columns of 2^%d, rows of 2^%d)", K1, K1, LOGN - K1);
+  else
+    std::snprintf(v.name, sizeof(v.name), "two-pass k1=%d (columns of 2^%d, rows of 2^%d; %d/%d words per thread)",
+                  K1, K1, LOGN - K1, 1 << LC, 1 << LR);
+  v.ntt = &launch_two_pass_ntt<LOGN, K1, LC, LR>;
+  v.polymul = &launch_two_pass_polymul<LOGN, K1, LC, LR>;
+  v.set_attrs = &set_attrs_two_pass<LOGN, K1, LC, LR>;
   v.ntt_launches = 2;
   v.polymul_launches = 3;
   v.polymul_scratch = true;

@@ -60,21 +60,30 @@ __host__ __device__ __forceinline__ uint64_t rand_word(uint64_t seed, uint64_t k
 
 // A warp writes 128 consecutive words per step as two 512-byte stores: lane j
 // holds words 2j, 2j + 1 and 64 + 2j, 65 + 2j of the chunk.  The total is a
-// multiple of 8 words (N >= 8), so a pair never straddles two limbs.
+// multiple of 8 words (N >= 8), so a pair never straddles two limbs.  Each
+// warp walks one contiguous run of chunks, so the limb (and with it p and the
+// mask) changes rarely and is worked out only when it does.
 __global__ void k_sample_uniform(uint64_t* out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
                                  const DevMod* __restrict__ mods, uint64_t seed) {
   const size_t words = ((size_t)count * L) << log_n;
+  const size_t chunks = (words + 127) >> 7;
   const uint32_t lane = threadIdx.x & 31u;
   const size_t warp = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
   const size_t warps = ((size_t)gridDim.x * blockDim.x) >> 5;
-  for (size_t c = warp << 7; c < words; c += warps << 7) {
+  const size_t per = (chunks + warps - 1) / warps;
+  const size_t c0 = warp * per, c1 = min(c0 + per, chunks);
+  size_t row = ~(size_t)0;
+  uint64_t p = 0, mask = 0;
+  for (size_t ch = c0; ch < c1; ++ch) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const size_t k = c + ((size_t)h << 6) + (lane << 1);
+      const size_t k = (ch << 7) + ((size_t)h << 6) + (lane << 1);
       if (k >= words) break;
-      const uint32_t l = (uint32_t)(k >> log_n) % L;
-      const uint64_t p = __ldg(&mods[cm0 + l].p);
-      const uint64_t mask = (2ull << (63 - __clzll(p))) - 1ull;  // 2^(floor(log2 p) + 1) - 1
+      if ((k >> log_n) != row) {
+        row = k >> log_n;
+        p = __ldg(&mods[cm0 + (uint32_t)(row % L)].p);
+        mask = (2ull << (63 - __clzll(p))) - 1ull;  // 2^(floor(log2 p) + 1) - 1
+      }
       const uint64_t z = seed + (k + 1) * 0x9E3779B97F4A7C15ull;  // counter of word k; + gamma per word
       uint64_t v0 = mix64(z) & mask, v1 = mix64(z + 0x9E3779B97F4A7C15ull) & mask;
       if (v0 >= p) v0 -= p;
