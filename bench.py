@@ -333,6 +333,13 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
         if rank == 0:
             print(json.dumps({"rows": rows}), flush=True)
         return 0
+    if args.uneven_only:  # profiling entry: the uneven batch (graphs, one queue launch, per call) alone
+        uneven = run_uneven(torch, y, stream, lambda: torch.cuda.synchronize(), lambda v: v, 1, args.no_autotune)
+        uneven.pop("_items")
+        uneven.pop("_mix")
+        if rank == 0:
+            print(json.dumps({"uneven_batch": uneven}), flush=True)
+        return 0
 
     # ---- device-resident throughput (value) ---------------------------
     for _ in range(max(args.warmup, 3)):
@@ -813,6 +820,8 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch comparison")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving sweep")
+    ap.add_argument("--uneven-only", action="store_true",
+                    help="run only the uneven-batch comparison (for profiling)")
     ap.add_argument("--rows-only", action="store_true",
                     help="run only the sampler, CRT-lifting and 32-bit measurements (for profiling)")
     ap.add_argument("--no-rows", action="store_true",

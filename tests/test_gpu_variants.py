@@ -64,3 +64,30 @@ def test_autotune_selects_a_variant_and_stays_exact(cuda, orc, tmp_path, monkeyp
     got = c.cpu().numpy().view(np.uint64).reshape(a.shape)
     assert np.array_equal(got[1], orc.polymul(a[1], b[1], log_n, 0))
     y.set_variant(log_n, 0)
+
+
+@pytest.mark.parametrize("log_n", [16])
+def test_pipelined_variants_over_many_tiles(cuda, orc, log_n):
+    """The pipelined polymul kernels are persistent: with 48 limbs (768 tiles
+    of 4096 words, above the resident CTAs of every pass) each CTA runs
+    several tiles, and every copy-ahead overlaps the previous tile."""
+    torch = cuda
+    names = y.variants(log_n)
+    pipe = [v for v, n in enumerate(names) if "pipelined" in n]
+    assert pipe, names
+    L, cm0, pairs = 4, 2, 12
+    ps = y.primes(L, cm0)
+    a = uniform_polys(1800 + log_n, pairs, L, log_n, ps)
+    b = uniform_polys(1900 + log_n, pairs, L, log_n, ps)
+    want = [orc.polymul(a[i], b[i], log_n, cm0) for i in range(pairs)]
+    try:
+        for v in pipe:
+            y.set_variant(log_n, v)
+            c = torch.empty(a.size, dtype=torch.int64, device="cuda")
+            y.dev_polymul(c, _dev(torch, a), _dev(torch, b), pairs, L, log_n, cm0)
+            torch.cuda.synchronize()
+            got = c.cpu().numpy().view(np.uint64).reshape(a.shape)
+            for i in range(pairs):
+                assert np.array_equal(got[i], want[i]), (names[v], i)
+    finally:
+        y.set_variant(log_n, 0)

@@ -279,7 +279,7 @@ int BatchExecutor::run_queue(DeviceContext* ctx, const yell_polymul_desc* descs,
     }
     buckets.push_back(b);
   }
-  if (buckets.size() > (1u << 24)) return fail(kInvalidArgument, "batch: too many buckets");
+  if (buckets.size() > kQueueMaxBuckets) return fail(kInvalidArgument, "batch: too many buckets");
   // ---- queue: forward column passes, whole-limb tiles, row steps, inverse
   // column passes.  All resident CTAs run the same kind of item most of the
   // time, so the SMs' instruction caches hold one body at a time.
@@ -358,6 +358,7 @@ int BatchExecutor::run_queue(DeviceContext* ctx, const yell_polymul_desc* descs,
   ql.buckets = reinterpret_cast<const QueueBucket*>(d_lists_ + buckets_off);
   ql.items = reinterpret_cast<const QueueItem*>(d_lists_ + items_off);
   ql.n_items = (uint32_t)items.size();
+  ql.n_buckets = (uint32_t)buckets.size();
   ql.status = d_queue_ctl_;
   ql.next = d_queue_ctl_ + 1;
   ql.done = d_queue_ctl_ + 2;
@@ -428,6 +429,7 @@ int BatchExecutor::queue_wait_check(DeviceContext* ctx, cudaStream_t s, uint64_t
   ql.buckets = reinterpret_cast<const QueueBucket*>(d_lists_ + 64);
   ql.items = reinterpret_cast<const QueueItem*>(d_lists_ + 64 + sizeof(QueueBucket) + 16);
   ql.n_items = 2 * tiles;
+  ql.n_buckets = 1;
   ql.status = d_queue_ctl_;
   ql.next = d_queue_ctl_ + 1;
   ql.done = d_queue_ctl_ + 2;

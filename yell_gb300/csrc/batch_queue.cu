@@ -75,60 +75,94 @@ __device__ __forceinline__ void run_item(uint32_t kind, const QueueBucket& B, ui
   }
 }
 
+// Tickets of one CTA: slot cur is the item being run, slot cur + 1 the next
+// one (its item already read), slot cur + 2 the one after it (ticket taken).
+struct TicketRing {
+  uint32_t ticket[3];
+  QueueItem item[3];
+};
+
+__device__ __forceinline__ uint32_t ring_next(uint32_t s) { return s == 2 ? 0u : s + 1u; }
+
 // One function per degree, not inlined: each body gets its own register
 // allocation within the kernel's 128 registers.  Inlined into one switch, the
 // bodies shared one allocation and the kernel spilled 448 bytes per thread;
-// separately each spills at most 16.  The bucket is read inside the callee,
-// so nothing large crosses the call.
+// separately each spills at most 16.  The bucket stays in shared memory.
+// Thread 0 starts the two queue reads of later items here, before the body:
+// the next item's descriptor and the ticket after it.  Both complete while
+// the body runs and are stored when it returns, so neither round trip (nor
+// one across the call) is waited for.
 template <int LOGN>
-__device__ __noinline__ void run_item_of(uint32_t kind, const QueueBucket* __restrict__ buckets, uint32_t bucket,
-                                         uint32_t bid) {
-  const QueueBucket B = buckets[bucket];
-  run_item<LOGN>(kind, B, bid);
+__device__ __noinline__ void run_item_of(uint32_t kind, const QueueBucket* s_buckets, uint32_t bucket, uint32_t bid,
+                                         const QueueLaunch* q, TicketRing* ring, uint32_t cur) {
+  const uint32_t s1 = ring_next(cur), s2 = ring_next(s1);
+  uint32_t t2 = 0;
+  QueueItem it1{0, 0};
+  if (threadIdx.x == 0) {
+    const uint32_t t1 = ring->ticket[s1];
+    if (t1 < q->n_items) it1 = q->items[t1];
+    t2 = atomicAdd(q->next, 1u);
+  }
+  run_item<LOGN>(kind, s_buckets[bucket], bid);
+  if (threadIdx.x == 0) {
+    ring->item[s1] = it1;
+    ring->ticket[s2] = t2;  // slot s2 was read before the previous item's barrier
+  }
 }
 
-__device__ __forceinline__ void dispatch(uint32_t kind, const QueueBucket* buckets, uint32_t bucket, uint32_t log_n,
-                                         uint32_t bid) {
+__device__ __forceinline__ void dispatch(uint32_t kind, const QueueBucket* s_buckets, uint32_t bucket, uint32_t log_n,
+                                         uint32_t bid, const QueueLaunch* q, TicketRing* ring, uint32_t cur) {
   switch (log_n) {
-    case 3: run_item_of<3>(kind, buckets, bucket, bid); break;
-    case 4: run_item_of<4>(kind, buckets, bucket, bid); break;
-    case 5: run_item_of<5>(kind, buckets, bucket, bid); break;
-    case 6: run_item_of<6>(kind, buckets, bucket, bid); break;
-    case 7: run_item_of<7>(kind, buckets, bucket, bid); break;
-    case 8: run_item_of<8>(kind, buckets, bucket, bid); break;
-    case 9: run_item_of<9>(kind, buckets, bucket, bid); break;
-    case 10: run_item_of<10>(kind, buckets, bucket, bid); break;
-    case 11: run_item_of<11>(kind, buckets, bucket, bid); break;
-    case 12: run_item_of<12>(kind, buckets, bucket, bid); break;
-    case 13: run_item_of<13>(kind, buckets, bucket, bid); break;
-    case 14: run_item_of<14>(kind, buckets, bucket, bid); break;
-    case 15: run_item_of<15>(kind, buckets, bucket, bid); break;
-    case 16: run_item_of<16>(kind, buckets, bucket, bid); break;
-    case 17: run_item_of<17>(kind, buckets, bucket, bid); break;
-    case 18: run_item_of<18>(kind, buckets, bucket, bid); break;
-    case 19: run_item_of<19>(kind, buckets, bucket, bid); break;
-    case 20: run_item_of<20>(kind, buckets, bucket, bid); break;
+    case 3: run_item_of<3>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 4: run_item_of<4>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 5: run_item_of<5>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 6: run_item_of<6>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 7: run_item_of<7>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 8: run_item_of<8>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 9: run_item_of<9>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 10: run_item_of<10>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 11: run_item_of<11>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 12: run_item_of<12>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 13: run_item_of<13>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 14: run_item_of<14>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 15: run_item_of<15>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 16: run_item_of<16>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 17: run_item_of<17>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 18: run_item_of<18>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 19: run_item_of<19>(kind, s_buckets, bucket, bid, q, ring, cur); break;
+    case 20: run_item_of<20>(kind, s_buckets, bucket, bid, q, ring, cur); break;
     default: break;
   }
 }
 
-// Each CTA takes its next ticket while it works on the current item, so the
-// atomic's round trip is hidden behind the item.  Still deadlock-free: the
-// smallest ticket taken and not finished is always some CTA's current item
-// (a prefetched ticket is larger than its CTA's current one), and it depends
-// only on smaller tickets, which are all finished.
+// Each CTA holds two tickets beyond the item it runs (their atomics and the
+// next item's descriptor read are hidden behind the item).  Still
+// deadlock-free: the smallest ticket taken and not finished is always some
+// CTA's current item (a CTA's prefetched tickets are larger than its current
+// one), and it depends only on smaller tickets, which are all finished.
 __global__ void __launch_bounds__(kQueueThreads, 2) k_batch_queue(QueueLaunch q) {
-  __shared__ uint32_t s_ticket[2];
-  if (threadIdx.x == 0) s_ticket[0] = atomicAdd(q.next, 1u);
+  __shared__ TicketRing ring;
+  __shared__ __align__(16) QueueBucket s_buckets[kQueueMaxBuckets];
+  static_assert(sizeof(QueueBucket) % 8 == 0, "buckets are copied as 8-byte words");
+  {
+    const uint2* src = reinterpret_cast<const uint2*>(q.buckets);
+    uint2* dst = reinterpret_cast<uint2*>(s_buckets);
+    const uint32_t words = min(q.n_buckets, kQueueMaxBuckets) * (uint32_t)(sizeof(QueueBucket) / 8);
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+  }
+  if (threadIdx.x == 0) {
+    const uint32_t t0 = atomicAdd(q.next, 1u);
+    ring.ticket[0] = t0;
+    ring.item[0] = t0 < q.n_items ? q.items[t0] : QueueItem{0, 0};
+    ring.ticket[1] = atomicAdd(q.next, 1u);
+  }
   __syncthreads();
-  for (uint32_t cur = 0;; cur ^= 1u) {
-    const uint32_t t = s_ticket[cur];
+  for (uint32_t cur = 0;; cur = ring_next(cur)) {
+    const uint32_t t = ring.ticket[cur];
     if (t >= q.n_items) break;
-    uint32_t next = 0;
-    if (threadIdx.x == 0) next = atomicAdd(q.next, 1u);
-    const QueueItem it = q.items[t];
-    const uint32_t kind = it.bucket_kind & 0xFFu;
-    const QueueBucket B = q.buckets[it.bucket_kind >> 8];
+    const QueueItem it = ring.item[cur];
+    const uint32_t kind = it.bucket_kind & 0xFFu, bucket = it.bucket_kind >> 8;
+    const QueueBucket& B = s_buckets[bucket];
     uint32_t* publish = nullptr;
     if (kind != kItemWhole) {
       const uint32_t tpl = B.log_n - kTileLog;  // tiles per limb: 2^tpl
@@ -139,9 +173,7 @@ __global__ void __launch_bounds__(kQueueThreads, 2) k_batch_queue(QueueLaunch q)
       }
       if (kind != kItemColInv) publish = cnt + (kind == kItemColFwd ? 0 : 1);
     }
-    dispatch(kind, q.buckets, it.bucket_kind >> 8, B.log_n, it.bid);
-    // s_ticket[cur ^ 1] was last read before the previous iteration's barrier
-    if (threadIdx.x == 0) s_ticket[cur ^ 1u] = next;
+    dispatch(kind, s_buckets, bucket, B.log_n, it.bid, &q, &ring, cur);
     __syncthreads();  // every thread's stores issued; the tiles are free again
     if (publish && threadIdx.x == 0) {
       __threadfence();

@@ -32,9 +32,10 @@ struct QueueItem {
 };
 
 struct QueueLaunch {
-  const QueueBucket* buckets;
+  const QueueBucket* buckets;  // 8-byte aligned; copied to shared memory at the kernel's start
   const QueueItem* items;
   uint32_t n_items;
+  uint32_t n_buckets;  // at most kQueueMaxBuckets
   uint32_t* next;      // ticket dispenser, zero before the launch
   uint32_t* done;      // per-limb completion counters, zero before the launch
   uint32_t* status;    // first error of a bounded wait (YELL_ERR_TIMEOUT), sticky
@@ -46,6 +47,7 @@ struct QueueLaunch {
 // degrees are fixed in batch_queue.cu).
 constexpr uint32_t kQueueMinLogN = 3, kQueueMaxLogN = 20, kQueueFirstTwoPass = 13;
 constexpr uint32_t kQueueTileLog = 12;  // tile words of every item (2^11 at N = 8)
+constexpr uint32_t kQueueMaxBuckets = kQueueMaxLogN - kQueueMinLogN + 1;  // one bucket per degree
 
 // Dynamic shared memory of the queue kernel (two 4096-word tiles).
 size_t queue_smem_bytes();

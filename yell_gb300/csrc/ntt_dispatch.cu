@@ -97,6 +97,7 @@ void build_table() {
   add_two_pass_variants_b(g_table);
   add_two_pass_variants_c(g_table);
   add_two_pass_variants_d(g_table);
+  add_two_pass_variants_e(g_table);
 }
 
 int current_device() {

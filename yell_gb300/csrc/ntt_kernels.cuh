@@ -20,6 +20,8 @@
 // column tile); the other ends are staged through shared memory so that the
 // HBM accesses stay coalesced.
 #pragma once
+#include <atomic>
+#include <cstring>
 #include <utility>
 
 #include "kernels.h"
@@ -669,6 +671,204 @@ __global__ void __launch_bounds__(C::THREADS, min_blocks(512, C::THREADS))
 }
 
 // ===========================================================================
+// Pipelined two-pass polymul: the same three kernels as persistent CTAs that
+// copy the next tile's words into shared memory (cp.async, 16 bytes per copy,
+// into the padded layout) while they compute the current tile.  A tile's
+// first round then reads shared memory instead of waiting on HBM, and the
+// copy of tile t + grid overlaps the last round and the stores of tile t.
+// Same butterflies, same words as the kernels above.
+// ===========================================================================
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Waits for this thread's copies; a CTA barrier after it publishes everyone's.
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Column tile (rows of 2^LB words, stride 2^LOGB) -> padded shared layout.
+template <class C, int LOGB>
+__device__ __forceinline__ void stage_cols_async(uint64_t* s, const uint64_t* g) {
+  static_assert(C::LB >= 1, "column pairs per 16-byte copy");
+  for (uint32_t v = threadIdx.x * 2; v < (1u << C::T); v += C::THREADS * 2)
+    cp_async16(s + sidx(v), g + ((size_t)(v >> C::LB) << LOGB) + (v & ((1u << C::LB) - 1u)));
+}
+
+// Contiguous 2^T-word region -> padded shared layout.
+template <class C>
+__device__ __forceinline__ void stage_region_async(uint64_t* s, const uint64_t* g) {
+  for (uint32_t v = threadIdx.x * 2; v < (1u << C::T); v += C::THREADS * 2) cp_async16(s + sidx(v), g + v);
+}
+
+template <class C, int LOGB>
+__global__ void __launch_bounds__(C::THREADS, min_blocks(512, C::THREADS))
+    k_col_pass2_pipe(ConstLimbSet a, ConstLimbSet b, LimbSet ca, LimbSet cb, const DevMod* __restrict__ mods,
+                     uint32_t tiles) {
+  extern __shared__ __align__(16) uint64_t smem[];
+  constexpr int K = C::K, LB = C::LB, NR = C::NR;
+  constexpr uint32_t log_n = K + LOGB;
+  constexpr int TPL = LOGB - LB;
+  static_assert(NR >= 2, "the last round reads shared memory before the next tile is staged");
+  uint64_t* sa = smem;
+  uint64_t* sb = smem + tile_smem_words(1u << kTileLog);
+  const uint32_t tid = threadIdx.x;
+  constexpr int E = 1 << C::LOGE;
+  uint64_t xa[E], xb[E];
+  uint32_t bid = blockIdx.x;
+  if (bid < tiles) {
+    const uint32_t limb = ca.ordered(bid >> TPL), col0 = (bid & ((1u << TPL) - 1u)) << LB;
+    stage_cols_async<C, LOGB>(sa, a.limb(limb, log_n) + col0);
+    stage_cols_async<C, LOGB>(sb, b.limb(limb, log_n) + col0);
+    cp_async_commit();
+  }
+  for (; bid < tiles; bid += gridDim.x) {
+    const uint32_t limb = ca.ordered(bid >> TPL), col0 = (bid & ((1u << TPL) - 1u)) << LB;
+    const DevMod m = load_mod(mods, ca.cm(limb));
+    const uint64_t np = 0 - m.p, p2 = m.p << 1;
+    cp_async_wait_all();
+    __syncthreads();
+    using R0 = Round<C, 0>;
+    const uint32_t b0 = R0::base(tid);
+    smem_load<R0>(xa, sa, b0);
+    smem_load<R0>(xb, sb, b0);
+    ct_stages2<R0::R, R0::E, 0>(xa, xb, m.fwd, R0::HI, R0::gr(b0, 0), np, p2);
+    smem_store<R0>(xa, sa, b0);  // the words this thread read: no barrier needed before
+    smem_store<R0>(xb, sb, b0);
+    __syncthreads();
+    fwd_rounds<C, 1, NR - 1>(sa, tid, 0, 0, m.fwd, m.p, true);
+    fwd_rounds<C, 1, NR - 1>(sb, tid, 0, 0, m.fwd, m.p, true);
+    using RL = Round<C, NR - 1>;
+    const uint32_t bl = RL::base(tid);
+    smem_load<RL>(xa, sa, bl);
+    smem_load<RL>(xb, sb, bl);
+    __syncthreads();  // the tile is in registers: the buffers take the next one
+    const uint32_t nb = bid + gridDim.x;
+    if (nb < tiles) {
+      const uint32_t nl = ca.ordered(nb >> TPL), nc = (nb & ((1u << TPL) - 1u)) << LB;
+      stage_cols_async<C, LOGB>(sa, a.limb(nl, log_n) + nc);
+      stage_cols_async<C, LOGB>(sb, b.limb(nl, log_n) + nc);
+      cp_async_commit();
+    }
+    ct_stages2<RL::R, RL::E, 0>(xa, xb, m.fwd, RL::HI, RL::gr(bl, 0), np, p2);
+    gstore_cols<RL, LOGB>(xa, ca.limb(limb, log_n) + col0, bl);
+    gstore_cols<RL, LOGB>(xb, cb.limb(limb, log_n) + col0, bl);
+  }
+}
+
+template <class C, int K1>
+__global__ void __launch_bounds__(C::THREADS, min_blocks(512, C::THREADS))
+    k_polymul_rows_pipe(LimbSet ca, ConstLimbSet sbuf, const DevMod* __restrict__ mods, uint32_t tiles) {
+  extern __shared__ __align__(16) uint64_t smem[];
+  constexpr int K = C::K, NR = C::NR;
+  constexpr int BK = C::LOCAL_BARRIER;
+  constexpr uint32_t log_n = K + K1;
+  constexpr int TPL = log_n - kTileLog;
+  uint64_t* sa = smem;
+  uint64_t* sb = smem + tile_smem_words(1u << kTileLog);
+  const uint32_t tid = threadIdx.x;
+  constexpr int E = 1 << C::LOGE;
+  uint64_t xa[E], xb[E];
+  uint32_t bid = blockIdx.x;
+  if (bid < tiles) {
+    const uint32_t limb = ca.ordered(bid >> TPL), off = (bid & ((1u << TPL) - 1u)) << kTileLog;
+    stage_region_async<C>(sa, ca.limb(limb, log_n) + off);
+    stage_region_async<C>(sb, sbuf.limb(limb, log_n) + off);
+    cp_async_commit();
+  }
+  for (; bid < tiles; bid += gridDim.x) {
+    const uint32_t limb = ca.ordered(bid >> TPL), off = (bid & ((1u << TPL) - 1u)) << kTileLog;
+    const DevMod m = load_mod(mods, ca.cm(limb));
+    const uint32_t G = (off >> K) + C::sub(tid);
+    cp_async_wait_all();
+    __syncthreads();
+    using R0 = Round<C, 0>;
+    const uint32_t b0 = R0::base(tid);
+    smem_load<R0>(xa, sa, b0);
+    smem_load<R0>(xb, sb, b0);
+    ct_stages2<R0::R, R0::E, 0>(xa, xb, m.fwd, K1 + R0::HI, R0::gr(b0, G), 0 - m.p, m.p << 1);
+    smem_store<R0>(xa, sa, b0);
+    smem_store<R0>(xb, sb, b0);
+    round_barrier<C, BK>(tid);
+    fwd_rounds<C, 1, NR - 1, BK>(sa, tid, K1, G, m.fwd, m.p, true);
+    fwd_rounds<C, 1, NR - 1, BK>(sb, tid, K1, G, m.fwd, m.p, true);
+    using RB = Round<C, NR - 1>;
+    const uint32_t bb = RB::base(tid);
+    smem_load<RB>(xa, sa, bb);
+    smem_load<RB>(xb, sb, bb);
+    fused_product<C, false>(xa, xb, bb, log_n, K1, G, m);
+    smem_store<RB>(xa, sa, bb);
+    round_barrier<C, BK>(tid);
+    inv_rounds<C, NR - 2, 0, false, BK>(sa, tid, log_n, 0, G, m, true);
+    smem_load<R0>(xa, sa, b0);
+    __syncthreads();  // every row is in registers: the buffers take the next tile
+    const uint32_t nb = bid + gridDim.x;
+    if (nb < tiles) {
+      const uint32_t nl = ca.ordered(nb >> TPL), no = (nb & ((1u << TPL) - 1u)) << kTileLog;
+      stage_region_async<C>(sa, ca.limb(nl, log_n) + no);
+      stage_region_async<C>(sb, sbuf.limb(nl, log_n) + no);
+      cp_async_commit();
+    }
+    gs_round<R0, false>(xa, log_n, R0::BETA, R0::gr(b0, G), m);
+    gstore_rows<R0>(xa, ca.limb(limb, log_n) + off, b0);
+  }
+}
+
+// Inverse column pass, in place on ca.
+template <class C, int LOGB>
+__global__ void __launch_bounds__(C::THREADS, min_blocks(1024, C::THREADS))
+    k_col_inv_pipe(LimbSet ca, const DevMod* __restrict__ mods, uint32_t tiles) {
+  extern __shared__ __align__(16) uint64_t smem[];
+  constexpr int K = C::K, LB = C::LB, NR = C::NR;
+  constexpr uint32_t log_n = K + LOGB;
+  constexpr int TPL = LOGB - LB;
+  static_assert(NR >= 2, "the top round reads shared memory before the next tile is staged");
+  const uint32_t tid = threadIdx.x;
+  uint64_t x[1 << C::LOGE];
+  uint32_t bid = blockIdx.x;
+  if (bid < tiles) {
+    const uint32_t limb = ca.ordered(bid >> TPL), col0 = (bid & ((1u << TPL) - 1u)) << LB;
+    stage_cols_async<C, LOGB>(smem, ca.limb(limb, log_n) + col0);
+    cp_async_commit();
+  }
+  for (; bid < tiles; bid += gridDim.x) {
+    const uint32_t limb = ca.ordered(bid >> TPL), col0 = (bid & ((1u << TPL) - 1u)) << LB;
+    const DevMod m = load_mod(mods, ca.cm(limb));
+    cp_async_wait_all();
+    __syncthreads();
+    using RB = Round<C, NR - 1>;  // bottom round, executed first
+    const uint32_t bb = RB::base(tid);
+    smem_load<RB>(x, smem, bb);
+    gs_round<RB, false>(x, log_n, LOGB + RB::BETA, RB::gr(bb, 0), m);
+    smem_store<RB>(x, smem, bb);
+    __syncthreads();
+    inv_rounds<C, NR - 2, 0, false>(smem, tid, log_n, LOGB, 0, m, true);
+    using RT = Round<C, 0>;
+    const uint32_t bt = RT::base(tid);
+    smem_load<RT>(x, smem, bt);
+    __syncthreads();  // the tile is in registers: the buffer takes the next one
+    const uint32_t nb = bid + gridDim.x;
+    if (nb < tiles) {
+      const uint32_t nl = ca.ordered(nb >> TPL), nc = (nb & ((1u << TPL) - 1u)) << LB;
+      stage_cols_async<C, LOGB>(smem, ca.limb(nl, log_n) + nc);
+      cp_async_commit();
+    }
+    gs_round<RT, true>(x, log_n, LOGB + RT::BETA, RT::gr(bt, 0), m);
+    gstore_cols<RT, LOGB>(x, ca.limb(limb, log_n) + col0, bt);
+  }
+}
+
+// Resident CTAs of `kernel` on the current device (the persistent grids).
+template <typename KernelT>
+uint32_t resident_ctas(KernelT kernel, int threads, size_t smem) {
+  int dev = 0, sms = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess || per < 1)
+    return 152;
+  return (uint32_t)(sms * per);
+}
+
+// ===========================================================================
 // Launch templates.  A variant is (degree, tile size T) for whole-limb
 // degrees and (degree, column stages K1) for two-pass degrees.
 // ===========================================================================
@@ -797,6 +997,64 @@ cudaError_t set_attrs_two_pass() {
   return set_smem(k_polymul_rows<RC, K1>, 2 * kTileSmemBytes);
 }
 
+// Persistent grid of a pipelined kernel: its resident CTAs on this device,
+// computed once per device (the attributes are set before the first launch).
+template <typename KernelT>
+uint32_t persistent_grid(KernelT kernel, int threads, size_t smem, uint32_t tiles) {
+  static std::atomic<uint32_t> cached[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+  uint32_t g = cached[dev].load(std::memory_order_relaxed);
+  if (g == 0) {
+    g = resident_ctas(kernel, threads, smem);
+    cached[dev].store(g, std::memory_order_relaxed);
+  }
+  return g < tiles ? g : tiles;
+}
+
+template <int LOGN, int K1, int LC = 4, int LR = 4>
+cudaError_t launch_two_pass_polymul_pipe(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
+                                         const DevMod* mods, uint64_t* scratch, uint64_t* const* scratch_ptrs,
+                                         cudaStream_t st) {
+  constexpr int LOGB = LOGN - K1;
+  using CC = ColCfg<LOGN, K1, LC>;
+  using RC = RowCfg<LOGN, K1, LR>;
+  const uint32_t tiles = c.count << (LOGN - kTileLog);
+  if (tiles == 0) return cudaSuccess;
+  LimbSet sl = c;
+  sl.base = scratch_ptrs ? nullptr : scratch;
+  sl.ptrs = scratch_ptrs;
+  {
+    LaunchScope ps("polymul_col_fwd", st);
+    const uint32_t g = persistent_grid(k_col_pass2_pipe<CC, LOGB>, CC::THREADS, 2 * kTileSmemBytes, tiles);
+    k_col_pass2_pipe<CC, LOGB><<<g, CC::THREADS, 2 * kTileSmemBytes, st>>>(a, b, c, sl, mods, tiles);
+  }
+  {
+    LaunchScope ps("polymul_rows", st);
+    const uint32_t g = persistent_grid(k_polymul_rows_pipe<RC, K1>, RC::THREADS, 2 * kTileSmemBytes, tiles);
+    k_polymul_rows_pipe<RC, K1><<<g, RC::THREADS, 2 * kTileSmemBytes, st>>>(c, as_const(sl), mods, tiles);
+  }
+  {
+    LaunchScope ps("polymul_col_inv", st);
+    const uint32_t g = persistent_grid(k_col_inv_pipe<CC, LOGB>, CC::THREADS, kTileSmemBytes, tiles);
+    k_col_inv_pipe<CC, LOGB><<<g, CC::THREADS, kTileSmemBytes, st>>>(c, mods, tiles);
+  }
+  g_kernel_launches += 3;
+  return cudaGetLastError();
+}
+
+template <int LOGN, int K1, int LC = 4, int LR = 4>
+cudaError_t set_attrs_two_pass_pipe() {
+  constexpr int LOGB = LOGN - K1;
+  using CC = ColCfg<LOGN, K1, LC>;
+  using RC = RowCfg<LOGN, K1, LR>;
+  cudaError_t e;
+  if ((e = set_attrs_two_pass<LOGN, K1, LC, LR>()) != cudaSuccess) return e;
+  if ((e = set_smem(k_col_pass2_pipe<CC, LOGB>, 2 * kTileSmemBytes)) != cudaSuccess) return e;
+  if ((e = set_smem(k_polymul_rows_pipe<RC, K1>, 2 * kTileSmemBytes)) != cudaSuccess) return e;
+  return set_smem(k_col_inv_pipe<CC, LOGB>, kTileSmemBytes);
+}
+
 template <int LOGN, int T>
 Variant whole_variant() {
   Variant v;
@@ -826,6 +1084,18 @@ Variant two_pass_variant() {
   v.ntt_launches = 2;
   v.polymul_launches = 3;
   v.polymul_scratch = true;
+  return v;
+}
+
+// The same split with the pipelined (persistent, copy-ahead) polymul kernels;
+// the NTT keeps the one-tile-per-CTA kernels.
+template <int LOGN, int K1, int LC = 4, int LR = 4>
+Variant two_pass_pipe_variant() {
+  Variant v = two_pass_variant<LOGN, K1, LC, LR>();
+  const size_t n = std::strlen(v.name);
+  std::snprintf(v.name + n - 1, sizeof(v.name) - (n - 1), "; pipelined)");
+  v.polymul = &launch_two_pass_polymul_pipe<LOGN, K1, LC, LR>;
+  v.set_attrs = &set_attrs_two_pass_pipe<LOGN, K1, LC, LR>;
   return v;
 }
 

@@ -31,6 +31,7 @@ void add_two_pass_variants_a(std::vector<Variant>* by_degree);   // 2^14, 2^15
 void add_two_pass_variants_b(std::vector<Variant>* by_degree);   // 2^16, 2^17
 void add_two_pass_variants_c(std::vector<Variant>* by_degree);   // 2^18 .. 2^20
 void add_two_pass_variants_d(std::vector<Variant>* by_degree);   // more 2^16 splits and round widths
+void add_two_pass_variants_e(std::vector<Variant>* by_degree);   // pipelined polymul, 2^16
 
 // Variant table of a degree, and the variant selected on the current device.
 const std::vector<Variant>& variants_of(uint32_t log_n);
