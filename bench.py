@@ -294,6 +294,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
 
     import yell_gb300 as y
 
+    if local_rank >= torch.cuda.device_count():
+        print(f"bench.py: rank {rank} needs GPU {local_rank}, the box has {torch.cuda.device_count()}",
+              file=sys.stderr)
+        return 2
     torch.cuda.set_device(local_rank)
     # Replicas: no collective on the data path.  The ranks only meet on the
     # host (barriers around the timed region, the max of their times), so a

@@ -37,3 +37,11 @@ def test_world_size_mismatch_is_an_error():
                        cwd=ROOT, env=env, timeout=300)
     assert r.returncode != 0
     assert "WORLD_SIZE" in r.stderr
+
+
+def test_rank_without_a_gpu_is_an_error():
+    """Our arm on a machine with fewer GPUs than ranks (here: none) stops
+    with a message instead of failing inside CUDA."""
+    r = _run(["--gpus", "1", "--steps", "1", "--warmup", "3"], timeout=300)
+    assert r.returncode == 2, r.stderr[-2000:]
+    assert "needs GPU 0" in r.stderr
