@@ -658,7 +658,8 @@ def run_rows(torch, y, stream, dc, reps: int = 10, groups: int = 3):
 def run_uneven(torch, y, stream, barrier, max_over_ranks, world, no_autotune=False):
     """512 polymuls of mixed degree and limb count (seed 4): one batched call
     (bucketed, CUDA graph per batch shape), one launch of the persistent
-    work-queue kernel, and 512 plain per-call calls."""
+    work-queue kernel, the queue's items as three phase launches, and 512
+    plain per-call calls."""
     from yell_gb300.workloads import mix_limb_ntts, mix_operands, uneven_mix
 
     mix = uneven_mix(4, 512)
@@ -685,13 +686,17 @@ def run_uneven(torch, y, stream, barrier, max_over_ranks, world, no_autotune=Fal
     def queue():
         y.dev_polymul_batch_queue(items, stream=stream)
 
+    def phased():
+        y.dev_polymul_batch_phased(items, stream=stream)
+
     def per_call():
         for (dc, da, db, log_n, L, cm0), sc in zip(items, singles):
             y.dev_polymul(dc, da, db, 1, L, log_n, cm0, scratch=sc, stream=stream)
 
     out = {"workload": "512 polymuls, log2 N uniform in 10..16, L uniform in 1..16 (seed 4)",
            "limb_ntts": limb_ntts}
-    for name, fn, steps in (("batched", batched, 10), ("persistent_queue", queue, 10), ("per_call", per_call, 3)):
+    for name, fn, steps in (("batched", batched, 10), ("persistent_queue", queue, 10), ("phased_queue", phased, 10),
+                            ("per_call", per_call, 3)):
         for _ in range(2):
             fn()
         barrier()
@@ -705,6 +710,7 @@ def run_uneven(torch, y, stream, barrier, max_over_ranks, world, no_autotune=Fal
     out["batched"]["path"] = "degree buckets on forked streams, one CUDA graph per batch shape"
     out["persistent_queue"]["path"] = "one launch: resident CTAs take work items from a device queue"
     out["persistent_queue"]["status"] = y.batch_queue_status()
+    out["phased_queue"]["path"] = "the queue's items as three launches, one per phase, no device waits"
     out["batched_vs_per_call"] = out["batched"]["value"] / out["per_call"]["value"]
     out["queue_vs_per_call"] = out["persistent_queue"]["value"] / out["per_call"]["value"]
     out["_items"] = items

@@ -201,6 +201,12 @@ int yell_dev_polymul_batch(const yell_polymul_desc* descs, uint32_t n, void* str
  * records YELL_ERR_TIMEOUT, read (and cleared) by yell_batch_queue_status,
  * which waits for the queued work.  Asynchronous on `stream`. */
 int yell_dev_polymul_batch_queue(const yell_polymul_desc* descs, uint32_t n, void* stream);
+/* The same work items as THREE launches in queue order, one per phase
+ * (forward column passes and whole-limb tiles; row steps; inverse column
+ * passes), each kernel with its own register budget.  Launch order carries
+ * the dependencies, so nothing waits on the device.  Asynchronous on
+ * `stream`; results identical to yell_dev_polymul_batch. */
+int yell_dev_polymul_batch_phased(const yell_polymul_desc* descs, uint32_t n, void* stream);
 int yell_batch_queue_status(uint32_t* status);
 /* Check of the bounded wait: a queue whose row steps wait on column passes
  * that are never queued; every wait runs out after timeout_ns (<= 10 s) and

@@ -1,7 +1,8 @@
-"""The uneven batch as ONE launch of the persistent work-queue kernel: results
-against the oracle and against the graph-bucketed batch, repeated launches
-(counters reset), and the bounded dependency wait (a queue whose waits cannot
-be satisfied records YELL_ERR_TIMEOUT instead of hanging)."""
+"""The uneven batch as ONE launch of the persistent work-queue kernel, and the
+same work items as three phase launches: results against the oracle and
+against the graph-bucketed batch, repeated launches (counters reset), and the
+bounded dependency wait (a queue whose waits cannot be satisfied records
+YELL_ERR_TIMEOUT instead of hanging)."""
 import time
 
 import numpy as np
@@ -59,6 +60,30 @@ def test_config4_queue_equals_graph_batch(cuda, orc):
         assert np.array_equal(want[i], orc.polymul(a, b, log_n, 0)), i
 
 
+def test_phased_every_degree_matches_oracle(cuda, orc):
+    """The queue's items as three phase launches: every degree 2^3..2^20, mixed
+    limb counts and moduli, word for word against the oracle."""
+    mix = [(d, 1 + d % 3) for d in range(3, 21)] + [(13, 4), (10, 2), (16, 1), (3, 5)]
+    cm0s = [(i + 2) % 5 for i in range(len(mix))]
+    ops = []
+    for i, ((log_n, L), cm0) in enumerate(zip(mix, cm0s)):
+        ps = y.primes(L, cm0)
+        ops.append((uniform_polys(3700 + i, 1, L, log_n, ps)[0], uniform_polys(3800 + i, 1, L, log_n, ps)[0]))
+    got = _run(cuda, mix, ops, cm0s, y.dev_polymul_batch_phased)
+    for (log_n, L), (a, b), cm0, g in zip(mix, ops, cm0s, got):
+        assert np.array_equal(g, orc.polymul(a, b, log_n, cm0)), (log_n, L, cm0)
+
+
+def test_config4_phased_equals_graph_batch(cuda):
+    mix = uneven_mix(4, 512)
+    ops = mix_operands(mix, y.primes(16), 4)
+    want = _run(cuda, mix, ops, [0] * len(mix), y.dev_polymul_batch)
+    for rep in range(2):
+        got = _run(cuda, mix, ops, [0] * len(mix), y.dev_polymul_batch_phased)
+        for i in range(len(mix)):
+            assert np.array_equal(got[i], want[i]), (rep, i)
+
+
 def test_bounded_wait_records_timeout(cuda, orc):
     t0 = time.perf_counter()
     st = y.batch_queue_wait_check(0.02)
@@ -81,5 +106,7 @@ def test_queue_errors(cuda):
     t = cuda.zeros(1 << 10, dtype=cuda.int64, device="cuda")
     with pytest.raises(y.YellError):
         y.dev_polymul_batch_queue([(t, t, t, 10, 1, 0)])  # output aliases operands
+    with pytest.raises(y.YellError):
+        y.dev_polymul_batch_phased([(t, t, t, 10, 1, 0)])
     with pytest.raises(y.YellError):
         y.batch_queue_wait_check(0.0)

@@ -26,7 +26,7 @@ __all__ = [
     "dev_ntt_limbs", "dev_elementwise", "dev_polymul", "polymul_scratch_words", "kernel_launches", "allocations",
     "Poly", "PinnedBuffer", "sample_uniform", "sample_zo", "sample_hwt", "sample_gaussian",
     "crt_words", "dev_crt_lift", "poly_to_bigint", "words_to_ints", "DevPoly", "BatchTicket",
-    "batch_submit", "dev_polymul_batch_queue", "batch_queue_status", "batch_queue_wait_check",
+    "batch_submit", "dev_polymul_batch_queue", "dev_polymul_batch_phased", "batch_queue_status", "batch_queue_wait_check",
 ]
 
 
@@ -261,6 +261,14 @@ def dev_polymul_batch_queue(items, stream=None) -> None:
     for i, (c, a, b, log_n, L, cm0) in enumerate(items):
         descs[i] = _capi.PolymulDesc(_dptr(c), _dptr(a), _dptr(b), log_n, L, cm0, 0)
     call("yell_dev_polymul_batch_queue", ctypes.addressof(descs), len(items), _stream(stream))
+
+
+def dev_polymul_batch_phased(items, stream=None) -> None:
+    """The queue's work items as three stream-ordered launches, one per phase."""
+    descs = (_capi.PolymulDesc * len(items))()
+    for i, (c, a, b, log_n, L, cm0) in enumerate(items):
+        descs[i] = _capi.PolymulDesc(_dptr(c), _dptr(a), _dptr(b), log_n, L, cm0, 0)
+    call("yell_dev_polymul_batch_phased", ctypes.addressof(descs), len(items), _stream(stream))
 
 
 def batch_queue_status() -> int:

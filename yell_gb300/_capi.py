@@ -115,6 +115,7 @@ SIGNATURES = {
     "yell32_poly_add_product_of": (_int, [_vp, _vp, _vp, _u32, _u32]),
     "yell32_poly_negate": (_int, [_vp, _u32, _u32]),
     "yell_dev_polymul_batch_queue": (_int, [_vp, _u32, _vp]),
+    "yell_dev_polymul_batch_phased": (_int, [_vp, _u32, _vp]),
     "yell_batch_queue_status": (_int, [_vp]),
     "yell_batch_queue_wait_check": (_int, [_u64, _vp]),
     "yell_dev_poly_alloc": (_int, [_u32, _u32, _u32, _vp]),

@@ -241,12 +241,17 @@ int BatchExecutor::reserve_queue_ctl(size_t words) {
 }
 
 int BatchExecutor::run_queue(DeviceContext* ctx, const yell_polymul_desc* descs, uint32_t n, cudaStream_t s,
-                             uint64_t timeout_ns) {
-  TraceRange trace("yell batch queue");
-  if (!queue_attrs_) {
+                             uint64_t timeout_ns, bool phased) {
+  TraceRange trace(phased ? "yell batch phases" : "yell batch queue");
+  if (!phased && !queue_attrs_) {
     const cudaError_t e = queue_set_attributes();
     if (e != cudaSuccess) return fail_cuda(e, "queue kernel attributes");
     queue_attrs_ = true;
+  }
+  if (phased && !phase_attrs_) {
+    const cudaError_t e = phases_set_attributes();
+    if (e != cudaSuccess) return fail_cuda(e, "phase kernel attributes");
+    phase_attrs_ = true;
   }
   // ---- buckets: limb lists, scratch for the two-pass degrees -------------
   std::array<std::vector<uint32_t>, kDegrees> members;
@@ -287,6 +292,7 @@ int BatchExecutor::run_queue(DeviceContext* ctx, const yell_polymul_desc* descs,
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device());
   const uint32_t resident = (uint32_t)std::max(sms, 1) * 2;
   std::vector<QueueItem> items;
+  uint32_t phase_items[4] = {0, 0, 0, 0};
   for (int phase = 0; phase < 4; ++phase)
     for (size_t bi = 0; bi < buckets.size(); ++bi) {
       const Bucket& b = buckets[bi];
@@ -303,6 +309,7 @@ int BatchExecutor::run_queue(DeviceContext* ctx, const yell_polymul_desc* descs,
         tiles = (b.limbs + per - 1) / per;
       }
       for (uint32_t t = 0; t < tiles; ++t) items.push_back(QueueItem{(uint32_t)bi << 8 | kind, t});
+      phase_items[phase] += tiles;
     }
   const size_t buckets_off = (bytes + 15) / 16 * 16;
   bytes = buckets_off + buckets.size() * sizeof(QueueBucket);
@@ -351,7 +358,7 @@ int BatchExecutor::run_queue(DeviceContext* ctx, const yell_polymul_desc* descs,
   e = cudaMemcpyAsync(d_lists_, h_lists_, bytes, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaEventRecord(staged_, s);
   // ticket counter and limb counters start at zero; the status word (index 0) is sticky
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_queue_ctl_ + 1, 0, (1 + counters) * sizeof(uint32_t), s);
+  if (e == cudaSuccess && !phased) e = cudaMemsetAsync(d_queue_ctl_ + 1, 0, (1 + counters) * sizeof(uint32_t), s);
   if (e != cudaSuccess) return fail_cuda(e, "queue upload");
 
   QueueLaunch ql;
@@ -365,9 +372,15 @@ int BatchExecutor::run_queue(DeviceContext* ctx, const yell_polymul_desc* descs,
   ql.timeout_ns = timeout_ns;
   ql.grid = (uint32_t)std::min<size_t>(items.size(), resident);
   const uint64_t l0 = g_kernel_launches.load();
-  e = launch_batch_queue(ql, s);
+  if (phased) {
+    // forward column passes and whole-limb tiles, row steps, inverse column passes
+    const uint32_t counts[3] = {phase_items[0] + phase_items[1], phase_items[2], phase_items[3]};
+    e = launch_batch_phases(qb, (uint32_t)buckets.size(), ql.items, counts, s);
+  } else {
+    e = launch_batch_queue(ql, s);
+  }
   last_launches_ = g_kernel_launches.load() - l0;
-  return e == cudaSuccess ? kOk : fail_cuda(e, "queue launch");
+  return e == cudaSuccess ? kOk : fail_cuda(e, phased ? "phase launch" : "queue launch");
 }
 
 int BatchExecutor::queue_status(cudaStream_t s, uint32_t* status) {
@@ -537,7 +550,9 @@ extern "C" int yell_dev_polymul_batch(const yell_polymul_desc* descs, uint32_t n
   return kOk;
 }
 
-extern "C" int yell_dev_polymul_batch_queue(const yell_polymul_desc* descs, uint32_t n, void* stream) {
+namespace {
+
+int batch_queue_entry(const yell_polymul_desc* descs, uint32_t n, void* stream, bool phased) {
   if (!descs || n == 0) return fail(kInvalidArgument, "empty batch");
   int st = validate_batch(descs, n);
   if (st != kOk) return st;
@@ -558,7 +573,7 @@ extern "C" int yell_dev_polymul_batch_queue(const yell_polymul_desc* descs, uint
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, db->user_ev, 0);
     if (e != cudaSuccess) return fail_cuda(e, "batch stream ordering");
   }
-  st = db->exec.run_queue(ctx, descs, n, s, kQueueWaitNs);
+  st = db->exec.run_queue(ctx, descs, n, s, kQueueWaitNs, phased);
   if (st != kOk) return st;
   if (stream) {
     e = cudaEventRecord(db->done_ev, s);
@@ -566,6 +581,16 @@ extern "C" int yell_dev_polymul_batch_queue(const yell_polymul_desc* descs, uint
     if (e != cudaSuccess) return fail_cuda(e, "batch stream ordering");
   }
   return kOk;
+}
+
+}  // namespace
+
+extern "C" int yell_dev_polymul_batch_queue(const yell_polymul_desc* descs, uint32_t n, void* stream) {
+  return batch_queue_entry(descs, n, stream, false);
+}
+
+extern "C" int yell_dev_polymul_batch_phased(const yell_polymul_desc* descs, uint32_t n, void* stream) {
+  return batch_queue_entry(descs, n, stream, true);
 }
 
 extern "C" int yell_batch_queue_status(uint32_t* status) {

@@ -37,8 +37,10 @@ class BatchExecutor {
   // items of every bucket in one device queue (batch_queue.h).  Asynchronous
   // on s; a dependency wait that exceeds timeout_ns records YELL_ERR_TIMEOUT
   // in the status word read by queue_status().
+  // With phased, the same items run as three stream-ordered launches, one
+  // per phase (batch_phases.cu), and nothing waits on the device.
   int run_queue(DeviceContext* ctx, const yell_polymul_desc* descs, uint32_t n, cudaStream_t s,
-                uint64_t timeout_ns);
+                uint64_t timeout_ns, bool phased = false);
   // Waits for s and returns (and clears) the queue kernel's status word.
   int queue_status(cudaStream_t s, uint32_t* status);
   // A queue whose row steps depend on column passes that are never queued:
@@ -80,6 +82,7 @@ class BatchExecutor {
   uint32_t* d_queue_ctl_ = nullptr;  // [0] status, [1] ticket counter, [2..] per-limb counters
   size_t queue_ctl_words_ = 0;
   bool queue_attrs_ = false;
+  bool phase_attrs_ = false;
   uint64_t generation_ = 0;
   std::array<cudaStream_t, kDegrees> side_{};
   std::array<cudaEvent_t, kDegrees> join_{};

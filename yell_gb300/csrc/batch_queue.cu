@@ -23,13 +23,6 @@ namespace {
 constexpr int kQueueThreads = 256;
 static_assert(kQueueTileLog == (uint32_t)kTileLog, "queue tiles are the two-pass tiles");
 
-// Column stages of the queue's two-pass items: rows of at most 512 words
-// (one warp's) from 2^16 up, so the row step needs only warp barriers.
-template <int LOGN>
-constexpr int k1_of() {
-  return LOGN == 13 ? 6 : (LOGN <= 15 ? 7 : LOGN - 9);
-}
-
 __device__ __forceinline__ uint64_t global_ns() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -65,7 +58,7 @@ __device__ __forceinline__ void run_item(uint32_t kind, const QueueBucket& B, ui
     static_assert(C::THREADS == kQueueThreads, "whole-limb tile of the queue kernel");
     polymul_whole_body<C>(B.c, B.a, B.b, B.mods, bid);
   } else {
-    constexpr int K1 = k1_of<LOGN>(), LOGB = LOGN - K1;
+    constexpr int K1 = queue_k1(LOGN), LOGB = LOGN - K1;
     using CC = ColCfg<LOGN, K1>;
     using RC = RowCfg<LOGN, K1>;
     static_assert(CC::THREADS == kQueueThreads && RC::THREADS == kQueueThreads, "two-pass tiles of the queue kernel");

@@ -44,14 +44,26 @@ struct QueueLaunch {
 };
 
 // Degrees served by the queue kernel (the column stages of its two-pass
-// degrees are fixed in batch_queue.cu).
+// degrees are fixed by queue_k1).
 constexpr uint32_t kQueueMinLogN = 3, kQueueMaxLogN = 20, kQueueFirstTwoPass = 13;
 constexpr uint32_t kQueueTileLog = 12;  // tile words of every item (2^11 at N = 8)
 constexpr uint32_t kQueueMaxBuckets = kQueueMaxLogN - kQueueMinLogN + 1;  // one bucket per degree
+
+// Column stages of the queue's two-pass items: rows of at most 512 words
+// (one warp's) from 2^16 up, so the row step needs only warp barriers.
+__host__ __device__ constexpr int queue_k1(int log_n) { return log_n == 13 ? 6 : (log_n <= 15 ? 7 : log_n - 9); }
 
 // Dynamic shared memory of the queue kernel (two 4096-word tiles).
 size_t queue_smem_bytes();
 cudaError_t queue_set_attributes();
 cudaError_t launch_batch_queue(const QueueLaunch& q, cudaStream_t s);
+
+// The same items as three launches in queue order (batch_phases.cu):
+// counts[0] forward column passes and whole-limb tiles, counts[1] row steps,
+// counts[2] inverse column passes.  The buckets are read on the host and
+// passed by value; `items` is the device copy of the queue.
+cudaError_t phases_set_attributes();
+cudaError_t launch_batch_phases(const QueueBucket* host_buckets, uint32_t n_buckets, const QueueItem* items,
+                                const uint32_t counts[3], cudaStream_t s);
 
 }  // namespace yell_gb300
