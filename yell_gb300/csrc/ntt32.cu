@@ -330,47 +330,61 @@ __global__ void __launch_bounds__(C::THREADS, 1024 / C::THREADS) k32_polymul(uin
 
 // ---- polymul by a CTA pair (thread-block cluster of 2) ------------------------
 // For N = 2^14 and 2^15 one limb is split over two CTAs of one cluster, each
-// holding half of it (2^(log N - 1) words, 80 KB at 2^15), so two CTAs fit on
-// an SM.  The forward stage that pairs words N/2 apart (stage 0, twiddle
-// w[1]) is applied while loading: each CTA reads both halves (the second read
-// of a word comes from L2) and keeps the butterfly output of its own half.
-// Stages 1 .. log N - 1 stay inside a half (group G = the CTA's rank).  The
-// inverse's last layer (N^-1 scaling fused) pairs the halves again: after a
-// cluster barrier each CTA reads the peer's words through distributed shared
-// memory and writes its own half of the outputs.
-template <int LOGN>
-struct PairCfg32 {
-  static constexpr int H = LOGN - 1;
-  using C = TileCfg<H, H, 0, 5>;
-  static constexpr size_t kSmem = Smem<uint32_t>::words(1u << H) * sizeof(uint32_t);
-};
-
-// The stages inside a half limb of 2^H words, as two tiles of the engine:
-// the top 5 (pair distances 2^(H-1) .. 2^(H-5)) as one round across the CTA
-// (CA: columns of stride 2^(H-5)), the other H - 5 in rows of 2^(H-5) words
-// (CB), each row held by 2^(H-10) threads of one warp, so the rounds inside a
-// row need only warp barriers.  The rounds are the same (5, H - 10, 5)
-// stages as one tile over the half would run, with one CTA barrier less per
-// transform.  The bottom round gives each thread 32 consecutive words, as
-// before.
-template <int H>
+// holding half of it (2^(log N - 1) words, 64 KB at 2^15).  The forward stage
+// that pairs words N/2 apart (stage 0, twiddle w[1]) is applied while
+// loading: each CTA reads both halves (the second read of a word comes from
+// L2) and keeps the butterfly output of its own half.  Stages 1 .. log N - 1
+// stay inside a half (group G = the CTA's rank).  The inverse's last layer
+// (N^-1 scaling fused) pairs the halves again: after a cluster barrier each
+// CTA reads the peer's words through distributed shared memory and writes its
+// own half of the outputs.
+//
+// The stages inside a half limb of 2^H words run as two tiles of the engine:
+// the top KTOP (pair distances 2^(H-1) .. 2^(H-KTOP)) across the CTA (CA:
+// columns of stride 2^(H-KTOP), CTA barriers), the other H - KTOP in rows of
+// 2^(H-KTOP) words (CB), each row held by the threads of one warp, so the
+// rounds inside a row need only warp barriers.  The bottom round gives each
+// thread 2^LOGE consecutive words.
+template <int H, int LOGE, int KTOP>
 struct HalfSplit {
-  using CA = TileCfg<H, 5, H - 5, 5>;
-  using CB = TileCfg<H, H - 5, 0, 5>;
-  static constexpr int KB = H - 5;
+  using CA = TileCfg<H, KTOP, H - KTOP, LOGE>;
+  using CB = TileCfg<H, H - KTOP, 0, LOGE>;
+  static constexpr int KB = H - KTOP, KTOP_STAGES = KTOP;
   static_assert(CA::THREADS == CB::THREADS && CB::LOCAL_BARRIER == 1, "rows must stay inside a warp");
   // Row index within the whole limb (the sub-transform group of CB's top stage).
   __device__ static __forceinline__ uint32_t row_group(uint32_t r, uint32_t tid) {
-    return (r << (H - KB)) + CB::sub(tid);
+    return (r << KTOP) + CB::sub(tid);
   }
+};
+
+// 2^14: 256-thread CTAs of 32 words per thread, three per SM at 80 registers.
+// 2^15: 1024-thread CTAs of 16 words per thread, one per SM at 64 registers,
+// top 7 stages across the CTA and rows of 128 words: the same 32 resident
+// warps per SM as two 512-thread CTAs of 32 words, without their 216 bytes of
+// register spills, and 1024 CTA-sized units per 512-limb launch fill 6.7
+// waves of 152 SMs where limb pairs filled 3.4 waves of 304 slots.  Measured
+// on GB300 (N = 2^15, L = 32, 16 pairs): 0.2228 ms, the same as two 512-thread
+// CTAs per SM (0.2228 ms); with the top 6 or 8 stages across the CTA 0.2238
+// and 0.2273 ms.
+template <int LOGN>
+struct PairCfg32 {
+  static constexpr int H = LOGN - 1;
+  static constexpr int LOGE = LOGN >= 15 ? 4 : 5;
+  static constexpr int KTOP = LOGN >= 15 ? 7 : 5;
+  using C = TileCfg<H, H, 0, LOGE>;
+  using S = HalfSplit<H, LOGE, KTOP>;
+  static constexpr int MIN_BLOCKS = C::THREADS <= 256 ? 3 : (C::THREADS <= 512 ? 2 : 1);
+  static constexpr size_t kSmem = Smem<uint32_t>::words(1u << H) * sizeof(uint32_t);
 };
 
 // Forward NTT of one half limb of `src` (the limb's first word) into the
 // bottom-round registers x of this thread: stage 0 while loading, stages
 // 1 .. log N - 1 in shared memory, the last round in registers.
-template <class C, bool CLUSTER_SYNC = false>
+template <class PC, bool CLUSTER_SYNC = false>
 __device__ __forceinline__ void pair_forward(uint32_t* x, const uint32_t* __restrict__ src, uint32_t* smem32,
                                              uint32_t tid, uint32_t r, const DevMod32& m, uint2 w1) {
+  using C = typename PC::C;
+  using S = typename PC::S;
   constexpr int H = C::K, NR = C::NR;
   constexpr uint32_t half = 1u << H;
   constexpr int IT = (int)(half / (C::THREADS * 4));
@@ -399,23 +413,71 @@ __device__ __forceinline__ void pair_forward(uint32_t* x, const uint32_t* __rest
   // an in-place transform may overwrite src only once both CTAs have read it
   if constexpr (CLUSTER_SYNC) cooperative_groups::this_cluster().sync();
   else __syncthreads();
-  using S = HalfSplit<H>;
+  using CA = typename S::CA;
   using CB = typename S::CB;
   using RBB = Round<CB, CB::NR - 1>;
   static_assert(RBB::R == RB::R && RBB::BETA == 0 && RBB::EB == 0, "same bottom round as one tile over the half");
-  fwd_rounds<typename S::CA, 0, 1>(smem32, tid, 1, r, m.fwd, p, true);  // stages 1..5, CTA barrier
+  constexpr uint32_t s_rows = 1 + S::KTOP_STAGES;  // first stage of the rows
+  fwd_rounds<CA, 0, CA::NR>(smem32, tid, 1, r, m.fwd, p, true);  // stages 1..KTOP, CTA barriers
   const uint32_t G = S::row_group(r, tid);
-  fwd_rounds<CB, 0, CB::NR - 1, CB::LOCAL_BARRIER>(smem32, tid, 6, G, m.fwd, p, true);
+  fwd_rounds<CB, 0, CB::NR - 1, CB::LOCAL_BARRIER>(smem32, tid, s_rows, G, m.fwd, p, true);
   const uint32_t bb = RBB::base(tid);
   smem_load<RBB>(x, smem32, bb);
-  ct_round<RBB>(x, m.fwd, 6u + RBB::HI, RBB::gr(bb, G), p);
+  ct_round<RBB>(x, m.fwd, s_rows + RBB::HI, RBB::gr(bb, G), p);
 }
 
-template <class C>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, C::THREADS <= 256 ? 3 : 2)
+// Inverse stages inside the half limb from the bottom-round registers x:
+// rows (warp barriers), then the top KTOP across the CTA; the words end in
+// shared memory.  CB's last round is followed by a CTA barrier.
+template <class PC>
+__device__ __forceinline__ void pair_inverse(uint32_t* x, uint32_t* smem32, uint32_t tid, uint32_t r,
+                                             uint32_t bb, const DevMod32& m) {
+  using C = typename PC::C;
+  using S = typename PC::S;
+  using CA = typename S::CA;
+  using CB = typename S::CB;
+  using RBB = Round<CB, CB::NR - 1>;
+  constexpr uint32_t log_n = C::K + 1;
+  const uint32_t G = S::row_group(r, tid);
+  gs_round<RBB, false>(x, log_n, (uint32_t)RBB::BETA, RBB::gr(bb, G), m);
+  smem_store<RBB>(x, smem32, bb);
+  round_barrier<CB, CB::LOCAL_BARRIER>(tid);
+  inv_rounds<CB, CB::NR - 2, 0, false, CB::LOCAL_BARRIER>(smem32, tid, log_n, 0, G, m, true);
+  inv_rounds<CB, 0, -1, false>(smem32, tid, log_n, 0, G, m, true);  // CTA barrier after
+  inv_rounds<CA, CA::NR - 1, -1, false>(smem32, tid, log_n, S::KB, r, m, true);
+}
+
+// Last inverse layer across the pair with the N^-1 scaling: u = word i
+// (rank 0), w = word i + N/2 (rank 1); each CTA writes its own half.
+template <class PC, bool UNROLL>
+__device__ __forceinline__ void pair_last_layer(uint32_t* dst, const uint32_t* smem32, const uint32_t* peer,
+                                                uint32_t tid, uint32_t r, const DevMod32& m) {
+  using C = typename PC::C;
+  constexpr int IT = (int)((1u << C::K) / (C::THREADS * 4));
+  const uint32_t p2 = m.p << 1;
+#pragma unroll(UNROLL ? IT : 1)
+  for (int i = 0; i < IT; ++i) {
+    const uint32_t v = (tid + i * C::THREADS) * 4;
+    const uint4 own = *reinterpret_cast<const uint4*>(smem32 + Smem<uint32_t>::idx(v));
+    const uint4 oth = *reinterpret_cast<const uint4*>(peer + Smem<uint32_t>::idx(v));
+    const uint32_t o[4] = {own.x, own.y, own.z, own.w}, q[4] = {oth.x, oth.y, oth.z, oth.w};
+    uint32_t res[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint32_t u = r == 0 ? o[k] : q[k], w = r == 0 ? q[k] : o[k];
+      res[k] = r == 0 ? mulmod_shoup(u + w, m.inv_n, m.inv_n_s, m.p)
+                      : mulmod_shoup(u - w + p2, m.inv_n_iphi, m.inv_n_iphi_s, m.p);
+    }
+    *reinterpret_cast<uint4*>(dst + v) = make_uint4(res[0], res[1], res[2], res[3]);
+  }
+}
+
+template <class PC>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PC::C::THREADS, PC::MIN_BLOCKS)
     k32_polymul_pair(uint32_t* c, const uint32_t* a, const uint32_t* b, Limbs32 ls,
                      const DevMod32* __restrict__ mods) {
   namespace cg = cooperative_groups;
+  using C = typename PC::C;
   extern __shared__ __align__(16) uint32_t smem32[];
   constexpr int H = C::K, NR = C::NR, E = 1 << C::LOGE;
   constexpr uint32_t log_n = H + 1, half = 1u << H;
@@ -435,13 +497,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, C::THREA
   const uint32_t bb = RB::base(tid);
   uint32_t* park = c + lbase + r * half + bb;
   uint32_t x[E];
-  pair_forward<C>(x, a + lbase, smem32, tid, r, m, w1);
+  pair_forward<PC>(x, a + lbase, smem32, tid, r, m, w1);
 #pragma unroll
   for (int i = 0; i < E; i += 4)
     *reinterpret_cast<uint4*>(park + i) = make_uint4(fwd_correct(x[i], p, p2), fwd_correct(x[i + 1], p, p2),
                                                      fwd_correct(x[i + 2], p, p2), fwd_correct(x[i + 3], p, p2));
   __syncthreads();  // the buffer is reused for b
-  pair_forward<C>(x, b + lbase, smem32, tid, r, m, w1);
+  pair_forward<PC>(x, b + lbase, smem32, tid, r, m, w1);
 #pragma unroll
   for (int i = 0; i < E; i += 4) {
     const uint4 ah = *reinterpret_cast<const uint4*>(park + i);  // written above by this thread
@@ -450,47 +512,20 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, C::THREA
     x[i + 2] = mulmod_barrett(ah.z, fwd_correct(x[i + 2], p, p2), p, m.pn);
     x[i + 3] = mulmod_barrett(ah.w, fwd_correct(x[i + 3], p, p2), p, m.pn);
   }
-  {
-    // inverse stages inside the half: rows (warp barriers), then the top 5
-    // across the CTA; the same bottom-round words as RB
-    using S = HalfSplit<H>;
-    using CB = typename S::CB;
-    using RBB = Round<CB, CB::NR - 1>;
-    const uint32_t G = S::row_group(r, tid);
-    gs_round<RBB, false>(x, log_n, (uint32_t)RBB::BETA, RBB::gr(bb, G), m);
-    smem_store<RBB>(x, smem32, bb);
-    round_barrier<CB, CB::LOCAL_BARRIER>(tid);
-    inv_rounds<CB, CB::NR - 2, -1, false>(smem32, tid, log_n, 0, G, m, true);  // CTA barrier after
-    inv_rounds<typename S::CA, 0, -1, false>(smem32, tid, log_n, S::KB, r, m, true);
-  }
-  // last layer across the pair: u = word i (rank 0), w = word i + N/2 (rank 1)
+  pair_inverse<PC>(x, smem32, tid, r, bb, m);
   cluster.sync();
-  const uint32_t* peer = cluster.map_shared_rank(smem32, (int)(r ^ 1u));
-  uint32_t* dst = c + lbase + r * half;
-#pragma unroll
-  for (int i = 0; i < IT; ++i) {
-    const uint32_t v = (tid + i * C::THREADS) * 4;
-    const uint4 own = *reinterpret_cast<const uint4*>(smem32 + Smem<uint32_t>::idx(v));
-    const uint4 oth = *reinterpret_cast<const uint4*>(peer + Smem<uint32_t>::idx(v));
-    const uint32_t o[4] = {own.x, own.y, own.z, own.w}, q[4] = {oth.x, oth.y, oth.z, oth.w};
-    uint32_t res[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const uint32_t u = r == 0 ? o[k] : q[k], w = r == 0 ? q[k] : o[k];
-      res[k] = r == 0 ? mulmod_shoup(u + w, m.inv_n, m.inv_n_s, p)
-                      : mulmod_shoup(u - w + p2, m.inv_n_iphi, m.inv_n_iphi_s, p);
-    }
-    *reinterpret_cast<uint4*>(dst + v) = make_uint4(res[0], res[1], res[2], res[3]);
-  }
+  pair_last_layer<PC, true>(c + lbase + r * half, smem32, cluster.map_shared_rank(smem32, (int)(r ^ 1u)), tid, r, m);
   cluster.sync();  // the peer may still be reading this CTA's shared memory
 }
 
 // In-place NTT of one limb by a CTA pair (DIR: 0 forward, 1 forward lazy,
 // 2 backward), same split as k32_polymul_pair.
-template <class C, int DIR>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, C::THREADS <= 256 ? 3 : 2)
+template <class PC, int DIR>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PC::C::THREADS, PC::MIN_BLOCKS)
     k32_ntt_pair(uint32_t* data, Limbs32 ls, const DevMod32* __restrict__ mods) {
   namespace cg = cooperative_groups;
+  using C = typename PC::C;
+  using S = typename PC::S;
   extern __shared__ __align__(16) uint32_t smem32[];
   constexpr int H = C::K, NR = C::NR, E = 1 << C::LOGE;
   constexpr uint32_t log_n = H + 1, half = 1u << H;
@@ -505,7 +540,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, C::THREA
   uint32_t* base = data + ((size_t)limb << log_n);
   if constexpr (DIR != 2) {
     uint32_t x[E];
-    pair_forward<C, true>(x, base, smem32, tid, r, m, __ldg(m.fwd + 1));
+    pair_forward<PC, true>(x, base, smem32, tid, r, m, __ldg(m.fwd + 1));
     uint32_t* out = base + r * half + RB::base(tid);
 #pragma unroll
     for (int i = 0; i < E; i += 4) {
@@ -523,31 +558,15 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(C::THREADS, C::THREA
     }
     __syncthreads();
     {
-      using S = HalfSplit<H>;
+      using CA = typename S::CA;
       using CB = typename S::CB;
       const uint32_t G = S::row_group(r, tid);
       inv_rounds<CB, CB::NR - 1, 0, false, CB::LOCAL_BARRIER>(smem32, tid, log_n, 0, G, m, true);
       inv_rounds<CB, 0, -1, false>(smem32, tid, log_n, 0, G, m, true);  // CTA barrier after
-      inv_rounds<typename S::CA, 0, -1, false>(smem32, tid, log_n, S::KB, r, m, true);
+      inv_rounds<CA, CA::NR - 1, -1, false>(smem32, tid, log_n, S::KB, r, m, true);
     }
     cluster.sync();
-    const uint32_t* peer = cluster.map_shared_rank(smem32, (int)(r ^ 1u));
-    uint32_t* dst = base + r * half;
-#pragma unroll 1
-    for (int i = 0; i < IT; ++i) {
-      const uint32_t v = (tid + i * C::THREADS) * 4;
-      const uint4 a4 = *reinterpret_cast<const uint4*>(smem32 + Smem<uint32_t>::idx(v));
-      const uint4 b4 = *reinterpret_cast<const uint4*>(peer + Smem<uint32_t>::idx(v));
-      const uint32_t o[4] = {a4.x, a4.y, a4.z, a4.w}, q[4] = {b4.x, b4.y, b4.z, b4.w};
-      uint32_t res[4];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const uint32_t u = r == 0 ? o[k] : q[k], w = r == 0 ? q[k] : o[k];
-        res[k] = r == 0 ? mulmod_shoup(u + w, m.inv_n, m.inv_n_s, p)
-                        : mulmod_shoup(u - w + p2, m.inv_n_iphi, m.inv_n_iphi_s, p);
-      }
-      *reinterpret_cast<uint4*>(dst + v) = make_uint4(res[0], res[1], res[2], res[3]);
-    }
+    pair_last_layer<PC, false>(base + r * half, smem32, cluster.map_shared_rank(smem32, (int)(r ^ 1u)), tid, r, m);
     cluster.sync();
   }
 }
@@ -583,10 +602,10 @@ cudaError_t set_attrs32() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k32_polymul<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if constexpr (LOGN >= kMinPairLogN) {
     using PC = PairCfg32<LOGN>;
-    for (auto k : {k32_ntt_pair<typename PC::C, 0>, k32_ntt_pair<typename PC::C, 1>, k32_ntt_pair<typename PC::C, 2>})
+    for (auto k : {k32_ntt_pair<PC, 0>, k32_ntt_pair<PC, 1>, k32_ntt_pair<PC, 2>})
       if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PC::kSmem);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k32_polymul_pair<typename PC::C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      e = cudaFuncSetAttribute(k32_polymul_pair<PC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)PC::kSmem);
   }
   return e;
@@ -602,10 +621,10 @@ cudaError_t launch32(int kind, uint32_t* c, const uint32_t* a, const uint32_t* b
     using PC = PairCfg32<LOGN>;
     using P = typename PC::C;
     const uint32_t g = 2 * ls.count;
-    if (kind == 0) k32_ntt_pair<P, 0><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
-    else if (kind == 1) k32_ntt_pair<P, 1><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
-    else if (kind == 2) k32_ntt_pair<P, 2><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
-    else k32_polymul_pair<P><<<g, P::THREADS, PC::kSmem, st>>>(c, a, b, ls, mods);
+    if (kind == 0) k32_ntt_pair<PC, 0><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
+    else if (kind == 1) k32_ntt_pair<PC, 1><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
+    else if (kind == 2) k32_ntt_pair<PC, 2><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
+    else k32_polymul_pair<PC><<<g, P::THREADS, PC::kSmem, st>>>(c, a, b, ls, mods);
     return cudaGetLastError();
   }
   if (kind == 0) k32_ntt<C, 0><<<blocks, C::THREADS, CF::kSmem, st>>>(c, ls, mods);
