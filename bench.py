@@ -470,6 +470,20 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
            "path": "yell_polymul_host from pinned host buffers"}
     for buf in (pa, pb, pc):
         buf.free()
+    # the same call on plain (pageable) numpy arrays: moved by kernels that
+    # access the host memory in place where the device supports it
+    out = np.empty_like(a)
+    y.polymul_host(a, b, LOG_N, out=out)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        y.polymul_host(a, b, LOG_N, out=out)
+    torch.cuda.synchronize()
+    pg_s = max_over_ranks(time.perf_counter() - t0)
+    e2e["pageable"] = {"value": world * per_step * 3 / pg_s, "unit": UNIT, "ms_per_step": 1e3 * pg_s / 3,
+                       "host_access": y.host_access(),
+                       "path": "yell_polymul_host from pageable numpy arrays"}
+    del out
     if not args.no_facade:
         e2e["facade"] = run_e2e_facade(y, a, b, dc.cpu().numpy().view(np.uint64).reshape(a.shape))
         barrier()

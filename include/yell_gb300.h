@@ -152,6 +152,16 @@ int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_
 void* yell_host_alloc(size_t bytes); /* pinned; NULL on failure */
 void yell_host_free(void* p);
 
+/* Host-pointer calls above 2^15 words (yell_ntt_*, yell_poly_*) on a device
+ * that reaches pageable host memory through the host's page tables (GB300
+ * with Grace over NVLink-C2C) move the caller's limbs with kernels that load
+ * and store them where they lie, instead of pageable copies through the
+ * driver; limbs not 16-byte aligned take the copies.  On by default where
+ * supported; yell_set_host_access(0) forces the copies (results are the
+ * same).  yell_host_access reports whether the current device uses it. */
+int yell_set_host_access(int enable);
+int yell_host_access(int* in_use);
+
 /* ---- device-resident calls (device pointers, asynchronous on `stream`) --
  * A batch is `count` polys of L limbs laid out (count, L, N) contiguous;
  * limb l of every poly uses prime cm0 + l. */

@@ -22,7 +22,8 @@ __all__ = [
     "YellError", "load", "prime", "primes", "max_moduli", "min_log_degree", "max_log_degree",
     "init_ntt_tables", "ntt_tables", "ntt_forward", "ntt_forward_lazy", "ntt_backward",
     "poly_forward", "poly_forward_lazy", "poly_backward", "poly_mulmod", "poly_addmod",
-    "poly_submod", "poly_add_product_of", "poly_negate", "polymul_host", "dev_ntt",
+    "poly_submod", "poly_add_product_of", "poly_negate", "polymul_host", "set_host_access", "host_access",
+    "dev_ntt",
     "dev_ntt_limbs", "dev_elementwise", "dev_polymul", "polymul_scratch_words", "kernel_launches", "allocations",
     "Poly", "PinnedBuffer", "sample_uniform", "sample_zo", "sample_hwt", "sample_gaussian",
     "crt_words", "dev_crt_lift", "poly_to_bigint", "words_to_ints", "DevPoly", "BatchTicket",
@@ -192,6 +193,19 @@ class PinnedBuffer:
             self.free()
         except Exception:
             pass
+
+
+def set_host_access(enable: bool) -> None:
+    """Host-pointer calls move limbs by kernels that access host memory in place
+    (where the device supports it) or, when disabled, by copies."""
+    call("yell_set_host_access", 1 if enable else 0)
+
+
+def host_access() -> bool:
+    """Whether host-pointer calls on the current device use direct host access."""
+    v = ctypes.c_int()
+    call("yell_host_access", ctypes.byref(v))
+    return bool(v.value)
 
 
 def polymul_host(a, b, log_n: int, cm0: int = 0, out=None) -> np.ndarray:

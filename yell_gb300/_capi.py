@@ -77,6 +77,8 @@ SIGNATURES = {
     "yell_polymul_host": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32]),
     "yell_host_alloc": (_vp, [_sz]),
     "yell_host_free": (None, [_vp]),
+    "yell_set_host_access": (_int, [_int]),
+    "yell_host_access": (_int, [_vp]),
     "yell_dev_ntt": (_int, [_vp, _u32, _u32, _u32, _u32, _int, _vp]),
     "yell_dev_ntt_limbs": (_int, [_vp, _vp, _u32, _u32, _int, _vp]),
     "yell_dev_elementwise": (_int, [_int, _vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),

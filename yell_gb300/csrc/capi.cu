@@ -70,6 +70,19 @@ int check_aligned(const void* p, const char* what) {
   return kOk;
 }
 
+// A contiguous host operand that kernels should access in place: the device
+// reaches pageable memory through the host's page tables, the memory is
+// pageable (pinned memory copies as fast by DMA), and 16-byte aligned.
+bool direct_host(DeviceContext* ctx, const void* p) {
+  if (!ctx->host_access() || reinterpret_cast<uintptr_t>(p) % 16 != 0) return false;
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();  // clear the error the failed query recorded
+    return false;
+  }
+  return attr.type == cudaMemoryTypeUnregistered;
+}
+
 // Host-memory drop-in: copy L limbs (separate host arrays) into the context's
 // staging area, run `body`, copy `nout` result limb sets back, synchronise.
 // Holds the staging lock for the whole call.
@@ -98,11 +111,22 @@ int host_ntt(uint64_t* const* limbs, uint32_t L, uint32_t log_n, uint32_t cm0, N
   std::lock_guard<std::mutex> g(ctx->staging.lock);
   YELL_TRY(ctx->staging.reserve(n * L));
   uint64_t* d = ctx->staging.ptr;
-  for (uint32_t i = 0; i < L; ++i)
-    YELL_CUDA(cudaMemcpyAsync(d + i * n, limbs[i], n * 8, cudaMemcpyHostToDevice, st), "H2D limb");
+  // the limbs move by kernels that read and write the host memory where it
+  // lies when the device can, else by copies through the driver
+  const bool direct = ctx->host_access() && host_limbs_accessible(limbs, L);
+  if (direct) {
+    YELL_CUDA(gather_host_limbs(d, limbs, L, log_n, st), "gather host limbs");
+  } else {
+    for (uint32_t i = 0; i < L; ++i)
+      YELL_CUDA(cudaMemcpyAsync(d + i * n, limbs[i], n * 8, cudaMemcpyHostToDevice, st), "H2D limb");
+  }
   YELL_CUDA(launch_ntt(contiguous(d, L, L, cm0), log_n, mods, dir, ctx->shape, st), "launch ntt");
-  for (uint32_t i = 0; i < L; ++i)
-    YELL_CUDA(cudaMemcpyAsync(limbs[i], d + i * n, n * 8, cudaMemcpyDeviceToHost, st), "D2H limb");
+  if (direct) {
+    YELL_CUDA(scatter_host_limbs(limbs, d, L, log_n, st), "scatter host limbs");
+  } else {
+    for (uint32_t i = 0; i < L; ++i)
+      YELL_CUDA(cudaMemcpyAsync(limbs[i], d + i * n, n * 8, cudaMemcpyDeviceToHost, st), "D2H limb");
+  }
   YELL_CUDA(cudaStreamSynchronize(st), "synchronize");
   return kOk;
 }
@@ -147,18 +171,30 @@ int host_elementwise(EwOp op, uint64_t* const* dst, const uint64_t* const* a,
   uint64_t* da = ctx->staging.ptr;
   uint64_t* db = da + w;
   uint64_t* dd = db + w;
-  for (uint32_t i = 0; i < L; ++i) {
-    YELL_CUDA(cudaMemcpyAsync(da + i * n, a[i], n * 8, cudaMemcpyHostToDevice, st), "H2D a");
-    if (op != EwOp::kNegate)
-      YELL_CUDA(cudaMemcpyAsync(db + i * n, b[i], n * 8, cudaMemcpyHostToDevice, st), "H2D b");
-    if (op == EwOp::kMuladd)
-      YELL_CUDA(cudaMemcpyAsync(dd + i * n, dst[i], n * 8, cudaMemcpyHostToDevice, st), "H2D acc");
+  const bool direct = ctx->host_access() && host_limbs_accessible(dst, L) && host_limbs_accessible(a, L) &&
+                      (op == EwOp::kNegate || host_limbs_accessible(b, L));
+  if (direct) {
+    YELL_CUDA(gather_host_limbs(da, a, L, log_n, st), "gather a");
+    if (op != EwOp::kNegate) YELL_CUDA(gather_host_limbs(db, b, L, log_n, st), "gather b");
+    if (op == EwOp::kMuladd) YELL_CUDA(gather_host_limbs(dd, dst, L, log_n, st), "gather acc");
+  } else {
+    for (uint32_t i = 0; i < L; ++i) {
+      YELL_CUDA(cudaMemcpyAsync(da + i * n, a[i], n * 8, cudaMemcpyHostToDevice, st), "H2D a");
+      if (op != EwOp::kNegate)
+        YELL_CUDA(cudaMemcpyAsync(db + i * n, b[i], n * 8, cudaMemcpyHostToDevice, st), "H2D b");
+      if (op == EwOp::kMuladd)
+        YELL_CUDA(cudaMemcpyAsync(dd + i * n, dst[i], n * 8, cudaMemcpyHostToDevice, st), "H2D acc");
+    }
   }
   YELL_CUDA(launch_elementwise(op, contiguous(dd, L, L, 0), const_contiguous(da, L, L, 0),
                                const_contiguous(db, L, L, 0), log_n, mods, st),
             "launch elementwise");
-  for (uint32_t i = 0; i < L; ++i)
-    YELL_CUDA(cudaMemcpyAsync(dst[i], dd + i * n, n * 8, cudaMemcpyDeviceToHost, st), "D2H");
+  if (direct) {
+    YELL_CUDA(scatter_host_limbs(dst, dd, L, log_n, st), "scatter result");
+  } else {
+    for (uint32_t i = 0; i < L; ++i)
+      YELL_CUDA(cudaMemcpyAsync(dst[i], dd + i * n, n * 8, cudaMemcpyDeviceToHost, st), "D2H");
+  }
   YELL_CUDA(cudaStreamSynchronize(st), "synchronize");
   return kOk;
 }
@@ -259,6 +295,19 @@ int yell_poly_negate(uint64_t* const* limbs, uint32_t L, uint32_t log_n) {
   return host_elementwise(EwOp::kNegate, limbs, limbs, nullptr, L, log_n);
 }
 
+int yell_set_host_access(int enable) {
+  g_host_access.store(enable != 0);
+  return kOk;
+}
+
+int yell_host_access(int* in_use) {
+  if (!in_use) return fail(kInvalidArgument, "null output");
+  DeviceContext* ctx;
+  YELL_TRY(get_ctx(&ctx));
+  *in_use = ctx->host_access() ? 1 : 0;
+  return kOk;
+}
+
 void* yell_host_alloc(size_t bytes) {
   void* p = nullptr;
   if (lib_malloc_host(&p, bytes) != cudaSuccess) return nullptr;
@@ -316,6 +365,32 @@ int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_
     YELL_TRY(ctx->pipe_buf[s].reserve(3 * cw + sw));
   }
   cudaStream_t h2d = ctx->pipe_stream[0], comp = ctx->pipe_stream[1], d2h = ctx->pipe_stream[2];
+  // Pageable operands move by kernels that access them in place where the
+  // device can (copies from pageable memory run through driver staging at a
+  // sixth of the link's rate); pinned ones by the copy engines.
+  const bool dir_a = direct_host(ctx, a), dir_b = direct_host(ctx, b), dir_c = direct_host(ctx, c);
+  const size_t n = (size_t)1 << log_n;
+  std::vector<const uint64_t*> limb_ptrs;
+  auto copy_in = [&](uint64_t* dst, const uint64_t* src, size_t words, bool direct, const char* what) -> int {
+    if (!direct) {
+      YELL_CUDA(cudaMemcpyAsync(dst, src, words * 8, cudaMemcpyHostToDevice, h2d), what);
+      return kOk;
+    }
+    limb_ptrs.resize(words / n);
+    for (size_t i = 0; i < limb_ptrs.size(); ++i) limb_ptrs[i] = src + i * n;
+    YELL_CUDA(gather_host_limbs(dst, limb_ptrs.data(), (uint32_t)limb_ptrs.size(), log_n, h2d), what);
+    return kOk;
+  };
+  auto copy_out = [&](uint64_t* dst, const uint64_t* src, size_t words) -> int {
+    if (!dir_c) {
+      YELL_CUDA(cudaMemcpyAsync(dst, src, words * 8, cudaMemcpyDeviceToHost, d2h), "D2H c");
+      return kOk;
+    }
+    std::vector<uint64_t*> outs(words / n);
+    for (size_t i = 0; i < outs.size(); ++i) outs[i] = dst + i * n;
+    YELL_CUDA(scatter_host_limbs(outs.data(), src, (uint32_t)outs.size(), log_n, d2h), "scatter c");
+    return kOk;
+  };
   uint32_t k = 0;
   for (uint32_t p0 = 0, np = 0; p0 < pairs; p0 += np, ++k) {
     const int s = (int)(k % DeviceContext::kPipeSlots);
@@ -329,8 +404,8 @@ int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_
     uint64_t* dc = db + cw;
     uint64_t* ds = dc + cw;
     if (reuse) YELL_CUDA(cudaStreamWaitEvent(h2d, ctx->pipe_comp[s], 0), "pipe order");
-    YELL_CUDA(cudaMemcpyAsync(da, a + p0 * pair_words, w * 8, cudaMemcpyHostToDevice, h2d), "H2D a");
-    YELL_CUDA(cudaMemcpyAsync(db, b + p0 * pair_words, w * 8, cudaMemcpyHostToDevice, h2d), "H2D b");
+    YELL_TRY(copy_in(da, a + p0 * pair_words, w, dir_a, "H2D a"));
+    YELL_TRY(copy_in(db, b + p0 * pair_words, w, dir_b, "H2D b"));
     YELL_CUDA(cudaEventRecord(ctx->pipe_h2d[s], h2d), "pipe event");
     YELL_CUDA(cudaStreamWaitEvent(comp, ctx->pipe_h2d[s], 0), "pipe order");
     if (reuse) YELL_CUDA(cudaStreamWaitEvent(comp, ctx->pipe_d2h[s], 0), "pipe order");
@@ -340,7 +415,7 @@ int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_
               "launch polymul");
     YELL_CUDA(cudaEventRecord(ctx->pipe_comp[s], comp), "pipe event");
     YELL_CUDA(cudaStreamWaitEvent(d2h, ctx->pipe_comp[s], 0), "pipe order");
-    YELL_CUDA(cudaMemcpyAsync(c + p0 * pair_words, dc, w * 8, cudaMemcpyDeviceToHost, d2h), "D2H c");
+    YELL_TRY(copy_out(c + p0 * pair_words, dc, w));
     YELL_CUDA(cudaEventRecord(ctx->pipe_d2h[s], d2h), "pipe event");
   }
   for (int i = 0; i < 3; ++i) YELL_CUDA(cudaStreamSynchronize(ctx->pipe_stream[i]), "synchronize");

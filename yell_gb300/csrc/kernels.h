@@ -87,6 +87,17 @@ bool polymul_scratch_optional(uint32_t log_n);
 // device (called once per device, outside any stream capture).
 cudaError_t init_kernel_attributes();
 
+// Copies between the caller's host limbs (L separate arrays of N words) and
+// L contiguous device limbs, by kernels that load and store the host memory
+// directly (host_access.cu).  Only for a device that reaches pageable host
+// memory through the host's page tables (DeviceContext::host_access); every
+// limb must be 16-byte aligned (host_limbs_accessible).
+bool host_limbs_accessible(const uint64_t* const* limbs, uint32_t L);
+cudaError_t gather_host_limbs(uint64_t* dev, const uint64_t* const* limbs, uint32_t L, uint32_t log_n,
+                              cudaStream_t st);
+cudaError_t scatter_host_limbs(uint64_t* const* limbs, const uint64_t* dev, uint32_t L, uint32_t log_n,
+                               cudaStream_t st);
+
 // Kernels launched by one call of launch_ntt / launch_polymul / elementwise.
 uint32_t ntt_launch_count(uint32_t log_n, const NttShape& shape);
 uint32_t polymul_launch_count(uint32_t log_n, const NttShape& shape);

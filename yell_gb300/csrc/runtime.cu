@@ -216,8 +216,17 @@ int DeviceContext::init() {
   e = init_kernel_attributes();
   if (e != cudaSuccess) return fail_cuda(e, "cudaFuncSetAttribute");
   load_tuning(device_);
+  int pageable = 0, host_tables = 0;
+  if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device_) == cudaSuccess &&
+      cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device_) ==
+          cudaSuccess)
+    pageable_access_ = pageable == 1 && host_tables == 1;
   return kOk;
 }
+
+std::atomic<bool> g_host_access{true};
+
+bool DeviceContext::host_access() const { return pageable_access_ && g_host_access.load(std::memory_order_relaxed); }
 
 DeviceContext* DeviceContext::current(int* status) {
   static std::mutex mu;

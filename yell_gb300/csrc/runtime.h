@@ -66,6 +66,10 @@ uint64_t* noalloc_scratch(int device);
 void build_host_tables(uint32_t log_n, uint32_t cm, uint64_t* out4n, uint64_t* sc4);
 
 // One per CUDA device, created on first use with that device current.
+// Direct host-memory access by kernels, on devices that support it (on by
+// default; yell_set_host_access).
+extern std::atomic<bool> g_host_access;
+
 class DeviceContext {
  public:
   // Context of the current device; nullptr and a recorded error on failure.
@@ -131,11 +135,19 @@ class DeviceContext {
 
   NttShape shape;  // launch shape (autotuner may adjust)
 
+  // The device loads and stores pageable host memory through the host's page
+  // tables (cudaDevAttrPageableMemoryAccess and
+  // cudaDevAttrPageableMemoryAccessUsesHostPageTables), and direct host access
+  // is enabled (yell_set_host_access): host-pointer calls then move the
+  // caller's limbs with gather / scatter kernels instead of pageable copies.
+  bool host_access() const;
+
  private:
   explicit DeviceContext(int device);
   int init();
 
   int device_;
+  bool pageable_access_ = false;
   cudaStream_t stream_ = nullptr;
   cudaMemPool_t pool_ = nullptr;
   mutable std::mutex tables_mu_;
