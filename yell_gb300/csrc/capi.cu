@@ -71,17 +71,9 @@ int check_aligned(const void* p, const char* what) {
 }
 
 // A contiguous host operand that kernels should access in place: the device
-// reaches pageable memory through the host's page tables, the memory is
-// pageable (pinned memory copies as fast by DMA), and 16-byte aligned.
-bool direct_host(DeviceContext* ctx, const void* p) {
-  if (!ctx->host_access() || reinterpret_cast<uintptr_t>(p) % 16 != 0) return false;
-  cudaPointerAttributes attr;
-  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
-    cudaGetLastError();  // clear the error the failed query recorded
-    return false;
-  }
-  return attr.type == cudaMemoryTypeUnregistered;
-}
+// reaches pageable memory through the host's page tables and the operand is
+// pageable (pinned memory copies as fast by DMA) and 16-byte aligned.
+bool direct_host(DeviceContext* ctx, const void* p) { return ctx->host_access() && pageable_host(p); }
 
 // Host-memory drop-in: copy L limbs (separate host arrays) into the context's
 // staging area, run `body`, copy `nout` result limb sets back, synchronise.
@@ -369,27 +361,13 @@ int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_
   // device can (copies from pageable memory run through driver staging at a
   // sixth of the link's rate); pinned ones by the copy engines.
   const bool dir_a = direct_host(ctx, a), dir_b = direct_host(ctx, b), dir_c = direct_host(ctx, c);
-  const size_t n = (size_t)1 << log_n;
-  std::vector<const uint64_t*> limb_ptrs;
-  auto copy_in = [&](uint64_t* dst, const uint64_t* src, size_t words, bool direct, const char* what) -> int {
-    if (!direct) {
-      YELL_CUDA(cudaMemcpyAsync(dst, src, words * 8, cudaMemcpyHostToDevice, h2d), what);
-      return kOk;
-    }
-    limb_ptrs.resize(words / n);
-    for (size_t i = 0; i < limb_ptrs.size(); ++i) limb_ptrs[i] = src + i * n;
-    YELL_CUDA(gather_host_limbs(dst, limb_ptrs.data(), (uint32_t)limb_ptrs.size(), log_n, h2d), what);
-    return kOk;
+  auto copy_in = [&](uint64_t* dst, const uint64_t* src, size_t words, bool direct) {
+    return direct ? gather_host_contiguous(dst, src, (uint32_t)(words >> log_n), log_n, h2d)
+                  : cudaMemcpyAsync(dst, src, words * 8, cudaMemcpyHostToDevice, h2d);
   };
-  auto copy_out = [&](uint64_t* dst, const uint64_t* src, size_t words) -> int {
-    if (!dir_c) {
-      YELL_CUDA(cudaMemcpyAsync(dst, src, words * 8, cudaMemcpyDeviceToHost, d2h), "D2H c");
-      return kOk;
-    }
-    std::vector<uint64_t*> outs(words / n);
-    for (size_t i = 0; i < outs.size(); ++i) outs[i] = dst + i * n;
-    YELL_CUDA(scatter_host_limbs(outs.data(), src, (uint32_t)outs.size(), log_n, d2h), "scatter c");
-    return kOk;
+  auto copy_out = [&](uint64_t* dst, const uint64_t* src, size_t words) {
+    return dir_c ? scatter_host_contiguous(dst, src, (uint32_t)(words >> log_n), log_n, d2h)
+                 : cudaMemcpyAsync(dst, src, words * 8, cudaMemcpyDeviceToHost, d2h);
   };
   uint32_t k = 0;
   for (uint32_t p0 = 0, np = 0; p0 < pairs; p0 += np, ++k) {
@@ -404,8 +382,8 @@ int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_
     uint64_t* dc = db + cw;
     uint64_t* ds = dc + cw;
     if (reuse) YELL_CUDA(cudaStreamWaitEvent(h2d, ctx->pipe_comp[s], 0), "pipe order");
-    YELL_TRY(copy_in(da, a + p0 * pair_words, w, dir_a, "H2D a"));
-    YELL_TRY(copy_in(db, b + p0 * pair_words, w, dir_b, "H2D b"));
+    YELL_CUDA(copy_in(da, a + p0 * pair_words, w, dir_a), "H2D a");
+    YELL_CUDA(copy_in(db, b + p0 * pair_words, w, dir_b), "H2D b");
     YELL_CUDA(cudaEventRecord(ctx->pipe_h2d[s], h2d), "pipe event");
     YELL_CUDA(cudaStreamWaitEvent(comp, ctx->pipe_h2d[s], 0), "pipe order");
     if (reuse) YELL_CUDA(cudaStreamWaitEvent(comp, ctx->pipe_d2h[s], 0), "pipe order");
@@ -415,7 +393,7 @@ int yell_polymul_host(uint64_t* c, const uint64_t* a, const uint64_t* b, uint32_
               "launch polymul");
     YELL_CUDA(cudaEventRecord(ctx->pipe_comp[s], comp), "pipe event");
     YELL_CUDA(cudaStreamWaitEvent(d2h, ctx->pipe_comp[s], 0), "pipe order");
-    YELL_TRY(copy_out(c + p0 * pair_words, dc, w));
+    YELL_CUDA(copy_out(c + p0 * pair_words, dc, w), "D2H c");
     YELL_CUDA(cudaEventRecord(ctx->pipe_d2h[s], d2h), "pipe event");
   }
   for (int i = 0; i < 3; ++i) YELL_CUDA(cudaStreamSynchronize(ctx->pipe_stream[i]), "synchronize");

@@ -106,10 +106,17 @@ int yell_dev_poly_upload(yell_dev_poly* p, const uint64_t* const* limbs) {
   if (st != kOk) return st;
   const size_t n = limb_words(p);
   cudaStream_t s = ctx->stream();
-  for (uint32_t l = 0; l < p->L; ++l) {
+  for (uint32_t l = 0; l < p->L; ++l)
     if (!limbs[l]) return fail(kInvalidArgument, "null limb pointer");
-    const cudaError_t e = cudaMemcpyAsync(p->data + l * n, limbs[l], n * 8, cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return fail_cuda(e, "upload limb");
+  if (ctx->host_access() && host_limbs_accessible(limbs, p->L)) {
+    // one kernel reads every limb where it lies (no pageable copies)
+    const cudaError_t e = gather_host_limbs(p->data, limbs, p->L, p->log_n, s);
+    if (e != cudaSuccess) return fail_cuda(e, "upload");
+  } else {
+    for (uint32_t l = 0; l < p->L; ++l) {
+      const cudaError_t e = cudaMemcpyAsync(p->data + l * n, limbs[l], n * 8, cudaMemcpyHostToDevice, s);
+      if (e != cudaSuccess) return fail_cuda(e, "upload limb");
+    }
   }
   const cudaError_t e = cudaStreamSynchronize(s);
   return e == cudaSuccess ? kOk : fail_cuda(e, "upload");
@@ -122,10 +129,16 @@ int yell_dev_poly_download(const yell_dev_poly* p, uint64_t* const* limbs) {
   if (st != kOk) return st;
   const size_t n = limb_words(p);
   cudaStream_t s = ctx->stream();
-  for (uint32_t l = 0; l < p->L; ++l) {
+  for (uint32_t l = 0; l < p->L; ++l)
     if (!limbs[l]) return fail(kInvalidArgument, "null limb pointer");
-    const cudaError_t e = cudaMemcpyAsync(limbs[l], p->data + l * n, n * 8, cudaMemcpyDeviceToHost, s);
-    if (e != cudaSuccess) return fail_cuda(e, "download limb");
+  if (ctx->host_access() && host_limbs_accessible(limbs, p->L)) {
+    const cudaError_t e = scatter_host_limbs(limbs, p->data, p->L, p->log_n, s);
+    if (e != cudaSuccess) return fail_cuda(e, "download");
+  } else {
+    for (uint32_t l = 0; l < p->L; ++l) {
+      const cudaError_t e = cudaMemcpyAsync(limbs[l], p->data + l * n, n * 8, cudaMemcpyDeviceToHost, s);
+      if (e != cudaSuccess) return fail_cuda(e, "download limb");
+    }
   }
   const cudaError_t e = cudaStreamSynchronize(s);
   return e == cudaSuccess ? kOk : fail_cuda(e, "download");

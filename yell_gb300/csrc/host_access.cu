@@ -15,6 +15,7 @@
 // host.  Each thread moves 16-byte pairs, kUnroll of them in flight, with
 // consecutive threads on consecutive pairs.
 #include <algorithm>
+#include <vector>
 
 #include "kernels.h"
 #include "profiler.h"
@@ -93,6 +94,30 @@ cudaError_t scatter_host_limbs(uint64_t* const* limbs, const uint64_t* dev, uint
                                cudaStream_t st) {
   LaunchScope ps("host_scatter", st);
   return host_limbs<false>(const_cast<const uint64_t* const*>(limbs), const_cast<uint64_t*>(dev), L, log_n, st);
+}
+
+bool pageable_host(const void* p) {
+  if (!p || reinterpret_cast<uintptr_t>(p) % 16 != 0) return false;
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();  // clear the error the failed query recorded
+    return false;
+  }
+  return attr.type == cudaMemoryTypeUnregistered;
+}
+
+cudaError_t gather_host_contiguous(uint64_t* dev, const uint64_t* host, uint32_t limbs, uint32_t log_n,
+                                   cudaStream_t st) {
+  std::vector<const uint64_t*> ptrs(limbs);
+  for (uint32_t i = 0; i < limbs; ++i) ptrs[i] = host + ((size_t)i << log_n);
+  return gather_host_limbs(dev, ptrs.data(), limbs, log_n, st);
+}
+
+cudaError_t scatter_host_contiguous(uint64_t* host, const uint64_t* dev, uint32_t limbs, uint32_t log_n,
+                                    cudaStream_t st) {
+  std::vector<uint64_t*> ptrs(limbs);
+  for (uint32_t i = 0; i < limbs; ++i) ptrs[i] = host + ((size_t)i << log_n);
+  return scatter_host_limbs(ptrs.data(), dev, limbs, log_n, st);
 }
 
 }  // namespace yell_gb300

@@ -97,6 +97,14 @@ cudaError_t gather_host_limbs(uint64_t* dev, const uint64_t* const* limbs, uint3
                               cudaStream_t st);
 cudaError_t scatter_host_limbs(uint64_t* const* limbs, const uint64_t* dev, uint32_t L, uint32_t log_n,
                                cudaStream_t st);
+// The same for `limbs` limbs laid out contiguously at `host`, for pageable
+// memory (pageable_host: 16-byte aligned, not pinned or registered; pinned
+// memory copies as fast through the copy engines, and asynchronously).
+bool pageable_host(const void* p);
+cudaError_t gather_host_contiguous(uint64_t* dev, const uint64_t* host, uint32_t limbs, uint32_t log_n,
+                                   cudaStream_t st);
+cudaError_t scatter_host_contiguous(uint64_t* host, const uint64_t* dev, uint32_t limbs, uint32_t log_n,
+                                    cudaStream_t st);
 
 // Kernels launched by one call of launch_ntt / launch_polymul / elementwise.
 uint32_t ntt_launch_count(uint32_t log_n, const NttShape& shape);

@@ -253,6 +253,21 @@ bool yell_server::admit(std::vector<ReqPtr>* batch) {
   return !batch->empty();
 }
 
+// Host operands: pageable ones move by kernels that access them in place
+// where the device can (a copy from or to pageable memory would hold the
+// scheduler thread until it completes); pinned ones by the copy engines.
+static cudaError_t host_in(DeviceContext* ctx, uint64_t* dev, const uint64_t* host, uint32_t limbs, uint32_t log_n,
+                           cudaStream_t st) {
+  if (ctx->host_access() && pageable_host(host)) return gather_host_contiguous(dev, host, limbs, log_n, st);
+  return cudaMemcpyAsync(dev, host, ((size_t)limbs << log_n) * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
+}
+
+static cudaError_t host_out(DeviceContext* ctx, uint64_t* host, const uint64_t* dev, uint32_t limbs, uint32_t log_n,
+                            cudaStream_t st) {
+  if (ctx->host_access() && pageable_host(host)) return scatter_host_contiguous(host, dev, limbs, log_n, st);
+  return cudaMemcpyAsync(host, dev, ((size_t)limbs << log_n) * sizeof(uint64_t), cudaMemcpyDeviceToHost, st);
+}
+
 int yell_server::launch(Slot& s, std::vector<ReqPtr>& batch) {
   TraceRange trace("yell serve step");
   const size_t n = batch.size();
@@ -266,14 +281,14 @@ int yell_server::launch(Slot& s, std::vector<ReqPtr>& batch) {
     const size_t bytes = r.words * sizeof(uint64_t);
     if (is_ntt(r.req)) {  // input into the output buffer, transformed there in place
       if (!(r.req.flags & YELL_REQ_DEVICE))
-        e = cudaMemcpyAsync(r.d_c, r.req.a, bytes, cudaMemcpyHostToDevice, s.stream);
+        e = host_in(ctx, r.d_c, r.req.a, r.req.L, r.req.log_n, s.stream);
       else if (r.d_c != r.d_a)
         e = cudaMemcpyAsync(r.d_c, r.d_a, bytes, cudaMemcpyDeviceToDevice, s.stream);
       continue;
     }
     if (!(r.req.flags & YELL_REQ_DEVICE)) {
-      e = cudaMemcpyAsync(r.d_a, r.req.a, bytes, cudaMemcpyHostToDevice, s.stream);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(r.d_b, r.req.b, bytes, cudaMemcpyHostToDevice, s.stream);
+      e = host_in(ctx, r.d_a, r.req.a, r.req.L, r.req.log_n, s.stream);
+      if (e == cudaSuccess) e = host_in(ctx, r.d_b, r.req.b, r.req.L, r.req.log_n, s.stream);
     }
     descs.push_back(yell_polymul_desc{r.d_c, r.d_a, r.d_b, r.req.log_n, r.req.L, r.req.cm0, 0});
     scratch.push_back(r.d_s);
@@ -302,8 +317,7 @@ int yell_server::launch(Slot& s, std::vector<ReqPtr>& batch) {
   }
   for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
     Request& r = *batch[i];
-    if (!(r.req.flags & YELL_REQ_DEVICE))
-      e = cudaMemcpyAsync(r.req.c, r.d_c, r.words * sizeof(uint64_t), cudaMemcpyDeviceToHost, s.stream);
+    if (!(r.req.flags & YELL_REQ_DEVICE)) e = host_out(ctx, r.req.c, r.d_c, r.req.L, r.req.log_n, s.stream);
   }
   if (e == cudaSuccess) e = cudaEventRecord(s.done, s.stream);
   if (e != cudaSuccess) return fail_cuda(e, "server launch");
