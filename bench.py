@@ -691,6 +691,7 @@ def run_uneven(torch, y, stream, barrier, max_over_ranks, world, no_autotune=Fal
         if not no_autotune:
             y.autotune(log_n, 8, 4)
     limb_ntts = mix_limb_ntts(mix)
+    tuned = {f"2^{d}": y.variants(d)[y.get_variant(d)] for d in range(10, 17)}
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
 
@@ -708,7 +709,8 @@ def run_uneven(torch, y, stream, barrier, max_over_ranks, world, no_autotune=Fal
             y.dev_polymul(dc, da, db, 1, L, log_n, cm0, scratch=sc, stream=stream)
 
     out = {"workload": "512 polymuls, log2 N uniform in 10..16, L uniform in 1..16 (seed 4)",
-           "limb_ntts": limb_ntts}
+           "limb_ntts": limb_ntts,
+           "launch_variants": tuned}
     for name, fn, steps in (("batched", batched, 10), ("persistent_queue", queue, 10), ("phased_queue", phased, 10),
                             ("per_call", per_call, 3)):
         for _ in range(2):
