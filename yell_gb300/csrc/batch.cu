@@ -2,9 +2,10 @@
 //
 // The batch is split into size buckets (one per degree).  Each bucket is
 // flattened into device-resident lists of limb pointers and modulus indices,
-// so one launch sequence (1 kernel for whole-limb degrees, 4 for two-pass
+// so one launch sequence (1 kernel for whole-limb degrees, 3 for two-pass
 // degrees) covers every polymul of that degree whatever its L.  Buckets run
-// concurrently on forked streams.  With graphs on, the whole fork/launch/join
+// concurrently on forked streams, launched in degree order (starting the
+// largest buckets first measured 1% slower on the 512-polymul uneven batch).  With graphs on, the whole fork/launch/join
 // sequence is captured once per batch shape (the ordered list of (degree,
 // limb count) buckets); later batches of the same shape upload their pointer
 // lists and replay the graph.
