@@ -34,7 +34,7 @@ def test_direct_path_is_used_where_supported(cuda):
     assert y.host_access()
 
 
-@pytest.mark.parametrize("log_n, L", [(16, 32), (17, 3), (15, 2)])
+@pytest.mark.parametrize("log_n, L", [(16, 32), (17, 3), (15, 2), (8, 300)])  # 300: two gather launches
 def test_host_ntt_paths(cuda, orc, both_paths, log_n, L):
     ps = y.primes(L)
     x = uniform_polys(4100 + log_n, 1, L, log_n, ps)[0]
