@@ -482,19 +482,30 @@ __global__ void __launch_bounds__(C::THREADS) k_row_pass(LimbSet ls, const DevMo
 // reduction of ntt<N>::forward, the Barrett product of ops::mulmod and the
 // bottom inverse round, on one register set.
 // ===========================================================================
+// First twiddle of the fused product round (its forward top sub-stage), for
+// callers that request it a round ahead.
+template <class C>
+__device__ __forceinline__ ulonglong2 fused_w0(uint32_t b, uint32_t s_off, uint32_t G, const DevMod& m) {
+  using RB = Round<C, C::NR - 1>;
+  return __ldg(m.fwd + (1u << (s_off + RB::HI)) + RB::gr(b, G));
+}
+
 template <class C, bool INV_LAST>
 __device__ __forceinline__ void fused_product(uint64_t* xa, uint64_t* xb, uint32_t b, uint32_t log_n,
-                                              uint32_t s_off, uint32_t G, const DevMod& m) {
+                                              uint32_t s_off, uint32_t G, const DevMod& m, ulonglong2 w0) {
   using RB = Round<C, C::NR - 1>;
   static_assert(RB::R == C::LOGE && RB::BETA == 0, "bottom round must be full width");
   constexpr int E = 1 << C::LOGE;
   const uint64_t p = m.p, p2 = m.p << 1;
   const uint32_t gr = RB::gr(b, G);
-  ct_stages2<RB::R, RB::E, 0>(xa, xb, m.fwd, s_off + RB::HI, gr, 0 - p, p2);
+  ct_stages2p<RB::R, RB::E, 0>(xa, xb, m.fwd, s_off + RB::HI, gr, 0 - p, p2, &w0);
+  // the inverse round's first twiddles load while the products compute
+  ulonglong2 wg[GsFirst<RB, INV_LAST>::N0];
+  GsFirst<RB, INV_LAST>::load(wg, m.inv, log_n, 0, gr);
 #pragma unroll
   for (int i = 0; i < E; ++i)
     xa[i] = mulmod_barrett(fwd_correct(xa[i], p, p2), fwd_correct(xb[i], p, p2), p, m.pn);
-  gs_round<RB, INV_LAST>(xa, log_n, 0, gr, m);
+  gs_round_w<RB, INV_LAST>(xa, log_n, 0, gr, m, wg);
 }
 
 // Whole-limb fused polymul: c = INTT(NTT(a) * NTT(b)), N <= 2^13.
@@ -515,15 +526,16 @@ __device__ __forceinline__ void polymul_whole_body(LimbSet c, ConstLimbSet a, Co
   constexpr int E = 1 << C::LOGE;
   uint64_t xa[E], xb[E];
   if constexpr (NR == 1) {
+    using RB = Round<C, 0>;
+    const uint32_t bb = RB::base(tid);
+    const ulonglong2 w0 = fused_w0<C>(bb, 0, 0, m);
     stage_in_limbs<C>(sa, a, limb0, c.count, log_n);
     stage_in_limbs<C>(sb, b, limb0, c.count, log_n);
     __syncthreads();
-    using RB = Round<C, 0>;
-    const uint32_t bb = RB::base(tid);
     if (active) {
       smem_load<RB>(xa, sa, bb);
       smem_load<RB>(xb, sb, bb);
-      fused_product<C, true>(xa, xb, bb, log_n, 0, 0, m);
+      fused_product<C, true>(xa, xb, bb, log_n, 0, 0, m, w0);
       smem_store<RB>(xa, sa, bb);
     }
     __syncthreads();
@@ -536,19 +548,19 @@ __device__ __forceinline__ void polymul_whole_body(LimbSet c, ConstLimbSet a, Co
     if (active) {
       gload_rows<R0>(xa, a.limb(my_limb, log_n), b0 & umask);
       gload_rows<R0>(xb, b.limb(my_limb, log_n), b0 & umask);
-      ct_stages2<R0::R, R0::E, 0>(xa, xb, m.fwd, R0::HI, R0::gr(b0, 0), 0 - m.p, m.p << 1);
+      ct_stages2<R0::R, R0::E>(xa, xb, m.fwd, R0::HI, R0::gr(b0, 0), 0 - m.p, m.p << 1);
       smem_store<R0>(xa, sa, b0);
       smem_store<R0>(xb, sb, b0);
     }
     round_barrier<C, BK>(tid);
-    fwd_rounds<C, 1, NR - 1, BK>(sa, tid, 0, 0, m.fwd, m.p, active);
-    fwd_rounds<C, 1, NR - 1, BK>(sb, tid, 0, 0, m.fwd, m.p, active);
     using RB = Round<C, NR - 1>;
     const uint32_t bb = RB::base(tid);
+    const ulonglong2 w0 = fused_w0<C>(bb, 0, 0, m);
+    fwd_rounds2<C, 1, NR - 1, BK>(sa, sb, tid, 0, 0, m.fwd, m.p, active);
     if (active) {
       smem_load<RB>(xa, sa, bb);
       smem_load<RB>(xb, sb, bb);
-      fused_product<C, false>(xa, xb, bb, log_n, 0, 0, m);
+      fused_product<C, false>(xa, xb, bb, log_n, 0, 0, m, w0);
       smem_store<RB>(xa, sa, bb);
     }
     round_barrier<C, BK>(tid);
@@ -593,7 +605,7 @@ __device__ __forceinline__ void col_pass2_body(ConstLimbSet a, ConstLimbSet b, L
   const uint32_t b0 = R0::base(tid);
   gload_cols<R0, LOGB>(xa, a.limb(limb, log_n) + col0, b0);
   gload_cols<R0, LOGB>(xb, b.limb(limb, log_n) + col0, b0);
-  ct_stages2<R0::R, R0::E, 0>(xa, xb, m.fwd, R0::HI, R0::gr(b0, 0), np, p2);
+  ct_stages2<R0::R, R0::E>(xa, xb, m.fwd, R0::HI, R0::gr(b0, 0), np, p2);
   if constexpr (NR == 1) {
     gstore_cols<R0, LOGB>(xa, ca.limb(limb, log_n) + col0, b0);
     gstore_cols<R0, LOGB>(xb, cb.limb(limb, log_n) + col0, b0);
@@ -601,13 +613,12 @@ __device__ __forceinline__ void col_pass2_body(ConstLimbSet a, ConstLimbSet b, L
     smem_store<R0>(xa, sa, b0);
     smem_store<R0>(xb, sb, b0);
     __syncthreads();
-    fwd_rounds<C, 1, NR - 1>(sa, tid, 0, 0, m.fwd, m.p, true);
-    fwd_rounds<C, 1, NR - 1>(sb, tid, 0, 0, m.fwd, m.p, true);
+    fwd_rounds2<C, 1, NR - 1>(sa, sb, tid, 0, 0, m.fwd, m.p, true);
     using RL = Round<C, NR - 1>;
     const uint32_t bl = RL::base(tid);
     smem_load<RL>(xa, sa, bl);
     smem_load<RL>(xb, sb, bl);
-    ct_stages2<RL::R, RL::E, 0>(xa, xb, m.fwd, RL::HI, RL::gr(bl, 0), np, p2);
+    ct_stages2<RL::R, RL::E>(xa, xb, m.fwd, RL::HI, RL::gr(bl, 0), np, p2);
     gstore_cols<RL, LOGB>(xa, ca.limb(limb, log_n) + col0, bl);
     gstore_cols<RL, LOGB>(xb, cb.limb(limb, log_n) + col0, bl);
   }
@@ -645,17 +656,17 @@ __device__ __forceinline__ void polymul_rows_body(LimbSet ca, ConstLimbSet sbuf,
   const uint32_t b0 = R0::base(tid);
   gload_rows<R0, COH>(xa, pa, b0);
   gload_rows<R0, COH>(xb, pb, b0);
-  ct_stages2<R0::R, R0::E, 0>(xa, xb, m.fwd, K1 + R0::HI, R0::gr(b0, G), 0 - m.p, m.p << 1);
+  ct_stages2<R0::R, R0::E>(xa, xb, m.fwd, K1 + R0::HI, R0::gr(b0, G), 0 - m.p, m.p << 1);
   smem_store<R0>(xa, sa, b0);
   smem_store<R0>(xb, sb, b0);
   round_barrier<C, BK>(tid);
-  fwd_rounds<C, 1, NR - 1, BK>(sa, tid, K1, G, m.fwd, m.p, true);
-  fwd_rounds<C, 1, NR - 1, BK>(sb, tid, K1, G, m.fwd, m.p, true);
   using RB = Round<C, NR - 1>;
   const uint32_t bb = RB::base(tid);
+  const ulonglong2 w0 = fused_w0<C>(bb, K1, G, m);
+  fwd_rounds2<C, 1, NR - 1, BK>(sa, sb, tid, K1, G, m.fwd, m.p, true);
   smem_load<RB>(xa, sa, bb);
   smem_load<RB>(xb, sb, bb);
-  fused_product<C, false>(xa, xb, bb, log_n, K1, G, m);
+  fused_product<C, false>(xa, xb, bb, log_n, K1, G, m, w0);
   smem_store<RB>(xa, sa, bb);
   round_barrier<C, BK>(tid);
   inv_rounds<C, NR - 2, 0, false, BK>(sa, tid, log_n, 0, G, m, true);
@@ -731,12 +742,11 @@ __global__ void __launch_bounds__(C::THREADS, min_blocks(512, C::THREADS))
     const uint32_t b0 = R0::base(tid);
     smem_load<R0>(xa, sa, b0);
     smem_load<R0>(xb, sb, b0);
-    ct_stages2<R0::R, R0::E, 0>(xa, xb, m.fwd, R0::HI, R0::gr(b0, 0), np, p2);
+    ct_stages2<R0::R, R0::E>(xa, xb, m.fwd, R0::HI, R0::gr(b0, 0), np, p2);
     smem_store<R0>(xa, sa, b0);  // the words this thread read: no barrier needed before
     smem_store<R0>(xb, sb, b0);
     __syncthreads();
-    fwd_rounds<C, 1, NR - 1>(sa, tid, 0, 0, m.fwd, m.p, true);
-    fwd_rounds<C, 1, NR - 1>(sb, tid, 0, 0, m.fwd, m.p, true);
+    fwd_rounds2<C, 1, NR - 1>(sa, sb, tid, 0, 0, m.fwd, m.p, true);
     using RL = Round<C, NR - 1>;
     const uint32_t bl = RL::base(tid);
     smem_load<RL>(xa, sa, bl);
@@ -749,7 +759,7 @@ __global__ void __launch_bounds__(C::THREADS, min_blocks(512, C::THREADS))
       stage_cols_async<C, LOGB>(sb, b.limb(nl, log_n) + nc);
       cp_async_commit();
     }
-    ct_stages2<RL::R, RL::E, 0>(xa, xb, m.fwd, RL::HI, RL::gr(bl, 0), np, p2);
+    ct_stages2<RL::R, RL::E>(xa, xb, m.fwd, RL::HI, RL::gr(bl, 0), np, p2);
     gstore_cols<RL, LOGB>(xa, ca.limb(limb, log_n) + col0, bl);
     gstore_cols<RL, LOGB>(xb, cb.limb(limb, log_n) + col0, bl);
   }
@@ -785,17 +795,17 @@ __global__ void __launch_bounds__(C::THREADS, min_blocks(512, C::THREADS))
     const uint32_t b0 = R0::base(tid);
     smem_load<R0>(xa, sa, b0);
     smem_load<R0>(xb, sb, b0);
-    ct_stages2<R0::R, R0::E, 0>(xa, xb, m.fwd, K1 + R0::HI, R0::gr(b0, G), 0 - m.p, m.p << 1);
+    ct_stages2<R0::R, R0::E>(xa, xb, m.fwd, K1 + R0::HI, R0::gr(b0, G), 0 - m.p, m.p << 1);
     smem_store<R0>(xa, sa, b0);
     smem_store<R0>(xb, sb, b0);
     round_barrier<C, BK>(tid);
-    fwd_rounds<C, 1, NR - 1, BK>(sa, tid, K1, G, m.fwd, m.p, true);
-    fwd_rounds<C, 1, NR - 1, BK>(sb, tid, K1, G, m.fwd, m.p, true);
     using RB = Round<C, NR - 1>;
     const uint32_t bb = RB::base(tid);
+    const ulonglong2 w0 = fused_w0<C>(bb, K1, G, m);
+    fwd_rounds2<C, 1, NR - 1, BK>(sa, sb, tid, K1, G, m.fwd, m.p, true);
     smem_load<RB>(xa, sa, bb);
     smem_load<RB>(xb, sb, bb);
-    fused_product<C, false>(xa, xb, bb, log_n, K1, G, m);
+    fused_product<C, false>(xa, xb, bb, log_n, K1, G, m, w0);
     smem_store<RB>(xa, sa, bb);
     round_barrier<C, BK>(tid);
     inv_rounds<C, NR - 2, 0, false, BK>(sa, tid, log_n, 0, G, m, true);

@@ -273,28 +273,40 @@ __device__ __forceinline__ void ct_round(W* x, const PW* __restrict__ tw, uint32
 }
 
 // The same round applied to two operands that share twiddles (the two
-// inputs of a polymul at the same limb and position).
+// inputs of a polymul at the same limb and position).  The twiddles of
+// sub-stage k+1 are requested before sub-stage k computes.
 template <int R, int E, int k, class W, class PW>
-__device__ __forceinline__ void ct_stages2(W* x, W* y, const PW* __restrict__ tw, uint32_t s_first, uint32_t gr,
-                                           W np, W p2) {
+__device__ __forceinline__ void ct_stages2p(W* x, W* y, const PW* __restrict__ tw, uint32_t s_first, uint32_t gr,
+                                            W np, W p2, const PW* wk) {
   if constexpr (k < R) {
     constexpr int d = 1 << (R - 1 - k);
     constexpr int NJ = 1 << k;
-    const PW* src = tw + (1u << (s_first + k)) + (gr << k);
+    constexpr int NN = (k + 1 < R) ? (2 << k) : 1;
+    PW wn[NN];
+    if constexpr (k + 1 < R) {
+      ld_twiddles<NN>(wn, tw + (1u << (s_first + k + 1)) + (gr << (k + 1)));
+    }
 #pragma unroll
-    for (int jj = 0; jj < NJ; ++jj) {
-      const PW w = __ldg(src + jj);
+    for (int jj = 0; jj < NJ; ++jj)
 #pragma unroll
       for (int ex = 0; ex < E; ++ex)
 #pragma unroll
         for (int q = 0; q < d; ++q) {
           const int j = jj * 2 * d + q;
-          ct_bfly(x[(ex << R) | j], x[(ex << R) | (j + d)], w.x, w.y, np, p2);
-          ct_bfly(y[(ex << R) | j], y[(ex << R) | (j + d)], w.x, w.y, np, p2);
+          ct_bfly(x[(ex << R) | j], x[(ex << R) | (j + d)], wk[jj].x, wk[jj].y, np, p2);
+          ct_bfly(y[(ex << R) | j], y[(ex << R) | (j + d)], wk[jj].x, wk[jj].y, np, p2);
         }
-    }
-    ct_stages2<R, E, k + 1>(x, y, tw, s_first, gr, np, p2);
+    ct_stages2p<R, E, k + 1>(x, y, tw, s_first, gr, np, p2, wn);
   }
+}
+
+// Two-operand round with its first sub-stage's twiddle loaded here.
+template <int R, int E, class W, class PW>
+__device__ __forceinline__ void ct_stages2(W* x, W* y, const PW* __restrict__ tw, uint32_t s_first, uint32_t gr,
+                                           W np, W p2) {
+  PW w0[1];
+  w0[0] = __ldg(tw + (1u << s_first) + gr);
+  ct_stages2p<R, E, 0>(x, y, tw, s_first, gr, np, p2, w0);
 }
 
 // Inverse sub-stage k pairs (j, j + 2^k) with twiddle
@@ -335,18 +347,34 @@ __device__ __forceinline__ void gs_stages(W* x, const PW* __restrict__ itw, uint
   }
 }
 
+// Twiddles of an inverse round's first sub-stage (loaded ahead by callers
+// that have other work to cover their latency with).
+template <class RG, bool LAST>
+struct GsFirst {
+  static constexpr bool ONLY_LAST = LAST && RG::R == 1;
+  static constexpr int N0 = ONLY_LAST ? 1 : (1 << (RG::R - 1));
+  template <class PW>
+  __device__ static __forceinline__ void load(PW* w0, const PW* __restrict__ itw, uint32_t log_n,
+                                              uint32_t sigma_first, uint32_t gr) {
+    if constexpr (!ONLY_LAST) {
+      ld_twiddles<N0>(w0, itw + (1u << (log_n - 1 - sigma_first)) + (gr << (RG::R - 1)));
+    }
+  }
+};
+
+// Inverse round with its first sub-stage's twiddles already loaded.
+template <class RG, bool LAST, class W, class M, class PW>
+__device__ __forceinline__ void gs_round_w(W* x, uint32_t log_n, uint32_t sigma_first, uint32_t gr, const M& m,
+                                           const PW* w0) {
+  gs_stages<RG::R, RG::E, LAST, 0>(x, m.inv, log_n - 1 - sigma_first, gr, m, w0);
+}
+
 template <class RG, bool LAST, class W, class M>
 __device__ __forceinline__ void gs_round(W* x, uint32_t log_n, uint32_t sigma_first, uint32_t gr, const M& m) {
-  constexpr int R = RG::R;
   using PW = typename PairOf<W>::type;
-  const uint32_t top = log_n - 1 - sigma_first;
-  constexpr bool ONLY_LAST = LAST && R == 1;
-  constexpr int N0 = ONLY_LAST ? 1 : (1 << (R - 1));
-  PW w0[N0];
-  if constexpr (!ONLY_LAST) {
-    ld_twiddles<N0>(w0, m.inv + (1u << top) + (gr << (R - 1)));
-  }
-  gs_stages<R, RG::E, LAST, 0>(x, m.inv, top, gr, m, w0);
+  PW w0[GsFirst<RG, LAST>::N0];
+  GsFirst<RG, LAST>::load(w0, m.inv, log_n, sigma_first, gr);
+  gs_round_w<RG, LAST>(x, log_n, sigma_first, gr, m, w0);
 }
 
 // Reads the DevMod for modulus index cm with read-only loads.
@@ -435,6 +463,27 @@ __device__ __forceinline__ void fwd_rounds(W* s, uint32_t tid, uint32_t s_off, u
     fwd_round_smem<C, I>(s, tid, s_off, G, tw, p, active);
     round_barrier<C, BK>(tid);
     fwd_rounds<C, I + 1, I1, BK>(s, tid, s_off, G, tw, p, active);
+  }
+}
+
+// Forward rounds [I, I1) of two operands at the same positions (shared
+// twiddles), a barrier after each.
+template <class C, int I, int I1, int BK = 0, class W, class PW>
+__device__ __forceinline__ void fwd_rounds2(W* sa, W* sb, uint32_t tid, uint32_t s_off, uint32_t G, const PW* tw,
+                                            W p, bool active) {
+  if constexpr (I < I1) {
+    using RG = Round<C, I>;
+    W xa[1 << C::LOGE], xb[1 << C::LOGE];
+    const uint32_t b = RG::base(tid);
+    if (active) {
+      smem_load<RG>(xa, sa, b);
+      smem_load<RG>(xb, sb, b);
+      ct_stages2<RG::R, RG::E>(xa, xb, tw, s_off + RG::HI, RG::gr(b, G), (W)(0 - p), (W)(p << 1));
+      smem_store<RG>(xa, sa, b);
+      smem_store<RG>(xb, sb, b);
+    }
+    round_barrier<C, BK>(tid);
+    fwd_rounds2<C, I + 1, I1, BK>(sa, sb, tid, s_off, G, tw, p, active);
   }
 }
 
