@@ -305,6 +305,14 @@ int yell32_dev_ntt(uint32_t* d_polys, uint32_t count, uint32_t L, uint32_t log_n
                    int direction, void* stream);
 int yell32_dev_polymul(uint32_t* d_c, const uint32_t* d_a, const uint32_t* d_b, uint32_t pairs,
                        uint32_t L, uint32_t log_n, uint32_t cm0, void* stream);
+/* At N = 2^14 and 2^15 the polymul's CTAs wait on the device for the bulk
+ * copies that bring their operands into shared memory, each wait for at most
+ * 1 s.  A wait that runs out records YELL_ERR_TIMEOUT and the kernel still
+ * finishes (its output is then undefined).  This call waits for all work
+ * queued on the current device, stores the recorded status (YELL_OK or
+ * YELL_ERR_TIMEOUT) in *status and clears it.  No counterpart in the
+ * reference, whose calls do not wait on a device. */
+int yell32_wait_status(uint32_t* status);
 int yell32_dev_elementwise(int op, uint32_t* d_dst, const uint32_t* d_a, const uint32_t* d_b,
                            uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0, void* stream);
 /* poly<N> members on host limbs (moduli 0 .. L-1), as yell_poly_* above */

@@ -59,9 +59,32 @@ def test_device_polymul(cuda, o32, log_n):
     c = cuda.zeros(pairs * L * n, dtype=cuda.int32, device="cuda")
     m32.dev_polymul(c, _dev(cuda, a), _dev(cuda, b), pairs, L, log_n, cm0)
     cuda.cuda.synchronize()
+    assert m32.wait_status() == 0
     got = _host(c, (pairs, L, n))
     for i in range(pairs):
         assert np.array_equal(got[i], o32.polymul(a[i], b[i], log_n, cm0)), (log_n, i)
+
+
+@pytest.mark.parametrize("log_n", [14, 15])
+def test_polymul_offset_operands(cuda, o32, log_n):
+    """Operands and output 16 bytes past an allocation's start: the bulk copies
+    that stage the CTA-pair kernel's operands need 16-byte alignment only."""
+    pairs, L = 2, 2
+    n = 1 << log_n
+    a, b = _polys(21, pairs, L, log_n, 0), _polys(22, pairs, L, log_n, 0)
+    words = pairs * L * n
+
+    def shifted(x):
+        t = cuda.zeros(words + 4, dtype=cuda.int32, device="cuda")
+        t[4:] = _dev(cuda, x)
+        return t[4:]
+
+    c = cuda.zeros(words + 4, dtype=cuda.int32, device="cuda")[4:]
+    m32.dev_polymul(c, shifted(a), shifted(b), pairs, L, log_n, 0)
+    assert m32.wait_status() == 0
+    got = _host(c, (pairs, L, n))
+    for i in range(pairs):
+        assert np.array_equal(got[i], o32.polymul(a[i], b[i], log_n)), (log_n, i)
 
 
 def test_polymul_many_limbs(cuda, o32):
@@ -124,6 +147,7 @@ def test_full_size_roundtrip(cuda):
     c = cuda.zeros_like(t)
     m32.dev_polymul(c, _dev(cuda, a), _dev(cuda, one), pairs, L, log_n, 0)
     cuda.cuda.synchronize()
+    assert m32.wait_status() == 0
     assert np.array_equal(_host(c, a.shape), a)
 
 

@@ -5,12 +5,15 @@
 // The kernels reuse the tile engine of the 64-bit path at 32-bit words.  A CTA
 // holds whole limbs in shared memory (2^T words, T = max(log_n, 11), several
 // limbs per CTA below 2^11); every word is read from HBM once and written
-// once.  The fused polymul keeps one operand tile in shared memory at a time:
-// NTT(a) leaves its last forward round in registers and parks the reduced
-// words in the output limb (the same thread reads them back, so they stay in
-// L2), NTT(b) then runs in the same buffer, and the product, inverse rounds
-// and scaled last layer follow.  The butterflies, their order and their
-// twiddle indices are the reference's, so lazy words match it exactly.
+// once.  The single-CTA fused polymul keeps one operand tile in shared memory
+// at a time: NTT(a) leaves its last forward round in registers and parks the
+// reduced words in the output limb (the same thread reads them back, so they
+// stay in L2), NTT(b) then runs in the same buffer, and the product, inverse
+// rounds and scaled last layer follow.  At 2^14 and 2^15 a limb is split over
+// a CTA pair whose operands arrive by bulk asynchronous copies, b's while a
+// computes, and a's NTT waits in shared memory.  The butterflies, their order
+// and their twiddle indices are the reference's, so lazy words match it
+// exactly.
 #include <algorithm>
 #include <cstring>
 #include <memory>
@@ -518,6 +521,198 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PC::C::THREADS, PC::
   cluster.sync();  // the peer may still be reading this CTA's shared memory
 }
 
+// ---- polymul by a CTA pair with staged operands ------------------------------
+// The same butterflies as k32_polymul_pair, with the operands moved by bulk
+// asynchronous copies (cp.async.bulk, completion counted on an mbarrier):
+// both halves of a's limb land in a raw staging area S of shared memory; the
+// stage-0 butterflies read them from there; then b's copy into S starts and
+// runs while a's remaining stages compute.  a's reduced NTT stays in the work
+// tile W where its bottom round left it, and b is transformed in place in S
+// (its own-half outputs overwrite the raw words once every thread has read
+// its pairs).  Shared memory: W (half limb) + S (whole limb) + the mbarrier.
+// Every wait on the mbarrier is bounded; one that runs out records
+// YELL_ERR_TIMEOUT in g_k32_wait_status and the kernel carries on, so that
+// every thread still reaches every barrier.
+__device__ uint32_t g_k32_wait_status;
+
+__device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(mbar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Thread 0: announce `bytes` of copies on the mbarrier and start them.
+__device__ __forceinline__ void mbar_expect(uint64_t* mbar, uint32_t bytes) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(mbar);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+
+// Global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  const uint32_t b = (uint32_t)__cvta_generic_to_shared(mbar);
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(d), "l"(src), "r"(bytes), "r"(b) : "memory");
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits for phase `parity` of the mbarrier for at most 1 s of the global
+// timer or 2^24 polls.  Returns false, after recording YELL_ERR_TIMEOUT, when
+// either limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(mbar);
+  const uint64_t t0 = globaltimer_ns();
+  for (uint32_t i = 0; i < (1u << 24); ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((i & 255u) == 255u && globaltimer_ns() - t0 > 1000000000ull) break;
+  }
+  atomicCAS(&g_k32_wait_status, 0u, (uint32_t)YELL_ERR_TIMEOUT);
+  return false;
+}
+
+// Stage 0 (pairs N/2 apart, twiddle w[1]) from the raw halves of a limb in
+// S_lo and S_hi into this CTA's half in `dst` (swizzled tile layout).  With
+// IN_PLACE, dst overlaps S_lo:
+// every thread keeps its outputs in registers until all raw words are read.
+// Ends with a CTA barrier.
+template <class PC, bool IN_PLACE>
+__device__ __forceinline__ void stage0_from_smem(uint32_t* dst, const uint32_t* S_lo, const uint32_t* S_hi,
+                                                 uint32_t tid, uint32_t r, uint32_t p, uint2 w1) {
+  using C = typename PC::C;
+  constexpr uint32_t half = 1u << C::K;
+  constexpr int IT = (int)(half / (C::THREADS * 4));
+  const uint32_t p2 = p << 1, np = 0u - p;
+  uint4 out[IN_PLACE ? IT : 1];
+#pragma unroll
+  for (int i = 0; i < IT; ++i) {
+    const uint32_t v = (tid + i * C::THREADS) * 4;
+    const uint4 lo = *reinterpret_cast<const uint4*>(S_lo + v);
+    const uint4 hi = *reinterpret_cast<const uint4*>(S_hi + v);
+    uint32_t u0[4] = {lo.x, lo.y, lo.z, lo.w}, u1[4] = {hi.x, hi.y, hi.z, hi.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) ct_bfly(u0[k], u1[k], w1.x, w1.y, np, p2);
+    const uint4 o = r == 0 ? make_uint4(u0[0], u0[1], u0[2], u0[3]) : make_uint4(u1[0], u1[1], u1[2], u1[3]);
+    if constexpr (IN_PLACE) out[i] = o;
+    else *reinterpret_cast<uint4*>(dst + Smem<uint32_t>::idx(v)) = o;
+  }
+  if constexpr (IN_PLACE) {
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < IT; ++i)
+      *reinterpret_cast<uint4*>(dst + Smem<uint32_t>::idx((tid + i * C::THREADS) * 4)) = out[i];
+  }
+  __syncthreads();
+}
+
+// Stages 1 .. log N - 1 of the half limb in `work` (after stage 0), the last
+// round into the registers x; the same rounds as pair_forward.
+template <class PC>
+__device__ __forceinline__ void pair_forward_rounds(uint32_t* x, uint32_t* work, uint32_t tid, uint32_t r,
+                                                    const DevMod32& m) {
+  using C = typename PC::C;
+  using S = typename PC::S;
+  using CA = typename S::CA;
+  using CB = typename S::CB;
+  using RBB = Round<CB, CB::NR - 1>;
+  constexpr uint32_t s_rows = 1 + S::KTOP_STAGES;
+  fwd_rounds<CA, 0, CA::NR>(work, tid, 1, r, m.fwd, m.p, true);
+  const uint32_t G = S::row_group(r, tid);
+  fwd_rounds<CB, 0, CB::NR - 1, CB::LOCAL_BARRIER>(work, tid, s_rows, G, m.fwd, m.p, true);
+  const uint32_t bb = RBB::base(tid);
+  smem_load<RBB>(x, work, bb);
+  ct_round<RBB>(x, m.fwd, s_rows + RBB::HI, RBB::gr(bb, G), m.p);
+}
+
+template <int LOGN>
+struct StagedCfg32 {
+  using PC = PairCfg32<LOGN>;
+  static constexpr uint32_t kHalf = 1u << (LOGN - 1);
+  static constexpr size_t kSmem = 3 * (size_t)kHalf * sizeof(uint32_t) + 16;  // W, S, mbarrier
+  static constexpr int MIN_BLOCKS = (int)(228 * 1024 / (kSmem + 1024)) < PC::MIN_BLOCKS
+                                        ? (int)(228 * 1024 / (kSmem + 1024))
+                                        : PC::MIN_BLOCKS;
+};
+
+template <int LOGN>
+__global__ void __cluster_dims__(2, 1, 1)
+    __launch_bounds__(PairCfg32<LOGN>::C::THREADS, StagedCfg32<LOGN>::MIN_BLOCKS)
+    k32_polymul_pair_staged(uint32_t* c, const uint32_t* a, const uint32_t* b, Limbs32 ls,
+                            const DevMod32* __restrict__ mods) {
+  namespace cg = cooperative_groups;
+  using PC = PairCfg32<LOGN>;
+  using C = typename PC::C;
+  extern __shared__ __align__(128) uint32_t smem_st[];
+  constexpr int H = C::K, NR = C::NR, E = 1 << C::LOGE;
+  constexpr uint32_t log_n = H + 1, half = 1u << H;
+  using RB = Round<C, NR - 1>;
+  static_assert(RB::R == C::LOGE && RB::BETA == 0 && RB::EB == 0, "bottom round must own contiguous words");
+  uint32_t* W = smem_st;             // a's tile, then a's parked NTT
+  uint32_t* S = smem_st + half;      // raw limb (2 halves); b's tile after its stage 0
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_st + 3 * half);
+  cg::cluster_group cluster = cg::this_cluster();
+  const uint32_t r = cluster.block_rank();
+  const uint32_t limb = blockIdx.x >> 1;
+  const uint32_t tid = threadIdx.x;
+  const DevMod32 m = load_mod(mods, ls.cm(limb));
+  const uint32_t p = m.p, p2 = p << 1;
+  const uint2 w1 = __ldg(m.fwd + 1);
+  const size_t lbase = (size_t)limb << log_n;
+  const uint32_t bb = RB::base(tid);
+  if (tid == 0) {
+    mbar_init(mbar, 1);
+    mbar_expect(mbar, 2 * half * (uint32_t)sizeof(uint32_t));
+    bulk_g2s(S, a + lbase, half * (uint32_t)sizeof(uint32_t), mbar);
+    bulk_g2s(S + half, a + lbase + half, half * (uint32_t)sizeof(uint32_t), mbar);
+  }
+  __syncthreads();  // the mbarrier is initialised before anyone polls it
+  mbar_wait(mbar, 0);
+  stage0_from_smem<PC, false>(W, S, S + half, tid, r, p, w1);
+  if (tid == 0) {
+    // S was read through the generic proxy; the copies write it through the async one
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect(mbar, 2 * half * (uint32_t)sizeof(uint32_t));
+    bulk_g2s(S, b + lbase, half * (uint32_t)sizeof(uint32_t), mbar);
+    bulk_g2s(S + half, b + lbase + half, half * (uint32_t)sizeof(uint32_t), mbar);
+  }
+  uint32_t x[E];
+  pair_forward_rounds<PC>(x, W, tid, r, m);
+  // park a's reduced words where its bottom round read them (only this thread's positions)
+#pragma unroll
+  for (int i = 0; i < E; ++i) x[i] = fwd_correct(x[i], p, p2);
+  smem_store<RB>(x, W, bb);
+  mbar_wait(mbar, 1);
+  stage0_from_smem<PC, true>(S, S, S + half, tid, r, p, w1);
+  pair_forward_rounds<PC>(x, S, tid, r, m);
+  {
+    const uint32_t ib = Smem<uint32_t>::idx(bb);
+#pragma unroll
+    for (int i = 0; i < E; i += 4) {
+      const uint4 ah = *reinterpret_cast<const uint4*>(W + (ib ^ (uint32_t)i));
+      x[i] = mulmod_barrett(ah.x, fwd_correct(x[i], p, p2), p, m.pn);
+      x[i + 1] = mulmod_barrett(ah.y, fwd_correct(x[i + 1], p, p2), p, m.pn);
+      x[i + 2] = mulmod_barrett(ah.z, fwd_correct(x[i + 2], p, p2), p, m.pn);
+      x[i + 3] = mulmod_barrett(ah.w, fwd_correct(x[i + 3], p, p2), p, m.pn);
+    }
+  }
+  pair_inverse<PC>(x, S, tid, r, bb, m);
+  cluster.sync();
+  pair_last_layer<PC, true>(c + lbase + r * half, S, cluster.map_shared_rank(S, (int)(r ^ 1u)), tid, r, m);
+  cluster.sync();  // the peer may still be reading this CTA's shared memory
+}
+
 // In-place NTT of one limb by a CTA pair (DIR: 0 forward, 1 forward lazy,
 // 2 backward), same split as k32_polymul_pair.
 template <class PC, int DIR>
@@ -586,8 +781,12 @@ __global__ void k32_elementwise(uint32_t* dst, const uint32_t* a, const uint32_t
 }
 
 // ---- launch ----------------------------------------------------------------------
-// Degrees whose polymul runs on a CTA pair.
+// Degrees whose polymul runs on a CTA pair, with staged operands
+// (k32_polymul_pair_staged; measured on GB300 at L = 32 and 2^20 words per
+// operand: 2^15 203.6 us against 223.3 us for k32_polymul_pair, 2^14 176.4
+// against 195.9 us).
 constexpr int kMinPairLogN = 14;
+constexpr int kStagedMinLogN = 14;
 // Host-pointer calls up to this degree (single-CTA kernels) run in place on
 // the context's pinned, device-mapped host buffer.
 constexpr uint32_t kSmallCall32LogN = 13;
@@ -607,6 +806,9 @@ cudaError_t set_attrs32() {
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k32_polymul_pair<PC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)PC::kSmem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k32_polymul_pair_staged<LOGN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)StagedCfg32<LOGN>::kSmem);
   }
   return e;
 }
@@ -624,6 +826,8 @@ cudaError_t launch32(int kind, uint32_t* c, const uint32_t* a, const uint32_t* b
     if (kind == 0) k32_ntt_pair<PC, 0><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
     else if (kind == 1) k32_ntt_pair<PC, 1><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
     else if (kind == 2) k32_ntt_pair<PC, 2><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
+    else if (LOGN >= kStagedMinLogN)
+      k32_polymul_pair_staged<LOGN><<<g, P::THREADS, StagedCfg32<LOGN>::kSmem, st>>>(c, a, b, ls, mods);
     else k32_polymul_pair<PC><<<g, P::THREADS, PC::kSmem, st>>>(c, a, b, ls, mods);
     return cudaGetLastError();
   }
@@ -777,6 +981,25 @@ int yell32_dev_polymul(uint32_t* d_c, const uint32_t* d_a, const uint32_t* d_b, 
   if (!d_c || !d_a || !d_b || pairs == 0) return fail(kInvalidArgument, "null pointer or zero pairs");
   if (d_c == d_a || d_c == d_b) return fail(kInvalidArgument, "the product may not overwrite an operand");
   return run32(3, d_c, d_a, d_b, pairs, L, log_n, cm0, stream);
+}
+
+int yell32_wait_status(uint32_t* status) {
+  if (!status) return fail(kInvalidArgument, "null output");
+  int st = kOk;
+  DeviceContext* ctx = DeviceContext::current(&st);
+  if (!ctx) return st;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return fail_cuda(e, "synchronize");
+  uint32_t v = 0;
+  e = cudaMemcpyFromSymbol(&v, g_k32_wait_status, sizeof(v));
+  if (e != cudaSuccess) return fail_cuda(e, "read wait status");
+  if (v != 0) {
+    const uint32_t zero = 0;
+    e = cudaMemcpyToSymbol(g_k32_wait_status, &zero, sizeof(zero));
+    if (e != cudaSuccess) return fail_cuda(e, "clear wait status");
+  }
+  *status = v;
+  return kOk;
 }
 
 int yell32_dev_elementwise(int op, uint32_t* d_dst, const uint32_t* d_a, const uint32_t* d_b, uint32_t count,

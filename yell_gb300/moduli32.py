@@ -89,6 +89,15 @@ def dev_polymul(c, a, b, pairs: int, L: int, log_n: int, cm0: int = 0, stream=No
     call("yell32_dev_polymul", _dptr(c), _dptr(a), _dptr(b), pairs, L, log_n, cm0, _stream(stream))
 
 
+def wait_status() -> int:
+    """Waits for the device's queued work and returns (and clears) the status the
+    2^14 / 2^15 polymul kernels record when a wait for their operand copies runs out."""
+    import ctypes
+    st = ctypes.c_uint32(0)
+    call("yell32_wait_status", ctypes.byref(st))
+    return st.value
+
+
 def dev_elementwise(op: int, dst, a, b, count: int, L: int, log_n: int, cm0: int = 0,
                     stream=None) -> None:
     call("yell32_dev_elementwise", op, _dptr(dst), _dptr(a), _dptr(b) if b is not None else None,
