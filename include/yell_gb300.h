@@ -313,6 +313,11 @@ int yell32_dev_polymul(uint32_t* d_c, const uint32_t* d_a, const uint32_t* d_b, 
  * YELL_ERR_TIMEOUT) in *status and clears it.  No counterpart in the
  * reference, whose calls do not wait on a device. */
 int yell32_wait_status(uint32_t* status);
+/* Check of that bounded wait: a one-CTA kernel announces copies on an
+ * mbarrier, starts none, and waits as the polymul kernels do; the wait runs
+ * out after timeout_ns (<= 10 s) and *status receives YELL_ERR_TIMEOUT (read
+ * and cleared as by yell32_wait_status).  Synchronous. */
+int yell32_wait_check(uint64_t timeout_ns, uint32_t* status);
 int yell32_dev_elementwise(int op, uint32_t* d_dst, const uint32_t* d_a, const uint32_t* d_b,
                            uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0, void* stream);
 /* poly<N> members on host limbs (moduli 0 .. L-1), as yell_poly_* above */

@@ -151,6 +151,23 @@ def test_full_size_roundtrip(cuda):
     assert np.array_equal(_host(c, a.shape), a)
 
 
+def test_wait_check(cuda, o32):
+    """The staged 2^14 / 2^15 polymul's bounded copy wait: a wait that nothing
+    completes runs out and reports YELL_ERR_TIMEOUT, no GPU fault; the status is
+    read and cleared, and a polymul afterwards runs normally."""
+    from yell_gb300._capi import YELL_ERR_TIMEOUT
+    assert m32.wait_check(0.02) == YELL_ERR_TIMEOUT
+    assert m32.wait_status() == 0
+    with pytest.raises(YellError):
+        m32.wait_check(0.0)
+    pairs, L, log_n = 1, 2, 15
+    a, b = _polys(31, pairs, L, log_n, 0), _polys(32, pairs, L, log_n, 0)
+    c = cuda.zeros(pairs * L << log_n, dtype=cuda.int32, device="cuda")
+    m32.dev_polymul(c, _dev(cuda, a), _dev(cuda, b), pairs, L, log_n, 0)
+    assert m32.wait_status() == 0
+    assert np.array_equal(_host(c, (pairs, L, 1 << log_n))[0], o32.polymul(a[0], b[0], log_n))
+
+
 def test_errors(cuda):
     t = cuda.zeros(1 << 16, dtype=cuda.int32, device="cuda")
     with pytest.raises(YellError):

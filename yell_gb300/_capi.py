@@ -108,6 +108,7 @@ SIGNATURES = {
     "yell32_dev_ntt": (_int, [_vp, _u32, _u32, _u32, _u32, _int, _vp]),
     "yell32_dev_polymul": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),
     "yell32_wait_status": (_int, [_vp]),
+    "yell32_wait_check": (_int, [_u64, _vp]),
     "yell32_dev_elementwise": (_int, [_int, _vp, _vp, _vp, _u32, _u32, _u32, _u32, _vp]),
     "yell32_poly_forward": (_int, [_vp, _u32, _u32]),
     "yell32_poly_forward_lazy": (_int, [_vp, _u32, _u32]),

@@ -24,6 +24,7 @@
 
 #include <cooperative_groups.h>
 
+#include "async_copy.cuh"
 #include "kernels.h"
 #include "ntt_tile.cuh"
 #include "profiler.h"
@@ -535,58 +536,31 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PC::C::THREADS, PC::
 // every thread still reaches every barrier.
 __device__ uint32_t g_k32_wait_status;
 
-__device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
-  const uint32_t a = (uint32_t)__cvta_generic_to_shared(mbar);
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+// Bounded wait on the staged kernel's mbarrier; a wait that runs out records
+// YELL_ERR_TIMEOUT in g_k32_wait_status.
+__device__ __forceinline__ bool mbar_wait32(uint64_t* mbar, uint32_t parity,
+                                            uint64_t timeout_ns = 1000000000ull) {
+  return mbar_wait(mbar, parity, &g_k32_wait_status, (uint32_t)YELL_ERR_TIMEOUT, timeout_ns);
 }
 
-// Thread 0: announce `bytes` of copies on the mbarrier and start them.
-__device__ __forceinline__ void mbar_expect(uint64_t* mbar, uint32_t bytes) {
-  const uint32_t a = (uint32_t)__cvta_generic_to_shared(mbar);
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
-}
-
-// Global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16).
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
-  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
-  const uint32_t b = (uint32_t)__cvta_generic_to_shared(mbar);
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-               ::"r"(d), "l"(src), "r"(bytes), "r"(b) : "memory");
-}
-
-__device__ __forceinline__ uint64_t globaltimer_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Waits for phase `parity` of the mbarrier for at most 1 s of the global
-// timer or 2^24 polls.  Returns false, after recording YELL_ERR_TIMEOUT, when
-// either limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
-  const uint32_t a = (uint32_t)__cvta_generic_to_shared(mbar);
-  const uint64_t t0 = globaltimer_ns();
-  for (uint32_t i = 0; i < (1u << 24); ++i) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if ((i & 255u) == 255u && globaltimer_ns() - t0 > 1000000000ull) break;
+// Check of that bounded wait: one CTA announces 16 bytes of copies on an
+// mbarrier, starts none, and waits on it the way the staged kernel does; the
+// wait runs out after timeout_ns and records YELL_ERR_TIMEOUT.  No copy is in
+// flight when the CTA exits.
+__global__ void k32_wait_check(uint64_t timeout_ns) {
+  __shared__ uint64_t mbar;
+  if (threadIdx.x == 0) {
+    mbar_init(&mbar, 1);
+    mbar_expect(&mbar, 16);
   }
-  atomicCAS(&g_k32_wait_status, 0u, (uint32_t)YELL_ERR_TIMEOUT);
-  return false;
+  __syncthreads();
+  mbar_wait32(&mbar, 0, timeout_ns);
 }
 
 // Stage 0 (pairs N/2 apart, twiddle w[1]) from the raw halves of a limb in
 // S_lo and S_hi into this CTA's half in `dst` (swizzled tile layout).  With
-// IN_PLACE, dst overlaps S_lo:
-// every thread keeps its outputs in registers until all raw words are read.
+// IN_PLACE, dst overlaps S_lo: every thread keeps its outputs in registers
+// until all raw words are read.
 // Ends with a CTA barrier.
 template <class PC, bool IN_PLACE>
 __device__ __forceinline__ void stage0_from_smem(uint32_t* dst, const uint32_t* S_lo, const uint32_t* S_hi,
@@ -678,11 +652,11 @@ __global__ void __cluster_dims__(2, 1, 1)
     bulk_g2s(S + half, a + lbase + half, half * (uint32_t)sizeof(uint32_t), mbar);
   }
   __syncthreads();  // the mbarrier is initialised before anyone polls it
-  mbar_wait(mbar, 0);
+  mbar_wait32(mbar, 0);
   stage0_from_smem<PC, false>(W, S, S + half, tid, r, p, w1);
   if (tid == 0) {
     // S was read through the generic proxy; the copies write it through the async one
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    fence_proxy_async();
     mbar_expect(mbar, 2 * half * (uint32_t)sizeof(uint32_t));
     bulk_g2s(S, b + lbase, half * (uint32_t)sizeof(uint32_t), mbar);
     bulk_g2s(S + half, b + lbase + half, half * (uint32_t)sizeof(uint32_t), mbar);
@@ -693,7 +667,7 @@ __global__ void __cluster_dims__(2, 1, 1)
 #pragma unroll
   for (int i = 0; i < E; ++i) x[i] = fwd_correct(x[i], p, p2);
   smem_store<RB>(x, W, bb);
-  mbar_wait(mbar, 1);
+  mbar_wait32(mbar, 1);
   stage0_from_smem<PC, true>(S, S, S + half, tid, r, p, w1);
   pair_forward_rounds<PC>(x, S, tid, r, m);
   {
@@ -981,6 +955,19 @@ int yell32_dev_polymul(uint32_t* d_c, const uint32_t* d_a, const uint32_t* d_b, 
   if (!d_c || !d_a || !d_b || pairs == 0) return fail(kInvalidArgument, "null pointer or zero pairs");
   if (d_c == d_a || d_c == d_b) return fail(kInvalidArgument, "the product may not overwrite an operand");
   return run32(3, d_c, d_a, d_b, pairs, L, log_n, cm0, stream);
+}
+
+int yell32_wait_check(uint64_t timeout_ns, uint32_t* status) {
+  if (!status) return fail(kInvalidArgument, "null output");
+  if (timeout_ns == 0 || timeout_ns > 10'000'000'000ull) return fail(kInvalidArgument, "timeout must be in (0, 10 s]");
+  int st = kOk;
+  DeviceContext* ctx = DeviceContext::current(&st);
+  if (!ctx) return st;
+  k32_wait_check<<<1, 32, 0, ctx->stream()>>>(timeout_ns);
+  g_kernel_launches += 1;
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail_cuda(e, "wait check");
+  return yell32_wait_status(status);
 }
 
 int yell32_wait_status(uint32_t* status) {

@@ -98,6 +98,15 @@ def wait_status() -> int:
     return st.value
 
 
+def wait_check(timeout_s: float) -> int:
+    """Runs the check of the bounded copy wait: a wait that nothing completes runs
+    out after timeout_s and the returned status is YELL_ERR_TIMEOUT."""
+    import ctypes
+    st = ctypes.c_uint32(0)
+    call("yell32_wait_check", int(timeout_s * 1e9), ctypes.byref(st))
+    return st.value
+
+
 def dev_elementwise(op: int, dst, a, b, count: int, L: int, log_n: int, cm0: int = 0,
                     stream=None) -> None:
     call("yell32_dev_elementwise", op, _dptr(dst), _dptr(a), _dptr(b) if b is not None else None,
