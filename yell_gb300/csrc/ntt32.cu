@@ -361,25 +361,40 @@ struct HalfSplit {
   }
 };
 
-// 2^14: 256-thread CTAs of 32 words per thread, three per SM at 80 registers.
-// 2^15: 1024-thread CTAs of 16 words per thread, one per SM at 64 registers,
-// top 7 stages across the CTA and rows of 128 words: the same 32 resident
-// warps per SM as two 512-thread CTAs of 32 words, without their 216 bytes of
-// register spills, and 1024 CTA-sized units per 512-limb launch fill 6.7
-// waves of 152 SMs where limb pairs filled 3.4 waves of 304 slots.  Measured
-// on GB300 (N = 2^15, L = 32, 16 pairs): 0.2228 ms, the same as two 512-thread
-// CTAs per SM (0.2228 ms); with the top 6 or 8 stages across the CTA 0.2238
-// and 0.2273 ms.
-template <int LOGN>
-struct PairCfg32 {
+// Geometry of a CTA-pair kernel: half limbs of 2^(LOGN-1) words, 2^LOGE words
+// per thread, the top KTOP stages of the half across the CTA.
+template <int LOGN, int LOGE_, int KTOP_>
+struct PairGeom32 {
   static constexpr int H = LOGN - 1;
-  static constexpr int LOGE = LOGN >= 15 ? 4 : 5;
-  static constexpr int KTOP = LOGN >= 15 ? 7 : 5;
+  static constexpr int LOGE = LOGE_;
+  static constexpr int KTOP = KTOP_;
   using C = TileCfg<H, H, 0, LOGE>;
   using S = HalfSplit<H, LOGE, KTOP>;
   static constexpr int MIN_BLOCKS = C::THREADS <= 256 ? 3 : (C::THREADS <= 512 ? 2 : 1);
   static constexpr size_t kSmem = Smem<uint32_t>::words(1u << H) * sizeof(uint32_t);
 };
+
+// Polymul.  2^14: 256-thread CTAs of 32 words per thread, three per SM at 80
+// registers.  2^15: 1024-thread CTAs of 16 words per thread, one per SM at 64
+// registers, top 7 stages across the CTA and rows of 128 words: the same 32
+// resident warps per SM as two 512-thread CTAs of 32 words, without their
+// 216 bytes of register spills, and 1024 CTA-sized units per 512-limb launch
+// fill 6.7 waves of 152 SMs where limb pairs filled 3.4 waves of 304 slots.
+// Measured on GB300 (N = 2^15, L = 32, 16 pairs): 0.2228 ms, the same as two
+// 512-thread CTAs per SM (0.2228 ms); with the top 6 or 8 stages across the
+// CTA 0.2238 and 0.2273 ms.  Staged (k32_polymul_pair_staged, one CTA per SM
+// by its shared memory), 512-thread CTAs of 32 words at 128 registers took
+// 0.2087 / 0.2195 / 0.2353 ms with the top 5 / 6 / 7 stages across the CTA,
+// against 0.2053 ms for this geometry.
+template <int LOGN>
+using PairCfg32 = PairGeom32<LOGN, (LOGN >= 15 ? 4 : 5), (LOGN >= 15 ? 7 : 5)>;
+
+// NTT alone: 32 words per thread at both degrees; at 2^15 two 512-thread CTAs
+// per SM (64 registers, no spills) with the top 5 stages across the CTA:
+// rounds of 5 stages, one exchange fewer per transform.  Measured (2^15,
+// L = 32, 16 polys): backward 90.7 -> 77.1 us, forward 83.4 / 83.8 us.
+template <int LOGN>
+using NttPairCfg32 = PairGeom32<LOGN, 5, 5>;
 
 // Forward NTT of one half limb of `src` (the limb's first word) into the
 // bottom-round registers x of this thread: stage 0 while loading, stages
@@ -775,8 +790,9 @@ cudaError_t set_attrs32() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k32_polymul<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if constexpr (LOGN >= kMinPairLogN) {
     using PC = PairCfg32<LOGN>;
-    for (auto k : {k32_ntt_pair<PC, 0>, k32_ntt_pair<PC, 1>, k32_ntt_pair<PC, 2>})
-      if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PC::kSmem);
+    using NC = NttPairCfg32<LOGN>;
+    for (auto k : {k32_ntt_pair<NC, 0>, k32_ntt_pair<NC, 1>, k32_ntt_pair<NC, 2>})
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)NC::kSmem);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k32_polymul_pair<PC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)PC::kSmem);
@@ -796,10 +812,12 @@ cudaError_t launch32(int kind, uint32_t* c, const uint32_t* a, const uint32_t* b
   if constexpr (LOGN >= kMinPairLogN) {
     using PC = PairCfg32<LOGN>;
     using P = typename PC::C;
+    using NC = NttPairCfg32<LOGN>;
+    using NP = typename NC::C;
     const uint32_t g = 2 * ls.count;
-    if (kind == 0) k32_ntt_pair<PC, 0><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
-    else if (kind == 1) k32_ntt_pair<PC, 1><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
-    else if (kind == 2) k32_ntt_pair<PC, 2><<<g, P::THREADS, PC::kSmem, st>>>(c, ls, mods);
+    if (kind == 0) k32_ntt_pair<NC, 0><<<g, NP::THREADS, NC::kSmem, st>>>(c, ls, mods);
+    else if (kind == 1) k32_ntt_pair<NC, 1><<<g, NP::THREADS, NC::kSmem, st>>>(c, ls, mods);
+    else if (kind == 2) k32_ntt_pair<NC, 2><<<g, NP::THREADS, NC::kSmem, st>>>(c, ls, mods);
     else if (LOGN >= kStagedMinLogN)
       k32_polymul_pair_staged<LOGN><<<g, P::THREADS, StagedCfg32<LOGN>::kSmem, st>>>(c, a, b, ls, mods);
     else k32_polymul_pair<PC><<<g, P::THREADS, PC::kSmem, st>>>(c, a, b, ls, mods);
