@@ -30,6 +30,7 @@
 //            FastGaussianNoise.hpp) inverts a wider random number against
 //            the same cumulative distribution through lookup tables; the two
 //            agree in distribution (per value within 2^-63), not draw for draw.
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -174,21 +175,22 @@ __global__ void k_hwt_init(uint32_t* hitted, HwtCtl* ctl, uint32_t count, uint32
 // poly was rejected, which makes every draw independent: the last k that hits
 // a reservoir slot owns it (atomicMax over the initial slot index).  A
 // rejection (probability below k / 2^64) shifts every later draw; it is
-// recorded, and the poly is redone in draw order by k_hwt_rank.
-__global__ void k_hwt_reservoir(uint32_t* hitted, HwtCtl* ctl, uint32_t count, uint32_t log_n, uint32_t h,
-                                uint64_t seed) {
-  const uint64_t per = (1ull << log_n) - h;
-  const uint64_t total = per * count;
-  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t j = t / per, d = t - j * per;
-    const uint32_t k = h + (uint32_t)d;
-    const uint64_t w = rand_word(rand_word(seed, j), d);
-    if (w > accept_limit(k)) {
+// recorded, and the poly is redone in draw order by k_hwt_rank.  Poly j is
+// grid row j; the acceptance limit floor((2^64 - 1) / k) * k is at least
+// 2^64 - k, so only a draw above that needs the division.
+__global__ void k_hwt_reservoir(uint32_t* hitted, HwtCtl* ctl, uint32_t log_n, uint32_t h, uint64_t seed) {
+  const uint32_t per = (1u << log_n) - h;
+  const uint32_t j = blockIdx.y;
+  const uint64_t s = rand_word(seed, j);
+  for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < per; d += gridDim.x * blockDim.x) {
+    const uint32_t k = h + d;
+    const uint64_t w = rand_word(s, d);
+    if (w > 0ull - (uint64_t)k && w > accept_limit(k)) {
       atomicMin(&ctl[j].first_reject, k);
       continue;
     }
     const uint32_t pos = (uint32_t)(w % k);
-    if (pos < h) atomicMax(&hitted[j * h + pos], k);
+    if (pos < h) atomicMax(&hitted[(size_t)j * h + pos], k);
   }
 }
 
@@ -511,7 +513,16 @@ int yell_dev_sample_hwt(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t lo
   if (e == cudaSuccess) {
     LaunchScope ps("sample_hwt", a.st);
     k_hwt_init<<<grid_for((size_t)count * h), 256, 0, a.st>>>(hitted, ctl, count, h, n);
-    if (n > h) k_hwt_reservoir<<<grid_for((size_t)count * (n - h)), 256, 0, a.st>>>(hitted, ctl, count, log_n, h, seed);
+    if (n > h) {
+      // grid rows = polys (at most 65535 per launch); columns cover a poly's draws
+      const uint32_t cols = (uint32_t)std::min<size_t>(((size_t)(n - h) + 255) / 256, 152u * 16u);
+      for (uint32_t j0 = 0; j0 < count; j0 += 65535u) {
+        const uint32_t rows = std::min(count - j0, 65535u);
+        // rand_word(seed, j0 + j) = rand_word(seed + j0 * gamma, j)
+        k_hwt_reservoir<<<dim3(cols, rows), 256, 0, a.st>>>(hitted + (size_t)j0 * h, ctl + j0, log_n, h,
+                                                             seed + (uint64_t)j0 * 0x9E3779B97F4A7C15ull);
+      }
+    }
     k_hwt_rank<<<count, kRankThreads, smem, a.st>>>(hitted, ctl, bits, prefix, log_n, h, seed, sequential);
     k_hwt_write<<<grid_for(((size_t)count << log_n) >> 1), 256, 0, a.st>>>(d_out, count, L, log_n, cm0, a.mods, seed,
                                                                            h, ctl, bits, prefix);
