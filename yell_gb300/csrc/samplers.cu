@@ -75,6 +75,25 @@ __global__ void k_sample_uniform(uint64_t* out, uint32_t count, uint32_t L, uint
   const size_t c0 = warp * per, c1 = min(c0 + per, chunks);
   size_t row = ~(size_t)0;
   uint64_t p = 0, mask = 0;
+  if (log_n >= 7) {
+    // A chunk lies inside one limb and the total is a multiple of 128 words:
+    // no bound check, one limb check and one counter product per chunk.
+    constexpr uint64_t kGamma = 0x9E3779B97F4A7C15ull;
+    for (size_t ch = c0; ch < c1; ++ch) {
+      const size_t k = (ch << 7) + (lane << 1);
+      if ((k >> log_n) != row) {
+        row = k >> log_n;
+        p = __ldg(&mods[cm0 + (uint32_t)(row % L)].p);
+        mask = (2ull << (63 - __clzll(p))) - 1ull;  // 2^(floor(log2 p) + 1) - 1
+      }
+      const uint64_t z = seed + (k + 1) * kGamma;  // counter of word k; + gamma per word
+      const uint64_t v0 = csub(mix64(z) & mask, p), v1 = csub(mix64(z + kGamma) & mask, p);
+      const uint64_t v2 = csub(mix64(z + 64 * kGamma) & mask, p), v3 = csub(mix64(z + 65 * kGamma) & mask, p);
+      *reinterpret_cast<ulonglong2*>(out + k) = make_ulonglong2(v0, v1);
+      *reinterpret_cast<ulonglong2*>(out + k + 64) = make_ulonglong2(v2, v3);
+    }
+    return;
+  }
   for (size_t ch = c0; ch < c1; ++ch) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
