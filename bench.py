@@ -625,10 +625,18 @@ def run_rows(torch, y, stream, dc, reps: int = 10, groups: int = 3):
         "gaussian": lambda: y.sample_gaussian(buf, PAIRS, L, LOG_N, seed=3, stream=stream),
         "hwt_192": lambda: y.sample_hwt(buf, PAIRS, L, LOG_N, 192, seed=4, stream=stream),
     }
+    # what a write-only kernel reaches here: a device fill of the same bytes (a library kernel,
+    # timed as the reference point of the samplers, not as work of this library)
+    with torch.cuda.stream(stream):
+        fill_ms = timed(lambda: buf.fill_(1))
+    fill_gbs = 8 * words / (fill_ms * 1e-3) / 1e9
+    out["device_fill"] = {"ms": fill_ms, "achieved_gbs": fill_gbs, "frac": fill_gbs / hbm,
+                          "bytes": 8 * words, "what": "torch fill_ of the sampler buffer (write-only ceiling)"}
     for name, fn in samplers.items():
         ms = timed(fn)
         gbs = 8 * words / (ms * 1e-3) / 1e9
         out[f"sample_{name}"] = {"ms": ms, "achieved_gbs": gbs, "frac": gbs / hbm,
+                                 "frac_of_device_fill": fill_ms / ms,
                                  "algorithmic_bytes": 8 * words, "bound": "hbm (writes)"}
     del buf
     # CRT lifting of the polymul output (16 polys, L = 32 -> W words per coefficient)
