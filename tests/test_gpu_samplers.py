@@ -17,8 +17,8 @@ def _host(t, count, L, log_n):
     return t.cpu().numpy().view(np.uint64).reshape(count, L, 1 << log_n)
 
 
-@pytest.mark.parametrize("count,L,log_n,cm0,seed", [(1, 1, 3, 0, 0), (2, 3, 10, 7, 1), (3, 4, 13, 0, 99),
-                                                    (1, 2, 17, 500, 5)])
+@pytest.mark.parametrize("count,L,log_n,cm0,seed", [(1, 1, 3, 0, 0), (2, 3, 6, 0, 3), (5, 1, 7, 11, 4),
+                                                    (2, 3, 10, 7, 1), (3, 4, 13, 0, 99), (1, 2, 17, 500, 5)])
 def test_uniform_matches_oracle(cuda, orc, count, L, log_n, cm0, seed):
     t = _empty(cuda, count, L, log_n)
     y.sample_uniform(t, count, L, log_n, cm0, seed=seed)
