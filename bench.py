@@ -759,7 +759,7 @@ def run_serving(torch, y, uneven, duration_s: float):
                                  ("per_call", 1, min(duration_s, 0.25))):
         points = []
         with Server(hbm_budget_bytes=0, max_inflight=4, max_batch=max_batch) as srv:
-            srv.load_test(templates, 0.1 * peak_rps, 0.05, seed=1)  # warm-up
+            srv.load_test(templates, 0.1 * peak_rps, 0.25, seed=1)  # warm-up
             for f in loads:
                 st = srv.load_test(templates, f * peak_rps, dur, seed=5)
                 points.append({"load": f, "offered_rps": f * peak_rps,
