@@ -449,6 +449,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
         uneven.pop("_mix")
 
     rows = None if args.no_rows else run_rows(torch, y, stream, dc)
+    config2 = None if args.no_rows else run_config2(torch, y, stream)
 
     # ---- end to end through the host-memory C ABI call --------------------
     pa = y.PinnedBuffer(a.shape)
@@ -532,6 +533,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> int:
             "batched_vs_per_call": value / per_call_value,
             "uneven_batch": uneven,
             "serving": serving,
+            "batched_ntt": config2,
             "rows": rows,
         }
         print(json.dumps(line), flush=True)
@@ -589,6 +591,68 @@ def run_e2e_facade(y, a, b, want, steps: int = 2) -> dict:
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": steps,
             "path": "yell_poly_forward x2, yell_poly_mulmod, yell_poly_backward per pair on per-limb "
                     "pageable host allocations (the reference's poly<N> layout and call pattern)"}
+
+
+def run_config2(torch, y, stream, reps: int = 10, groups: int = 3):
+    """Batched NTT without a product: forward then inverse NTT of 64 polys x
+    L = 8 x N = 2^14 (P[0..7]), device-resident, one call per direction (a
+    column launch and a row launch each), against the same 1024 limb-NTTs as
+    one call per limb.  CUDA events on `stream`, the fastest of `groups`
+    averages over `reps`; the words are checked to come back unchanged."""
+    from yell_gb300.inputs import uniform_polys
+
+    log_n, L2, polys = 14, 8, 64
+    n = 1 << log_n
+    hbm, _ = peaks()
+    x0 = uniform_polys(2, polys, L2, log_n, y.primes(L2))
+    x = torch.from_numpy(x0.view(np.int64).reshape(-1).copy()).cuda()
+    y.init_ntt_tables(log_n, L2)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(groups):
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1) / reps)
+        return best
+
+    fwd = lambda: y.dev_ntt(x, polys, L2, log_n, 0, y.YELL_FORWARD, stream=stream)
+    inv = lambda: y.dev_ntt(x, polys, L2, log_n, 0, y.YELL_BACKWARD, stream=stream)
+    fwd_ms, inv_ms = timed(fwd), timed(inv)
+    both_ms = timed(lambda: (fwd(), inv()))
+    ok = bool(np.array_equal(x.cpu().numpy().view(np.uint64).reshape(x0.shape), x0))
+    limbs = [x[i * n:(i + 1) * n] for i in range(polys * L2)]
+
+    def per_call():
+        for i, v in enumerate(limbs):
+            y.dev_ntt(v, 1, 1, log_n, i % L2, y.YELL_FORWARD, stream=stream)
+        for i, v in enumerate(limbs):
+            y.dev_ntt(v, 1, 1, log_n, i % L2, y.YELL_BACKWARD, stream=stream)
+
+    pc_ms = timed(per_call)
+    limb_ntts = 2 * polys * L2
+    half = polys * L2 * (n // 2) * log_n  # butterflies of one direction over the batch
+    ct, gs = y.calibrate_butterflies()
+    out = {"workload": f"forward + inverse NTT, N=2^{log_n}, L={L2} (P[0..{L2 - 1}]), {polys} polys",
+           "value": limb_ntts / (both_ms * 1e-3), "unit": UNIT, "ms_per_batch": both_ms,
+           "forward_ms": fwd_ms, "inverse_ms": inv_ms, "round_trip_identity": ok,
+           "roofline": {"bound": "hbm", "algorithmic_bytes": 16 * n * limb_ntts,
+                        "achieved_gbs": 16 * n * limb_ntts / (both_ms * 1e-3) / 1e9,
+                        "frac": 16 * n * limb_ntts / (both_ms * 1e-3) / 1e9 / hbm},
+           "integer": {"forward_frac": integer_ceiling_s(half, 0, ct, gs) / (fwd_ms * 1e-3),
+                       "inverse_frac": integer_ceiling_s(0, half, ct, gs) / (inv_ms * 1e-3),
+                       "formula": "frac = (n_ct / ct_rate + n_gs / gs_rate) / measured time"},
+           "per_call": {"value": limb_ntts / (pc_ms * 1e-3), "unit": UNIT, "ms_per_batch": pc_ms,
+                        "path": "one yell_dev_ntt call per limb and direction (1024 launches)"},
+           "batched_vs_per_call": pc_ms / both_ms}
+    return out
 
 
 def run_rows(torch, y, stream, dc, reps: int = 10, groups: int = 3):
