@@ -545,7 +545,7 @@ int yell_dev_sample_hwt(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t lo
     k_hwt_rank<<<count, kRankThreads, smem, a.st>>>(hitted, ctl, bits, prefix, log_n, h, seed, sequential);
     k_hwt_write<<<grid_for(((size_t)count << log_n) >> 1), 256, 0, a.st>>>(d_out, count, L, log_n, cm0, a.mods, seed,
                                                                            h, ctl, bits, prefix);
-    g_kernel_launches += n > h ? 4 : 3;
+    g_kernel_launches += 3 + (n > h ? (count + 65534u) / 65535u : 0u);
     e = cudaGetLastError();
   }
   const int fs = a.ctx->scratch_free_async(scratch, a.st);
