@@ -350,7 +350,7 @@ int BatchExecutor::run_queue(DeviceContext* ctx, const yell_polymul_desc* descs,
     q.a = ConstLimbSet{nullptr, reinterpret_cast<const uint64_t* const*>(d_lists_ + b.a_off), cms, b.limbs, 1, 0, 0};
     q.b = ConstLimbSet{nullptr, reinterpret_cast<const uint64_t* const*>(d_lists_ + b.b_off), cms, b.limbs, 1, 0, 0};
     q.s = LimbSet{nullptr, reinterpret_cast<uint64_t* const*>(d_lists_ + b.s_off), cms, b.limbs, 1, 0, 0};
-    q.mods = b.mods;
+    q.mods = b.mods + kPolymulConsts;  // the fused polymul's copy of the constants
     q.log_n = b.log_n;
     q.counter_off = counter_off[bi];
     qb[bi] = q;
@@ -423,7 +423,7 @@ int BatchExecutor::queue_wait_check(DeviceContext* ctx, cudaStream_t s, uint64_t
   q.a = ConstLimbSet{nullptr, reinterpret_cast<const uint64_t* const*>(d_lists_ + 8), cms, 1, 1, 0, 0};
   q.b = q.a;
   q.s = LimbSet{nullptr, reinterpret_cast<uint64_t* const*>(d_lists_ + 16), cms, 1, 1, 0, 0};
-  q.mods = mods;
+  q.mods = mods + kPolymulConsts;
   q.log_n = log_n;
   q.counter_off = 0;
   std::memcpy(h_lists_ + 64, &q, sizeof q);

@@ -210,6 +210,18 @@ __device__ __forceinline__ uint64_t mulmod_barrett(uint64_t x, uint64_t y, uint6
   return barrett128(__umul64hi(x, y), x * y, p, pn);
 }
 
+// Montgomery product x*y*2^-64 mod p, lazily in [0, 2p), for x, y < 2p:
+// t = (x*y + m*p) / 2^64 with m = lo64(x*y) * (-p^-1) mod 2^64.  The low words
+// of x*y and m*p sum to 0 or 2^64, so their carry is (lo64(x*y) != 0); and
+// t < (4p^2 + 2^64 p) / 2^64 < 2p since 4p < 2^64.  Used for the fused
+// polymul's product, where only the final fully reduced words are observable
+// and the 2^-64 is cancelled by the inverse's scaling constant.
+__device__ __forceinline__ uint64_t mont_mul(uint64_t x, uint64_t y, uint64_t p, uint64_t neg_pinv) {
+  const uint64_t lo = x * y, hi = __umul64hi(x, y);
+  const uint64_t m = lo * neg_pinv;
+  return hi + __umul64hi(m, p) + (lo != 0 ? 1ull : 0ull);
+}
+
 // ops::muladd, include/yell/ops.hpp:144-158: barrett(x*y + rop).
 __device__ __forceinline__ uint64_t muladd_barrett(uint64_t rop, uint64_t x, uint64_t y, uint64_t p,
                                                    uint64_t pn) {

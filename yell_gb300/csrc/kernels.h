@@ -20,6 +20,13 @@ struct NttShape {
 constexpr uint32_t kMinLogN = 3;
 constexpr uint32_t kMaxLogN = 20;
 
+// Each degree's DevMod array holds two copies per modulus: [cm] for the
+// transforms and element-wise ops, [kPolymulConsts + cm] for the fused
+// polymul, whose product is a Montgomery product (pn holds -p^-1 mod 2^64)
+// and whose inverse scales by N^-1 * 2^64 (inv_n, inv_n_iphi and their Shoup
+// forms) to cancel the product's 2^-64.  Equal to kMaxModuli.
+constexpr uint32_t kPolymulConsts = 1000;
+
 // Kernel launches made by this library (for the caller's accounting).
 extern std::atomic<uint64_t> g_kernel_launches;
 

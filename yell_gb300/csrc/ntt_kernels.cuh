@@ -502,9 +502,9 @@ __device__ __forceinline__ void fused_product(uint64_t* xa, uint64_t* xb, uint32
   // the inverse round's first twiddles load while the products compute
   ulonglong2 wg[GsFirst<RB, INV_LAST>::N0];
   GsFirst<RB, INV_LAST>::load(wg, m.inv, log_n, 0, gr);
+  // m is the polymul copy of the constants: m.pn = -p^-1 mod 2^64
 #pragma unroll
-  for (int i = 0; i < E; ++i)
-    xa[i] = mulmod_barrett(fwd_correct(xa[i], p, p2), fwd_correct(xb[i], p, p2), p, m.pn);
+  for (int i = 0; i < E; ++i) xa[i] = mont_mul(csub(xa[i], p2), csub(xb[i], p2), p, m.pn);
   gs_round_w<RB, INV_LAST>(xa, log_n, 0, gr, m, wg);
 }
 
@@ -919,6 +919,7 @@ cudaError_t launch_whole_ntt(const LimbSet& ls, const DevMod* mods, NttDir dir, 
 template <int LOGN, int T>
 cudaError_t launch_whole_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
                                  const DevMod* mods, uint64_t*, uint64_t* const*, cudaStream_t st) {
+  mods += kPolymulConsts;  // the fused polymul's copy of the constants
   using C = WholeCfg<LOGN, T>;
   const uint32_t per = 1u << (T - LOGN);
   const uint32_t grid = (c.count + per - 1) / per;
@@ -970,6 +971,7 @@ template <int LOGN, int K1, int LC = 4, int LR = 4>
 cudaError_t launch_two_pass_polymul(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
                                     const DevMod* mods, uint64_t* scratch, uint64_t* const* scratch_ptrs,
                                     cudaStream_t st) {
+  mods += kPolymulConsts;  // the fused polymul's copy of the constants
   constexpr int LOGB = LOGN - K1;
   using CC = ColCfg<LOGN, K1, LC>;
   using RC = RowCfg<LOGN, K1, LR>;
@@ -1026,6 +1028,7 @@ template <int LOGN, int K1, int LC = 4, int LR = 4>
 cudaError_t launch_two_pass_polymul_pipe(const LimbSet& c, const ConstLimbSet& a, const ConstLimbSet& b,
                                          const DevMod* mods, uint64_t* scratch, uint64_t* const* scratch_ptrs,
                                          cudaStream_t st) {
+  mods += kPolymulConsts;  // the fused polymul's copy of the constants
   constexpr int LOGB = LOGN - K1;
   using CC = ColCfg<LOGN, K1, LC>;
   using RC = RowCfg<LOGN, K1, LR>;

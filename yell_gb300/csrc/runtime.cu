@@ -41,6 +41,13 @@ uint64_t powmod(uint64_t b, uint64_t e, uint64_t p) {
 // floor(x * 2^64 / p), lib/ops.cpp:23-27.
 inline uint64_t shoupify(uint64_t x, uint64_t p) { return (uint64_t)(((u128)x << 64) / p); }
 
+// -p^-1 mod 2^64 for odd p (Newton's iteration doubles the correct low bits).
+inline uint64_t neg_inv_mod_2_64(uint64_t p) {
+  uint64_t x = p;  // p * p = 1 mod 8
+  for (int i = 0; i < 5; ++i) x *= 2 - p * x;
+  return 0 - x;
+}
+
 inline uint32_t bit_reverse(uint32_t x, uint32_t bits) {
   uint32_t r = 0;
   for (uint32_t i = 0; i < bits; ++i) r |= ((x >> i) & 1u) << (bits - 1 - i);
@@ -294,13 +301,14 @@ int DeviceContext::ensure_tables_list(uint32_t log_n, const uint32_t* cms, uint3
   const int nst = noalloc_prepare(device_);
   if (nst != kOk) return nst;
   cudaError_t e;
+  static_assert(kPolymulConsts == kMaxModuli, "the polymul constants follow the transforms'");
   if (!d_mods_[log_n]) {
-    e = lib_malloc(&d_mods_[log_n], kMaxModuli * sizeof(DevMod));
+    e = lib_malloc(&d_mods_[log_n], 2 * kMaxModuli * sizeof(DevMod));
     if (e != cudaSuccess) {
       d_mods_[log_n] = nullptr;
       return fail_cuda(e, "cudaMalloc(DevMod table)");
     }
-    e = cudaMemset(d_mods_[log_n], 0, kMaxModuli * sizeof(DevMod));
+    e = cudaMemset(d_mods_[log_n], 0, 2 * kMaxModuli * sizeof(DevMod));
     if (e != cudaSuccess) return fail_cuda(e, "cudaMemset(DevMod table)");
   }
   const uint32_t nwords = 1u << log_n;
@@ -349,6 +357,16 @@ int DeviceContext::ensure_tables_list(uint32_t log_n, const uint32_t* cms, uint3
     m.inv_n_iphi = sc[4 * i + 2];
     m.inv_n_iphi_s = sc[4 * i + 3];
     e = cudaMemcpy(d_mods_[log_n] + cm, &m, sizeof(DevMod), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail_cuda(e, "cudaMemcpy(DevMod)");
+    // the fused polymul's copy: Montgomery constant, inverse scaling times 2^64
+    DevMod pm = m;
+    const uint64_t r64 = (uint64_t)(((u128)1 << 64) % m.p);
+    pm.pn = neg_inv_mod_2_64(m.p);
+    pm.inv_n = mulmod_exact(m.inv_n, r64, m.p);
+    pm.inv_n_s = shoupify(pm.inv_n, m.p);
+    pm.inv_n_iphi = mulmod_exact(m.inv_n_iphi, r64, m.p);
+    pm.inv_n_iphi_s = shoupify(pm.inv_n_iphi, m.p);
+    e = cudaMemcpy(d_mods_[log_n] + kPolymulConsts + cm, &pm, sizeof(DevMod), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return fail_cuda(e, "cudaMemcpy(DevMod)");
     built[cm] = 1;
   }
