@@ -308,6 +308,16 @@ __device__ __forceinline__ uint32_t mulmod_barrett(uint32_t x, uint32_t y, uint3
   return barrett64((uint64_t)x * y, p, pn);
 }
 
+// Montgomery product x*y*2^-32 mod p, lazily in [0, 2p), for x, y < 2p and
+// 4p < 2^32: (x*y + m*p) / 2^32 with m = lo32(x*y) * (-p^-1) mod 2^32, the sum
+// exact in 64 bits (below 2^63).  The fused polymul's product; its 2^-32 is
+// cancelled by the inverse's scaling constants.
+__device__ __forceinline__ uint32_t mont_mul(uint32_t x, uint32_t y, uint32_t p, uint32_t neg_pinv) {
+  const uint64_t t = (uint64_t)x * y;
+  const uint32_t m = (uint32_t)t * neg_pinv;
+  return (uint32_t)((t + (uint64_t)m * p) >> 32);
+}
+
 __device__ __forceinline__ uint32_t muladd_barrett(uint32_t rop, uint32_t x, uint32_t y, uint32_t p,
                                                    uint32_t pn) {
   return barrett64((uint64_t)x * y + rop, p, pn);

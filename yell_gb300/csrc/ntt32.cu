@@ -159,12 +159,14 @@ int ensure32(int device, uint32_t log_n, uint32_t cm0, uint32_t L, const DevMod3
   if (built.empty()) built.assign(kMaxModuli32, 0);
   cudaError_t e;
   if (!t.mods[log_n]) {
-    e = lib_malloc(&t.mods[log_n], kMaxModuli32 * sizeof(DevMod32));
+    // [cm]: transforms and element-wise ops; [kMaxModuli32 + cm]: the fused
+    // polymul (Montgomery product, inverse scaled by N^-1 * 2^32)
+    e = lib_malloc(&t.mods[log_n], 2 * kMaxModuli32 * sizeof(DevMod32));
     if (e != cudaSuccess) {
       t.mods[log_n] = nullptr;
       return fail_cuda(e, "cudaMalloc(DevMod32 table)");
     }
-    e = cudaMemset(t.mods[log_n], 0, kMaxModuli32 * sizeof(DevMod32));
+    e = cudaMemset(t.mods[log_n], 0, 2 * kMaxModuli32 * sizeof(DevMod32));
     if (e != cudaSuccess) return fail_cuda(e, "cudaMemset(DevMod32 table)");
   }
   const uint32_t n = 1u << log_n;
@@ -194,6 +196,17 @@ int ensure32(int device, uint32_t log_n, uint32_t cm0, uint32_t L, const DevMod3
     m.inv_n_iphi = sc[2];
     m.inv_n_iphi_s = sc[3];
     e = cudaMemcpy(t.mods[log_n] + cm, &m, sizeof m, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail_cuda(e, "upload DevMod32");
+    DevMod32 pm = m;
+    uint32_t inv = m.p;  // p * p = 1 mod 8; Newton's iteration doubles the correct low bits
+    for (int i = 0; i < 4; ++i) inv *= 2u - m.p * inv;
+    const uint64_t r32 = (1ull << 32) % m.p;
+    pm.pn = 0u - inv;
+    pm.inv_n = (uint32_t)(m.inv_n * r32 % m.p);
+    pm.inv_n_s = shoupify32(pm.inv_n, m.p);
+    pm.inv_n_iphi = (uint32_t)(m.inv_n_iphi * r32 % m.p);
+    pm.inv_n_iphi_s = shoupify32(pm.inv_n_iphi, m.p);
+    e = cudaMemcpy(t.mods[log_n] + kMaxModuli32 + cm, &pm, sizeof pm, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return fail_cuda(e, "upload DevMod32");
     built[cm] = 1;
   }
@@ -304,8 +317,7 @@ __global__ void __launch_bounds__(C::THREADS, 1024 / C::THREADS) k32_polymul(uin
 #pragma unroll
     for (int i = 0; i < E; i += 4)
       *reinterpret_cast<uint4*>(park + i) =
-          make_uint4(fwd_correct(x[i], p, p2), fwd_correct(x[i + 1], p, p2), fwd_correct(x[i + 2], p, p2),
-                     fwd_correct(x[i + 3], p, p2));
+          make_uint4(csub(x[i], p2), csub(x[i + 1], p2), csub(x[i + 2], p2), csub(x[i + 3], p2));
   }
   __syncthreads();
   // NTT(b), product, inverse
@@ -318,10 +330,10 @@ __global__ void __launch_bounds__(C::THREADS, 1024 / C::THREADS) k32_polymul(uin
 #pragma unroll
     for (int i = 0; i < E; i += 4) {
       const uint4 ah = *reinterpret_cast<const uint4*>(park + i);  // written above by this thread
-      x[i] = mulmod_barrett(ah.x, fwd_correct(x[i], p, p2), p, m.pn);
-      x[i + 1] = mulmod_barrett(ah.y, fwd_correct(x[i + 1], p, p2), p, m.pn);
-      x[i + 2] = mulmod_barrett(ah.z, fwd_correct(x[i + 2], p, p2), p, m.pn);
-      x[i + 3] = mulmod_barrett(ah.w, fwd_correct(x[i + 3], p, p2), p, m.pn);
+      x[i] = mont_mul(ah.x, csub(x[i], p2), p, m.pn);
+      x[i + 1] = mont_mul(ah.y, csub(x[i + 1], p2), p, m.pn);
+      x[i + 2] = mont_mul(ah.z, csub(x[i + 2], p2), p, m.pn);
+      x[i + 3] = mont_mul(ah.w, csub(x[i + 3], p2), p, m.pn);
     }
     gs_round<RB, NR == 1>(x, (uint32_t)C::K, (uint32_t)RB::BETA, RB::gr(bb, 0), m);
     smem_store<RB>(x, smem32, bb);
@@ -519,17 +531,17 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PC::C::THREADS, PC::
   pair_forward<PC>(x, a + lbase, smem32, tid, r, m, w1);
 #pragma unroll
   for (int i = 0; i < E; i += 4)
-    *reinterpret_cast<uint4*>(park + i) = make_uint4(fwd_correct(x[i], p, p2), fwd_correct(x[i + 1], p, p2),
-                                                     fwd_correct(x[i + 2], p, p2), fwd_correct(x[i + 3], p, p2));
+    *reinterpret_cast<uint4*>(park + i) =
+        make_uint4(csub(x[i], p2), csub(x[i + 1], p2), csub(x[i + 2], p2), csub(x[i + 3], p2));
   __syncthreads();  // the buffer is reused for b
   pair_forward<PC>(x, b + lbase, smem32, tid, r, m, w1);
 #pragma unroll
   for (int i = 0; i < E; i += 4) {
     const uint4 ah = *reinterpret_cast<const uint4*>(park + i);  // written above by this thread
-    x[i] = mulmod_barrett(ah.x, fwd_correct(x[i], p, p2), p, m.pn);
-    x[i + 1] = mulmod_barrett(ah.y, fwd_correct(x[i + 1], p, p2), p, m.pn);
-    x[i + 2] = mulmod_barrett(ah.z, fwd_correct(x[i + 2], p, p2), p, m.pn);
-    x[i + 3] = mulmod_barrett(ah.w, fwd_correct(x[i + 3], p, p2), p, m.pn);
+    x[i] = mont_mul(ah.x, csub(x[i], p2), p, m.pn);
+    x[i + 1] = mont_mul(ah.y, csub(x[i + 1], p2), p, m.pn);
+    x[i + 2] = mont_mul(ah.z, csub(x[i + 2], p2), p, m.pn);
+    x[i + 3] = mont_mul(ah.w, csub(x[i + 3], p2), p, m.pn);
   }
   pair_inverse<PC>(x, smem32, tid, r, bb, m);
   cluster.sync();
@@ -678,9 +690,9 @@ __global__ void __cluster_dims__(2, 1, 1)
   }
   uint32_t x[E];
   pair_forward_rounds<PC>(x, W, tid, r, m);
-  // park a's reduced words where its bottom round read them (only this thread's positions)
+  // park a's words (in [0, 2p)) where its bottom round read them (only this thread's positions)
 #pragma unroll
-  for (int i = 0; i < E; ++i) x[i] = fwd_correct(x[i], p, p2);
+  for (int i = 0; i < E; ++i) x[i] = csub(x[i], p2);
   smem_store<RB>(x, W, bb);
   mbar_wait32(mbar, 1);
   stage0_from_smem<PC, true>(S, S, S + half, tid, r, p, w1);
@@ -690,10 +702,10 @@ __global__ void __cluster_dims__(2, 1, 1)
 #pragma unroll
     for (int i = 0; i < E; i += 4) {
       const uint4 ah = *reinterpret_cast<const uint4*>(W + (ib ^ (uint32_t)i));
-      x[i] = mulmod_barrett(ah.x, fwd_correct(x[i], p, p2), p, m.pn);
-      x[i + 1] = mulmod_barrett(ah.y, fwd_correct(x[i + 1], p, p2), p, m.pn);
-      x[i + 2] = mulmod_barrett(ah.z, fwd_correct(x[i + 2], p, p2), p, m.pn);
-      x[i + 3] = mulmod_barrett(ah.w, fwd_correct(x[i + 3], p, p2), p, m.pn);
+      x[i] = mont_mul(ah.x, csub(x[i], p2), p, m.pn);
+      x[i + 1] = mont_mul(ah.y, csub(x[i + 1], p2), p, m.pn);
+      x[i + 2] = mont_mul(ah.z, csub(x[i + 2], p2), p, m.pn);
+      x[i + 3] = mont_mul(ah.w, csub(x[i + 3], p2), p, m.pn);
     }
   }
   pair_inverse<PC>(x, S, tid, r, bb, m);
@@ -809,6 +821,7 @@ cudaError_t launch32(int kind, uint32_t* c, const uint32_t* a, const uint32_t* b
   using CF = Cfg32<LOGN>;
   using C = typename CF::C;
   const uint32_t blocks = (ls.count + (1u << (C::T - LOGN)) - 1) >> (C::T - LOGN);
+  if (kind == 3) mods += kMaxModuli32;  // the fused polymul's copy of the constants
   if constexpr (LOGN >= kMinPairLogN) {
     using PC = PairCfg32<LOGN>;
     using P = typename PC::C;
