@@ -2,7 +2,7 @@
 """Benchmark of the batched fused polymul (N = 2^16, L = 32, 16 pairs).
 
 One step = one fused polymul over the whole batch: for each of the 16 pairs
-and each of the 32 RNS limbs, NTT(a), NTT(b), Barrett product, INTT = 3
+and each of the 32 RNS limbs, NTT(a), NTT(b), pointwise product, INTT = 3
 limb-NTTs per limb, 1536 limb-NTTs per step.  A is uniform, B a centred
 discrete Gaussian (sigma 3.2, |e| <= 19) mapped per limb, both from
 splitmix64 seeds.  Each step touches 768 MiB of operands and results plus
@@ -737,7 +737,7 @@ def run_rows(torch, y, stream, dc, reps: int = 10, groups: int = 3):
                                     "frac": floor_s / (ms * 1e-3),
                                     "formula": "frac = (n_ct / ct_rate + n_gs / gs_rate) / measured time",
                                     "note": "ceiling = register-only 32-bit CT/GS butterflies "
-                                            "(yell32_calibrate_butterflies); Barrett products not counted"}}
+                                            "(yell32_calibrate_butterflies); pointwise products not counted"}}
     return out
 
 
@@ -849,9 +849,10 @@ def integer_roofline(y, kernels: dict, ms_per_step: float, pairs: int, variant_n
     the register-only ceiling (yell_calibrate_butterflies).  Stage counts
     follow the launch variant: k1 column stages, log N - k1 row stages; the
     forward NTTs of a and b are CT butterflies, the inverse GS (its scaled last
-    layer counted as one GS stage).  The Barrett products (N L pairs of them)
-    and the final reductions are not counted, so each fraction understates the
-    kernel's use of the multiplier slightly."""
+    layer counted as one GS stage).  The pointwise products (N L pairs of them,
+    Montgomery products in the fused kernels) and the final reductions are not
+    counted, so each fraction understates the kernel's use of the multiplier
+    slightly."""
     import re
 
     ct_rate, gs_rate = y.calibrate_butterflies()
@@ -862,7 +863,7 @@ def integer_roofline(y, kernels: dict, ms_per_step: float, pairs: int, variant_n
            "ceiling_ct_bfly_per_s": ct_rate, "ceiling_gs_bfly_per_s": gs_rate,
            "formula": "frac = (n_ct / ct_rate + n_gs / gs_rate) / measured time",
            "variant": variant_name, "k1": k1,
-           "note": "ceiling = register-only CT/GS butterflies on every SM; Barrett products not counted"}
+           "note": "ceiling = register-only CT/GS butterflies on every SM; the pointwise products not counted"}
     n_ct, n_gs = 2 * half * LOG_N, half * LOG_N
     out["pipeline_bfly_per_s"] = (n_ct + n_gs) / (ms_per_step * 1e-3)
     out["pipeline_frac"] = integer_ceiling_s(n_ct, n_gs, ct_rate, gs_rate) / (ms_per_step * 1e-3)
