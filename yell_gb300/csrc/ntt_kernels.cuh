@@ -9,7 +9,7 @@
 //     B); the row pass applies stages k1..log_n-1, which stay inside
 //     contiguous blocks of B words.  The inverse runs the same passes in the
 //     opposite order; its column pass ends with the scaled last layer.
-//   * fused polymul: NTT(a), NTT(b), Barrett product and INTT in one kernel
+//   * fused polymul: NTT(a), NTT(b), pointwise product and INTT in one kernel
 //     (whole-limb) or three (two-pass: column pass of a and of b, one row
 //     kernel doing forward rows of both, the product and inverse rows, then
 //     the inverse column pass).  The last forward round of both operands,
@@ -479,8 +479,13 @@ __global__ void __launch_bounds__(C::THREADS) k_row_pass(LimbSet ls, const DevMo
 // ===========================================================================
 // Fused product round shared by both polymul kernels: the bottom forward
 // round (R = LOGE at bit 0) of both operands with shared twiddles, the
-// reduction of ntt<N>::forward, the Barrett product of ops::mulmod and the
-// bottom inverse round, on one register set.
+// pointwise product and the bottom inverse round, on one register set.  The
+// product is a Montgomery product of the lazy forward words (one conditional
+// subtraction each instead of ntt<N>::forward's reduction and the Barrett
+// reduction of ops::mulmod): x*y*2^-64 in [0, 2p), congruent to the
+// reference's product times 2^-64, which the inverse's scaling constants
+// (N^-1 * 2^64, the polymul copy of the constants) cancel, so the output
+// words equal the reference's.
 // ===========================================================================
 // First twiddle of the fused product round (its forward top sub-stage), for
 // callers that request it a round ahead.
