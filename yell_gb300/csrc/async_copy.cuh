@@ -1,9 +1,7 @@
-// Asynchronous copies into shared memory for sm_103a: bulk and 2-D tensor-map
-// copies whose completion is counted on an mbarrier, and bounded waits on
-// that mbarrier.
+// Asynchronous copies into shared memory for sm_103a: bulk copies whose
+// completion is counted on an mbarrier, and bounded waits on that mbarrier.
 #pragma once
 #include <cstdint>
-#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace yell_gb300 {
@@ -36,19 +34,6 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
   const uint32_t b = (uint32_t)__cvta_generic_to_shared(mbar);
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                ::"r"(d), "l"(src), "r"(bytes), "r"(b) : "memory");
-}
-
-// 2-D tensor-map tile load: box at element coordinates (x, y) -> dst (dense,
-// the box's inner dimension fastest).  x times the element size must be a
-// multiple of 16 bytes.
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tmap, int32_t x, int32_t y,
-                                            uint64_t* mbar) {
-  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
-  const uint32_t b = (uint32_t)__cvta_generic_to_shared(mbar);
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-      ::"r"(d), "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(b)
-      : "memory");
 }
 
 // Waits for phase `parity` of the mbarrier for at most timeout_ns of the
