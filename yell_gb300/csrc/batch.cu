@@ -93,6 +93,7 @@ int BatchExecutor::reserve_limbs(size_t limbs) {
 
 cudaError_t BatchExecutor::launch_buckets(const std::vector<Bucket>& buckets, cudaStream_t s,
                                           bool scratch_lists, bool fork) {
+  PlainLaunches plain;  // buckets run side by side
   fork = fork && buckets.size() > 1;
   cudaError_t le = fork ? cudaEventRecord(fork_, s) : cudaSuccess;
   for (size_t i = 0; i < buckets.size() && le == cudaSuccess; ++i) {

@@ -71,11 +71,15 @@ struct PhaseParams {
 };
 static_assert(sizeof(PhaseParams) <= 4000, "kernel parameter size");
 
-// Item first + blockIdx.x of the queue.
+// Item first + blockIdx.x of the queue.  Phases 1 and 2 are launched as
+// programmatic dependents of the phase before: their CTAs may start while its
+// last CTAs run, and wait for it before reading its words.
 template <int PHASE>
 __global__ void __launch_bounds__(kPhaseThreads, PHASE == 2 ? 4 : 2)
     k_batch_phase(const __grid_constant__ PhaseParams P, const QueueItem* __restrict__ items, uint32_t first) {
+  grid_dep_launch();
   const QueueItem it = items[first + blockIdx.x];
+  if constexpr (PHASE > 0) grid_dep_wait();
   dispatch_phase<PHASE>(P.b[it.bucket_kind >> 8], it.bid);
 }
 
@@ -102,8 +106,8 @@ cudaError_t launch_batch_phases(const QueueBucket* host_buckets, uint32_t n_buck
     if (counts[ph] != 0) {
       LaunchScope ps(names[ph], s);
       if (ph == 0) k_batch_phase<0><<<counts[0], kPhaseThreads, 2 * kTileSmemBytes, s>>>(P, items, first);
-      else if (ph == 1) k_batch_phase<1><<<counts[1], kPhaseThreads, 2 * kTileSmemBytes, s>>>(P, items, first);
-      else k_batch_phase<2><<<counts[2], kPhaseThreads, kTileSmemBytes, s>>>(P, items, first);
+      else if (ph == 1) launch_dependent(k_batch_phase<1>, counts[1], kPhaseThreads, 2 * kTileSmemBytes, s, P, items, first);
+      else launch_dependent(k_batch_phase<2>, counts[2], kPhaseThreads, kTileSmemBytes, s, P, items, first);
       g_kernel_launches += 1;
       const cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) return e;

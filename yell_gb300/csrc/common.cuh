@@ -337,4 +337,17 @@ template <> struct PairOf<uint32_t> {
   __device__ static __forceinline__ type make(uint32_t a, uint32_t b) { return make_uint2(a, b); }
 };
 
+// ---------------------------------------------------------------------------
+// Programmatic dependent launch.  The kernels of a two-pass transform are
+// launched with programmatic stream serialization: their CTAs may become
+// resident while the stream's previous kernel still runs its last CTAs, and
+// grid_dep_wait() returns once that kernel has completed with its writes
+// visible (at once for a kernel launched without the attribute, or when the
+// stream's previous work is not a kernel).  grid_dep_launch() at the start of
+// a CTA lets the stream's next kernel begin launching once every CTA of this
+// one has started.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 }  // namespace yell_gb300

@@ -30,6 +30,21 @@ constexpr uint32_t kPolymulConsts = 1000;
 // Kernel launches made by this library (for the caller's accounting).
 extern std::atomic<uint64_t> g_kernel_launches;
 
+// Whether this thread's two-pass launches run as programmatic dependents of
+// the stream's previous kernel (their CTAs become resident during its last
+// wave and wait there).  PlainLaunches clears it for a scope whose kernels
+// share the device with other streams' work (a batch's buckets on forked
+// streams, the server's batches in flight), where a waiting CTA would hold an
+// SM slot that another stream's kernel could use.
+extern thread_local bool g_dependent_launches;
+struct PlainLaunches {
+  bool saved;
+  PlainLaunches() : saved(g_dependent_launches) { g_dependent_launches = false; }
+  ~PlainLaunches() { g_dependent_launches = saved; }
+  PlainLaunches(const PlainLaunches&) = delete;
+  PlainLaunches& operator=(const PlainLaunches&) = delete;
+};
+
 // Device and pinned-host allocations made by this library.  Every allocation
 // goes through these wrappers, so the count covers all of them.
 extern std::atomic<uint64_t> g_allocations;

@@ -386,6 +386,7 @@ __global__ void __launch_bounds__(C::THREADS, min_blocks(INV ? 1024 : 768, C::TH
   constexpr int K = C::K, LB = C::LB, NR = C::NR;
   constexpr uint32_t log_n = K + LOGB;
   constexpr int TPL = LOGB - LB;  // log2(tiles per limb)
+  grid_dep_launch();
   const uint32_t tid = threadIdx.x;
   const uint32_t limb = dst.ordered(blockIdx.x >> TPL);
   const uint32_t col0 = (blockIdx.x & ((1u << TPL) - 1u)) << LB;
@@ -393,6 +394,7 @@ __global__ void __launch_bounds__(C::THREADS, min_blocks(INV ? 1024 : 768, C::TH
   uint64_t* out = dst.limb(limb, log_n) + col0;
   const DevMod m = load_mod(mods, dst.cm(limb));
   uint64_t x[1 << C::LOGE];
+  grid_dep_wait();  // the previous pass's words, when launched as a dependent
   if constexpr (!INV) {
     using R0 = Round<C, 0>;
     const uint32_t b0 = R0::base(tid);
@@ -443,12 +445,14 @@ __global__ void __launch_bounds__(C::THREADS) k_row_pass(LimbSet ls, const DevMo
   constexpr int K = C::K, NR = C::NR;
   constexpr uint32_t log_n = K + K1;
   constexpr int TPL = log_n - kTileLog;
+  grid_dep_launch();
   const uint32_t tid = threadIdx.x;
   const uint32_t limb = ls.ordered(blockIdx.x >> TPL);
   const uint32_t off = (blockIdx.x & ((1u << TPL) - 1u)) << kTileLog;
   uint64_t* data = ls.limb(limb, log_n) + off;
   const DevMod m = load_mod(mods, ls.cm(limb));
   const uint32_t G = (off >> K) + C::sub(tid);
+  grid_dep_wait();  // the previous pass's words, when launched as a dependent
   if constexpr (!INV) {
     using R0 = Round<C, 0>;
     uint64_t x[1 << C::LOGE];
@@ -590,7 +594,7 @@ __global__ void __launch_bounds__(C::THREADS, C::THREADS <= 256 ? 2 : 1) k_polym
 // Forward column pass of both polymul operands in one CTA: each thread
 // applies the same butterflies to a's and b's words at the same positions,
 // so every twiddle load serves two butterflies.  a -> ca, b -> cb.
-template <class C, int LOGB>
+template <class C, int LOGB, bool PDL = false>
 __device__ __forceinline__ void col_pass2_body(ConstLimbSet a, ConstLimbSet b, LimbSet ca, LimbSet cb,
                                                const DevMod* __restrict__ mods, uint32_t bid) {
   extern __shared__ __align__(16) uint64_t smem[];
@@ -608,6 +612,7 @@ __device__ __forceinline__ void col_pass2_body(ConstLimbSet a, ConstLimbSet b, L
   uint64_t xa[E], xb[E];
   using R0 = Round<C, 0>;
   const uint32_t b0 = R0::base(tid);
+  if constexpr (PDL) grid_dep_wait();  // whatever the stream's previous kernel wrote
   gload_cols<R0, LOGB>(xa, a.limb(limb, log_n) + col0, b0);
   gload_cols<R0, LOGB>(xb, b.limb(limb, log_n) + col0, b0);
   ct_stages2<R0::R, R0::E>(xa, xb, m.fwd, R0::HI, R0::gr(b0, 0), np, p2);
@@ -632,12 +637,13 @@ __device__ __forceinline__ void col_pass2_body(ConstLimbSet a, ConstLimbSet b, L
 template <class C, int LOGB>
 __global__ void __launch_bounds__(C::THREADS, min_blocks(512, C::THREADS))
     k_col_pass2(ConstLimbSet a, ConstLimbSet b, LimbSet ca, LimbSet cb, const DevMod* __restrict__ mods) {
-  col_pass2_body<C, LOGB>(a, b, ca, cb, mods, blockIdx.x);
+  grid_dep_launch();
+  col_pass2_body<C, LOGB, true>(a, b, ca, cb, mods, blockIdx.x);
 }
 
 // Two-pass fused row step: ca holds a's column-pass output and receives the
 // row-pass output of the product; sbuf holds b's column-pass output.
-template <class C, int K1, bool COH = false>
+template <class C, int K1, bool COH = false, bool PDL = false>
 __device__ __forceinline__ void polymul_rows_body(LimbSet ca, ConstLimbSet sbuf, const DevMod* __restrict__ mods,
                                                   uint32_t bid) {
   extern __shared__ __align__(16) uint64_t smem[];
@@ -659,6 +665,7 @@ __device__ __forceinline__ void polymul_rows_body(LimbSet ca, ConstLimbSet sbuf,
   uint64_t xa[E], xb[E];
   using R0 = Round<C, 0>;
   const uint32_t b0 = R0::base(tid);
+  if constexpr (PDL) grid_dep_wait();  // the column pass's words
   gload_rows<R0, COH>(xa, pa, b0);
   gload_rows<R0, COH>(xb, pb, b0);
   ct_stages2<R0::R, R0::E>(xa, xb, m.fwd, K1 + R0::HI, R0::gr(b0, G), 0 - m.p, m.p << 1);
@@ -683,7 +690,8 @@ __device__ __forceinline__ void polymul_rows_body(LimbSet ca, ConstLimbSet sbuf,
 template <class C, int K1>
 __global__ void __launch_bounds__(C::THREADS, min_blocks(512, C::THREADS))
     k_polymul_rows(LimbSet ca, ConstLimbSet sbuf, const DevMod* __restrict__ mods) {
-  polymul_rows_body<C, K1>(ca, sbuf, mods, blockIdx.x);
+  grid_dep_launch();
+  polymul_rows_body<C, K1, false, true>(ca, sbuf, mods, blockIdx.x);
 }
 
 // ===========================================================================
@@ -892,6 +900,27 @@ cudaError_t set_smem(KernelT kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+// Launch as a programmatic dependent of the stream's previous kernel (unless
+// g_dependent_launches is cleared): the kernel's CTAs may start while that
+// kernel's last CTAs finish, and wait (grid_dep_wait) before they read or
+// write global memory.  Used for the kernels of the two-pass NTT and
+// polymul, whose every CTA waits so.
+template <typename... KArgs, typename... Args>
+void launch_dependent(void (*kernel)(KArgs...), uint32_t grid, uint32_t threads, size_t smem, cudaStream_t st,
+                      Args... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = g_dependent_launches ? 1 : 0;
+  (void)cudaLaunchKernelEx(&cfg, kernel, args...);  // errors surface through cudaGetLastError
+}
+
 // Whole-limb tile: 2^T words (T >= log_n); 16 words per thread (8 at N = 8).
 template <int LOGN, int T>
 using WholeCfg = TileCfg<T, LOGN, 0, (LOGN >= 4 ? 4 : 3)>;
@@ -955,18 +984,18 @@ cudaError_t launch_two_pass_ntt(const LimbSet& ls, const DevMod* mods, NttDir di
   if (dir == NttDir::kBackward) {
     {
       LaunchScope ps("row_pass_inv", st);
-      k_row_pass<RC, K1, true><<<tiles, RC::THREADS, kTileSmemBytes, st>>>(ls, mods, 0);
+      launch_dependent(k_row_pass<RC, K1, true>, tiles, RC::THREADS, kTileSmemBytes, st, ls, mods, 0);
     }
     LaunchScope ps("col_pass_inv", st);
-    k_col_pass<CC, LOGB, true><<<tiles, CC::THREADS, kTileSmemBytes, st>>>(cls, ls, mods);
+    launch_dependent(k_col_pass<CC, LOGB, true>, tiles, CC::THREADS, kTileSmemBytes, st, cls, ls, mods);
   } else {
     {
       LaunchScope ps("col_pass_fwd", st);
-      k_col_pass<CC, LOGB, false><<<tiles, CC::THREADS, kTileSmemBytes, st>>>(cls, ls, mods);
+      launch_dependent(k_col_pass<CC, LOGB, false>, tiles, CC::THREADS, kTileSmemBytes, st, cls, ls, mods);
     }
     LaunchScope ps("row_pass_fwd", st);
-    k_row_pass<RC, K1, false><<<tiles, RC::THREADS, kTileSmemBytes, st>>>(
-        ls, mods, dir == NttDir::kForward ? 1 : 0);
+    launch_dependent(k_row_pass<RC, K1, false>, tiles, RC::THREADS, kTileSmemBytes, st, ls, mods,
+                     dir == NttDir::kForward ? 1 : 0);
   }
   g_kernel_launches += 2;
   return cudaGetLastError();
@@ -986,15 +1015,15 @@ cudaError_t launch_two_pass_polymul(const LimbSet& c, const ConstLimbSet& a, con
   sl.ptrs = scratch_ptrs;
   {
     LaunchScope ps("polymul_col_fwd", st);
-    k_col_pass2<CC, LOGB><<<tiles, CC::THREADS, 2 * kTileSmemBytes, st>>>(a, b, c, sl, mods);
+    launch_dependent(k_col_pass2<CC, LOGB>, tiles, CC::THREADS, 2 * kTileSmemBytes, st, a, b, c, sl, mods);
   }
   {
     LaunchScope ps("polymul_rows", st);
-    k_polymul_rows<RC, K1><<<tiles, RC::THREADS, 2 * kTileSmemBytes, st>>>(c, as_const(sl), mods);
+    launch_dependent(k_polymul_rows<RC, K1>, tiles, RC::THREADS, 2 * kTileSmemBytes, st, c, as_const(sl), mods);
   }
   {
     LaunchScope ps("polymul_col_inv", st);
-    k_col_pass<CC, LOGB, true><<<tiles, CC::THREADS, kTileSmemBytes, st>>>(as_const(c), c, mods);
+    launch_dependent(k_col_pass<CC, LOGB, true>, tiles, CC::THREADS, kTileSmemBytes, st, as_const(c), c, mods);
   }
   g_kernel_launches += 3;
   return cudaGetLastError();

@@ -57,6 +57,7 @@ inline uint32_t bit_reverse(uint32_t x, uint32_t bits) {
 }  // namespace
 
 std::atomic<uint64_t> g_kernel_launches{0};
+thread_local bool g_dependent_launches = true;
 std::atomic<uint64_t> g_allocations{0};
 
 const PrimeEntry& prime_entry(uint32_t cm) { return kPrimes[cm]; }

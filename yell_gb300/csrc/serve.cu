@@ -270,6 +270,7 @@ static cudaError_t host_out(DeviceContext* ctx, uint64_t* host, const uint64_t* 
 
 int yell_server::launch(Slot& s, std::vector<ReqPtr>& batch) {
   TraceRange trace("yell serve step");
+  PlainLaunches plain;  // batches of other slots run beside this one
   const size_t n = batch.size();
   std::vector<yell_polymul_desc> descs;
   std::vector<uint64_t*> scratch;
