@@ -691,7 +691,10 @@ template <class C, int K1>
 __global__ void __launch_bounds__(C::THREADS, min_blocks(512, C::THREADS))
     k_polymul_rows(LimbSet ca, ConstLimbSet sbuf, const DevMod* __restrict__ mods) {
   grid_dep_launch();
-  polymul_rows_body<C, K1, false, true>(ca, sbuf, mods, blockIdx.x);
+  // tiles in the reverse of the column pass's order: the first rows read the
+  // words the column pass wrote last, still in L2, and the inverse column
+  // pass (forward order) starts on the rows written last
+  polymul_rows_body<C, K1, false, true>(ca, sbuf, mods, gridDim.x - 1 - blockIdx.x);
 }
 
 // ===========================================================================
