@@ -45,6 +45,28 @@ struct PlainLaunches {
   PlainLaunches& operator=(const PlainLaunches&) = delete;
 };
 
+// Launch as a programmatic dependent of the stream's previous kernel (unless
+// g_dependent_launches is cleared): the kernel's CTAs may start while that
+// kernel's last CTAs finish, and wait (grid_dep_wait) before they read or
+// write global memory (every kernel launched so executes grid_dep_wait
+// first; common.cuh).  Used where one call is a chain of kernels on its
+// stream: the two-pass NTT and polymul, the HWT sampler.
+template <typename... KArgs, typename... Args>
+void launch_dependent(void (*kernel)(KArgs...), dim3 grid, uint32_t threads, size_t smem, cudaStream_t st,
+                      Args... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = g_dependent_launches ? 1 : 0;
+  (void)cudaLaunchKernelEx(&cfg, kernel, args...);  // errors surface through cudaGetLastError
+}
+
 // Device and pinned-host allocations made by this library.  Every allocation
 // goes through these wrappers, so the count covers all of them.
 extern std::atomic<uint64_t> g_allocations;

@@ -903,27 +903,6 @@ cudaError_t set_smem(KernelT kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-// Launch as a programmatic dependent of the stream's previous kernel (unless
-// g_dependent_launches is cleared): the kernel's CTAs may start while that
-// kernel's last CTAs finish, and wait (grid_dep_wait) before they read or
-// write global memory.  Used for the kernels of the two-pass NTT and
-// polymul, whose every CTA waits so.
-template <typename... KArgs, typename... Args>
-void launch_dependent(void (*kernel)(KArgs...), uint32_t grid, uint32_t threads, size_t smem, cudaStream_t st,
-                      Args... args) {
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(threads);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cfg.attrs = attr;
-  cfg.numAttrs = g_dependent_launches ? 1 : 0;
-  (void)cudaLaunchKernelEx(&cfg, kernel, args...);  // errors surface through cudaGetLastError
-}
-
 // Whole-limb tile: 2^T words (T >= log_n); 16 words per thread (8 at N = 8).
 template <int LOGN, int T>
 using WholeCfg = TileCfg<T, LOGN, 0, (LOGN >= 4 ? 4 : 3)>;

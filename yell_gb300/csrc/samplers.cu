@@ -183,6 +183,8 @@ struct HwtCtl {
 __host__ __device__ __forceinline__ uint64_t accept_limit(uint32_t k) { return (~0ull / k) * k; }
 
 __global__ void k_hwt_init(uint32_t* hitted, HwtCtl* ctl, uint32_t count, uint32_t h, uint32_t n) {
+  grid_dep_launch();
+  grid_dep_wait();  // the scratch may be the previous kernel's
   const size_t total = (size_t)count * h;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x)
     hitted[t] = (uint32_t)(t % h);
@@ -198,9 +200,11 @@ __global__ void k_hwt_init(uint32_t* hitted, HwtCtl* ctl, uint32_t count, uint32
 // grid row j; the acceptance limit floor((2^64 - 1) / k) * k is at least
 // 2^64 - k, so only a draw above that needs the division.
 __global__ void k_hwt_reservoir(uint32_t* hitted, HwtCtl* ctl, uint32_t log_n, uint32_t h, uint64_t seed) {
+  grid_dep_launch();
   const uint32_t per = (1u << log_n) - h;
   const uint32_t j = blockIdx.y;
   const uint64_t s = rand_word(seed, j);
+  grid_dep_wait();  // the initialised slots
   for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < per; d += gridDim.x * blockDim.x) {
     const uint32_t k = h + d;
     const uint64_t w = rand_word(s, d);
@@ -223,10 +227,12 @@ __global__ void __launch_bounds__(kRankThreads) k_hwt_rank(uint32_t* hitted, Hwt
                                                            uint32_t* prefix, uint32_t log_n, uint32_t h, uint64_t seed,
                                                            int sequential) {
   extern __shared__ uint32_t sbits[];
+  grid_dep_launch();
   const uint32_t j = blockIdx.x, tid = threadIdx.x;
   const uint32_t n = 1u << log_n, nw = n >= 32 ? n >> 5 : 1u;
   uint32_t* hit = hitted + (size_t)j * h;
   uint32_t* warp_sum = sbits + nw;
+  grid_dep_wait();  // the reservoir
   if (tid == 0 && (sequential || ctl[j].first_reject < n)) {
     const uint64_t s = rand_word(seed, j);
     for (uint32_t t = 0; t < h; ++t) hit[t] = t;
@@ -288,6 +294,7 @@ __global__ void k_hwt_write(uint64_t* out, uint32_t count, uint32_t L, uint32_t 
   const size_t pairs = ((size_t)count << log_n) >> 1;
   const uint32_t nmask = (1u << log_n) - 1u;
   const uint32_t nw = log_n >= 5 ? 1u << (log_n - 5) : 1u;
+  grid_dep_wait();  // the bit sets and ranks
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < pairs; t += (size_t)gridDim.x * blockDim.x) {
     const size_t k = t << 1;
     const size_t poly = k >> log_n;
@@ -531,20 +538,22 @@ int yell_dev_sample_hwt(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t lo
   if (smem > 48 * 1024) e = cudaFuncSetAttribute(k_hwt_rank, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess) {
     LaunchScope ps("sample_hwt", a.st);
-    k_hwt_init<<<grid_for((size_t)count * h), 256, 0, a.st>>>(hitted, ctl, count, h, n);
+    launch_dependent(k_hwt_init, grid_for((size_t)count * h), 256, 0, a.st, hitted, ctl, count, h, n);
     if (n > h) {
       // grid rows = polys (at most 65535 per launch); columns cover a poly's draws
       const uint32_t cols = (uint32_t)std::min<size_t>(((size_t)(n - h) + 255) / 256, 152u * 16u);
       for (uint32_t j0 = 0; j0 < count; j0 += 65535u) {
         const uint32_t rows = std::min(count - j0, 65535u);
         // rand_word(seed, j0 + j) = rand_word(seed + j0 * gamma, j)
-        k_hwt_reservoir<<<dim3(cols, rows), 256, 0, a.st>>>(hitted + (size_t)j0 * h, ctl + j0, log_n, h,
-                                                             seed + (uint64_t)j0 * 0x9E3779B97F4A7C15ull);
+        launch_dependent(k_hwt_reservoir, dim3(cols, rows), 256, 0, a.st, hitted + (size_t)j0 * h, ctl + j0, log_n, h,
+                         seed + (uint64_t)j0 * 0x9E3779B97F4A7C15ull);
       }
     }
-    k_hwt_rank<<<count, kRankThreads, smem, a.st>>>(hitted, ctl, bits, prefix, log_n, h, seed, sequential);
-    k_hwt_write<<<grid_for(((size_t)count << log_n) >> 1), 256, 0, a.st>>>(d_out, count, L, log_n, cm0, a.mods, seed,
-                                                                           h, ctl, bits, prefix);
+    launch_dependent(k_hwt_rank, count, kRankThreads, smem, a.st, hitted, ctl, bits, prefix, log_n, h, seed,
+                     sequential);
+    launch_dependent(k_hwt_write, grid_for(((size_t)count << log_n) >> 1), 256, 0, a.st, d_out, count, L, log_n, cm0,
+                     a.mods, seed, h, static_cast<const HwtCtl*>(ctl), static_cast<const uint32_t*>(bits),
+                     static_cast<const uint32_t*>(prefix));
     g_kernel_launches += 3 + (n > h ? (count + 65534u) / 65535u : 0u);
     e = cudaGetLastError();
   }
