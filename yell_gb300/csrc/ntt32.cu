@@ -672,6 +672,8 @@ __global__ void __cluster_dims__(2, 1, 1)
   const uint2 w1 = __ldg(m.fwd + 1);
   const size_t lbase = (size_t)limb << log_n;
   const uint32_t bb = RB::base(tid);
+  grid_dep_launch();
+  grid_dep_wait();  // the stream's previous kernel may produce a or b, or read c
   if (tid == 0) {
     mbar_init(mbar, 1);
     mbar_expect(mbar, 2 * half * (uint32_t)sizeof(uint32_t));
@@ -831,8 +833,9 @@ cudaError_t launch32(int kind, uint32_t* c, const uint32_t* a, const uint32_t* b
     if (kind == 0) k32_ntt_pair<NC, 0><<<g, NP::THREADS, NC::kSmem, st>>>(c, ls, mods);
     else if (kind == 1) k32_ntt_pair<NC, 1><<<g, NP::THREADS, NC::kSmem, st>>>(c, ls, mods);
     else if (kind == 2) k32_ntt_pair<NC, 2><<<g, NP::THREADS, NC::kSmem, st>>>(c, ls, mods);
-    else if (LOGN >= kStagedMinLogN)
-      k32_polymul_pair_staged<LOGN><<<g, P::THREADS, StagedCfg32<LOGN>::kSmem, st>>>(c, a, b, ls, mods);
+    else if (LOGN >= kStagedMinLogN)  // a programmatic dependent of the stream's previous kernel
+      launch_dependent(k32_polymul_pair_staged<LOGN>, g, P::THREADS, StagedCfg32<LOGN>::kSmem, st, c, a, b, ls,
+                       mods);
     else k32_polymul_pair<PC><<<g, P::THREADS, PC::kSmem, st>>>(c, a, b, ls, mods);
     return cudaGetLastError();
   }
