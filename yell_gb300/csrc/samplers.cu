@@ -66,6 +66,8 @@ __host__ __device__ __forceinline__ uint64_t rand_word(uint64_t seed, uint64_t k
 // mask) changes rarely and is worked out only when it does.
 __global__ void k_sample_uniform(uint64_t* out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
                                  const DevMod* __restrict__ mods, uint64_t seed) {
+  grid_dep_launch();
+  grid_dep_wait();  // out may be in use by the stream's previous kernel
   const size_t words = ((size_t)count * L) << log_n;
   const size_t chunks = (words + 127) >> 7;
   const uint32_t lane = threadIdx.x & 31u;
@@ -130,6 +132,8 @@ __device__ __forceinline__ void put_pair(uint64_t* out, size_t poly, uint32_t i,
 // Two adjacent coefficients per thread (k even), both bytes of one word.
 __global__ void k_sample_zo(uint64_t* out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
                             const DevMod* __restrict__ mods, uint64_t seed, uint32_t rho) {
+  grid_dep_launch();
+  grid_dep_wait();  // out may be in use by the stream's previous kernel
   const size_t pairs = ((size_t)count << log_n) >> 1;
   const uint32_t nmask = (1u << log_n) - 1u;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < pairs; t += (size_t)gridDim.x * blockDim.x) {
@@ -160,6 +164,8 @@ __device__ __forceinline__ int64_t gaussian_int(uint64_t r, const uint64_t* __re
 __global__ void k_sample_gaussian(uint64_t* out, uint32_t count, uint32_t L, uint32_t log_n, uint32_t cm0,
                                   const DevMod* __restrict__ mods, uint64_t seed, const uint64_t* __restrict__ cdt,
                                   uint32_t cdt_len, int32_t tail, uint64_t amplifier) {
+  grid_dep_launch();
+  grid_dep_wait();  // out may be in use by the stream's previous kernel
   const size_t pairs = ((size_t)count << log_n) >> 1;
   const uint32_t nmask = (1u << log_n) - 1u;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < pairs; t += (size_t)gridDim.x * blockDim.x) {
@@ -488,8 +494,8 @@ int yell_dev_sample_uniform(uint64_t* d_out, uint32_t count, uint32_t L, uint32_
   int st = prepare(d_out, count, L, log_n, cm0, stream, &a);
   if (st != kOk) return st;
   LaunchScope ps("sample_uniform", a.st);
-  k_sample_uniform<<<grid_for((((size_t)count * L) << log_n) >> 2), 256, 0, a.st>>>(d_out, count, L, log_n, cm0,
-                                                                            a.mods, seed);
+  launch_dependent(k_sample_uniform, grid_for((((size_t)count * L) << log_n) >> 2), 256, 0, a.st, d_out, count, L,
+                   log_n, cm0, a.mods, seed);
   g_kernel_launches += 1;
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? kOk : fail_cuda(e, "sample_uniform");
@@ -502,8 +508,8 @@ int yell_dev_sample_zo(uint64_t* d_out, uint32_t count, uint32_t L, uint32_t log
   int st = prepare(d_out, count, L, log_n, cm0, stream, &a);
   if (st != kOk) return st;
   LaunchScope ps("sample_zo", a.st);
-  k_sample_zo<<<grid_for(((size_t)count << log_n) >> 1), 256, 0, a.st>>>(d_out, count, L, log_n, cm0, a.mods,
-                                                                         seed, rho);
+  launch_dependent(k_sample_zo, grid_for(((size_t)count << log_n) >> 1), 256, 0, a.st, d_out, count, L, log_n, cm0,
+                   a.mods, seed, rho);
   g_kernel_launches += 1;
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? kOk : fail_cuda(e, "sample_zo");
@@ -576,8 +582,8 @@ int yell_dev_sample_gaussian(uint64_t* d_out, uint32_t count, uint32_t L, uint32
   st = gaussian_table(a.ctx->device(), sigma, tail, &cdt, &len);
   if (st != kOk) return st;
   LaunchScope ps("sample_gaussian", a.st);
-  k_sample_gaussian<<<grid_for(((size_t)count << log_n) >> 1), 256, 0, a.st>>>(d_out, count, L, log_n, cm0, a.mods,
-                                                                               seed, cdt, len, (int32_t)tail, amplifier);
+  launch_dependent(k_sample_gaussian, grid_for(((size_t)count << log_n) >> 1), 256, 0, a.st, d_out, count, L, log_n,
+                   cm0, a.mods, seed, cdt, len, (int32_t)tail, amplifier);
   g_kernel_launches += 1;
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? kOk : fail_cuda(e, "sample_gaussian");
