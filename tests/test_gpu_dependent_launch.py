@@ -72,3 +72,35 @@ def test_chain_of_calls_on_one_stream(cuda, orc):
     for i in range(pairs):
         assert np.array_equal(got_f[i], orc.poly_forward(w2[i], log_n, 0)), i
     assert np.array_equal(_host(r, a.shape), w2)
+
+
+def test_captured_into_a_caller_graph(cuda, orc):
+    """A caller captures the polymul (caller scratch, tables built before) into
+    its own CUDA graph: the dependent launches become programmatic edges of
+    the graph, and replays on new operands give the oracle's words."""
+    torch = cuda
+    log_n, pairs, L = 16, 2, 2
+    ps = y.primes(L)
+    y.init_ntt_tables(log_n, L, 0)
+    a = uniform_polys(61, pairs, L, log_n, ps)
+    b = uniform_polys(62, pairs, L, log_n, ps)
+    da, db = _dev(torch, a), _dev(torch, b)
+    c = torch.empty_like(da)
+    scratch = torch.empty(y.polymul_scratch_words(pairs, L, log_n), dtype=torch.int64, device="cuda")
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):  # one eager call first, as torch asks before a capture
+        y.dev_polymul(c, da, db, pairs, L, log_n, 0, scratch=scratch, stream=s)
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, capture_error_mode="thread_local"):
+        y.dev_polymul(c, da, db, pairs, L, log_n, 0, scratch=scratch,
+                      stream=torch.cuda.current_stream())
+    for seed in (63, 64):
+        a2 = uniform_polys(seed, pairs, L, log_n, ps)
+        da.copy_(_dev(torch, a2))
+        c.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        want = np.stack([orc.polymul(a2[i], b[i], log_n, 0) for i in range(pairs)])
+        assert np.array_equal(_host(c, a.shape), want), seed
