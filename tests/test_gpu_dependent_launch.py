@@ -104,3 +104,23 @@ def test_captured_into_a_caller_graph(cuda, orc):
         torch.cuda.synchronize()
         want = np.stack([orc.polymul(a2[i], b[i], log_n, 0) for i in range(pairs)])
         assert np.array_equal(_host(c, a.shape), want), seed
+
+
+@pytest.mark.parametrize("log_n,h", [(10, 64), (16, 192)])
+def test_samplers_after_a_foreign_write(cuda, orc, log_n, h):
+    """A torch kernel fills the output with all-ones words just before each
+    sampler call on the same stream: the HWT sample (zero fill beside the
+    draws, then the chosen words) and the ZO sample equal the oracle's."""
+    torch = cuda
+    count, L = 3, 2
+    t = torch.empty((count * L) << log_n, dtype=torch.int64, device="cuda")
+    for _ in range(2):
+        t.fill_(-1)
+        y.sample_hwt(t, count, L, log_n, h, cm0=1, seed=h + 7)
+        torch.cuda.synchronize()
+        got = _host(t, (count, L, 1 << log_n))
+        assert np.array_equal(got, orc.sample_hwt(count, L, log_n, h, 1, h + 7))
+        t.fill_(-1)
+        y.sample_zo(t, count, L, log_n, 1, rho=0x7F, seed=h + 8)
+        torch.cuda.synchronize()
+        assert np.array_equal(_host(t, (count, L, 1 << log_n)), orc.sample_zo(count, L, log_n, 1, 0x7F, h + 8))
