@@ -338,14 +338,15 @@ template <> struct PairOf<uint32_t> {
 };
 
 // ---------------------------------------------------------------------------
-// Programmatic dependent launch.  The kernels of a two-pass transform are
-// launched with programmatic stream serialization: their CTAs may become
-// resident while the stream's previous kernel still runs its last CTAs, and
+// Programmatic dependent launch.  Kernels launched with programmatic stream
+// serialization (launch_dependent, kernels.h) may have their CTAs resident
+// while the stream's previous kernel still runs its last CTAs;
 // grid_dep_wait() returns once that kernel has completed with its writes
 // visible (at once for a kernel launched without the attribute, or when the
-// stream's previous work is not a kernel).  grid_dep_launch() at the start of
-// a CTA lets the stream's next kernel begin launching once every CTA of this
-// one has started.
+// stream's previous work is not a kernel), and every such kernel calls it
+// before it reads or writes global memory other than the library's own
+// tables.  grid_dep_launch() at the start of a CTA lets the stream's next
+// kernel begin launching once every CTA of this one has started.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }

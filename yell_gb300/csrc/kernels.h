@@ -47,10 +47,9 @@ struct PlainLaunches {
 
 // Launch as a programmatic dependent of the stream's previous kernel (unless
 // g_dependent_launches is cleared): the kernel's CTAs may start while that
-// kernel's last CTAs finish, and wait (grid_dep_wait) before they read or
-// write global memory (every kernel launched so executes grid_dep_wait
-// first; common.cuh).  Used for the two-pass NTT and polymul, the samplers
-// and the staged 32-bit polymul.
+// kernel's last CTAs finish, and wait (grid_dep_wait, common.cuh) before
+// they touch global memory other than the library's tables.  Used for the
+// two-pass NTT and polymul, the samplers and the staged 32-bit polymul.
 template <typename... KArgs, typename... Args>
 void launch_dependent(void (*kernel)(KArgs...), dim3 grid, uint32_t threads, size_t smem, cudaStream_t st,
                       Args... args) {

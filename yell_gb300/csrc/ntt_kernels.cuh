@@ -387,6 +387,9 @@ __global__ void __launch_bounds__(C::THREADS, min_blocks(INV ? 1024 : 768, C::TH
   constexpr uint32_t log_n = K + LOGB;
   constexpr int TPL = LOGB - LB;  // log2(tiles per limb)
   grid_dep_launch();
+  // when launched as a dependent: the previous kernel's words, and limb or
+  // modulus lists it may have written, are read only after this
+  grid_dep_wait();
   const uint32_t tid = threadIdx.x;
   const uint32_t limb = dst.ordered(blockIdx.x >> TPL);
   const uint32_t col0 = (blockIdx.x & ((1u << TPL) - 1u)) << LB;
@@ -394,7 +397,6 @@ __global__ void __launch_bounds__(C::THREADS, min_blocks(INV ? 1024 : 768, C::TH
   uint64_t* out = dst.limb(limb, log_n) + col0;
   const DevMod m = load_mod(mods, dst.cm(limb));
   uint64_t x[1 << C::LOGE];
-  grid_dep_wait();  // the previous pass's words, when launched as a dependent
   if constexpr (!INV) {
     using R0 = Round<C, 0>;
     const uint32_t b0 = R0::base(tid);
@@ -446,13 +448,13 @@ __global__ void __launch_bounds__(C::THREADS) k_row_pass(LimbSet ls, const DevMo
   constexpr uint32_t log_n = K + K1;
   constexpr int TPL = log_n - kTileLog;
   grid_dep_launch();
+  grid_dep_wait();  // as in k_col_pass
   const uint32_t tid = threadIdx.x;
   const uint32_t limb = ls.ordered(blockIdx.x >> TPL);
   const uint32_t off = (blockIdx.x & ((1u << TPL) - 1u)) << kTileLog;
   uint64_t* data = ls.limb(limb, log_n) + off;
   const DevMod m = load_mod(mods, ls.cm(limb));
   const uint32_t G = (off >> K) + C::sub(tid);
-  grid_dep_wait();  // the previous pass's words, when launched as a dependent
   if constexpr (!INV) {
     using R0 = Round<C, 0>;
     uint64_t x[1 << C::LOGE];
@@ -594,7 +596,7 @@ __global__ void __launch_bounds__(C::THREADS, C::THREADS <= 256 ? 2 : 1) k_polym
 // Forward column pass of both polymul operands in one CTA: each thread
 // applies the same butterflies to a's and b's words at the same positions,
 // so every twiddle load serves two butterflies.  a -> ca, b -> cb.
-template <class C, int LOGB, bool PDL = false>
+template <class C, int LOGB>
 __device__ __forceinline__ void col_pass2_body(ConstLimbSet a, ConstLimbSet b, LimbSet ca, LimbSet cb,
                                                const DevMod* __restrict__ mods, uint32_t bid) {
   extern __shared__ __align__(16) uint64_t smem[];
@@ -612,7 +614,6 @@ __device__ __forceinline__ void col_pass2_body(ConstLimbSet a, ConstLimbSet b, L
   uint64_t xa[E], xb[E];
   using R0 = Round<C, 0>;
   const uint32_t b0 = R0::base(tid);
-  if constexpr (PDL) grid_dep_wait();  // whatever the stream's previous kernel wrote
   gload_cols<R0, LOGB>(xa, a.limb(limb, log_n) + col0, b0);
   gload_cols<R0, LOGB>(xb, b.limb(limb, log_n) + col0, b0);
   ct_stages2<R0::R, R0::E>(xa, xb, m.fwd, R0::HI, R0::gr(b0, 0), np, p2);
@@ -638,12 +639,13 @@ template <class C, int LOGB>
 __global__ void __launch_bounds__(C::THREADS, min_blocks(512, C::THREADS))
     k_col_pass2(ConstLimbSet a, ConstLimbSet b, LimbSet ca, LimbSet cb, const DevMod* __restrict__ mods) {
   grid_dep_launch();
-  col_pass2_body<C, LOGB, true>(a, b, ca, cb, mods, blockIdx.x);
+  grid_dep_wait();  // as in k_col_pass
+  col_pass2_body<C, LOGB>(a, b, ca, cb, mods, blockIdx.x);
 }
 
 // Two-pass fused row step: ca holds a's column-pass output and receives the
 // row-pass output of the product; sbuf holds b's column-pass output.
-template <class C, int K1, bool COH = false, bool PDL = false>
+template <class C, int K1, bool COH = false>
 __device__ __forceinline__ void polymul_rows_body(LimbSet ca, ConstLimbSet sbuf, const DevMod* __restrict__ mods,
                                                   uint32_t bid) {
   extern __shared__ __align__(16) uint64_t smem[];
@@ -665,7 +667,6 @@ __device__ __forceinline__ void polymul_rows_body(LimbSet ca, ConstLimbSet sbuf,
   uint64_t xa[E], xb[E];
   using R0 = Round<C, 0>;
   const uint32_t b0 = R0::base(tid);
-  if constexpr (PDL) grid_dep_wait();  // the column pass's words
   gload_rows<R0, COH>(xa, pa, b0);
   gload_rows<R0, COH>(xb, pb, b0);
   ct_stages2<R0::R, R0::E>(xa, xb, m.fwd, K1 + R0::HI, R0::gr(b0, G), 0 - m.p, m.p << 1);
@@ -691,10 +692,11 @@ template <class C, int K1>
 __global__ void __launch_bounds__(C::THREADS, min_blocks(512, C::THREADS))
     k_polymul_rows(LimbSet ca, ConstLimbSet sbuf, const DevMod* __restrict__ mods) {
   grid_dep_launch();
+  grid_dep_wait();  // as in k_col_pass
   // tiles in the reverse of the column pass's order: the first rows read the
   // words the column pass wrote last, still in L2, and the inverse column
   // pass (forward order) starts on the rows written last
-  polymul_rows_body<C, K1, false, true>(ca, sbuf, mods, gridDim.x - 1 - blockIdx.x);
+  polymul_rows_body<C, K1>(ca, sbuf, mods, gridDim.x - 1 - blockIdx.x);
 }
 
 // ===========================================================================
