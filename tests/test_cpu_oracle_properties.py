@@ -1,0 +1,66 @@
+"""Property checks of the oracle (the C restatement of the reference) on
+randomly drawn degrees, moduli and words, beside the fixed golden vectors:
+word-for-word equality with the reference's own compiled sources where that
+build is present, the negacyclic convolution theorem against the schoolbook
+product, linearity of the forward transform, and forward -> backward as the
+identity.  CPU only; hypothesis drives the draws."""
+import numpy as np
+import pytest
+
+hypothesis = pytest.importorskip("hypothesis")
+from hypothesis import given, settings, strategies as st  # noqa: E402
+
+import oracle  # noqa: E402
+from yell_gb300.inputs import splitmix64  # noqa: E402
+
+SETTINGS = settings(max_examples=40, deadline=None, derandomize=True)
+
+
+def _words(seed, n, bound):
+    x = splitmix64(seed, n) % np.uint64(bound)
+    # edge words at fixed places: 0 and the largest word allowed
+    x[0] = 0
+    x[-1] = bound - 1
+    return x
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference build not present")
+@SETTINGS
+@given(log_n=st.integers(3, 13), cm=st.integers(0, 999), seed=st.integers(0, 2**32))
+def test_port_equals_reference_build(orc, log_n, cm, seed):
+    ref = oracle.Oracle("ref")
+    p = orc.prime(cm)
+    n = 1 << log_n
+    x4 = _words(seed, n, 4 * p)
+    assert np.array_equal(orc.forward_lazy(x4, log_n, cm), ref.forward_lazy(x4, log_n, cm))
+    assert np.array_equal(orc.forward(x4, log_n, cm), ref.forward(x4, log_n, cm))
+    x2 = _words(seed + 1, n, 2 * p)
+    assert np.array_equal(orc.backward(x2, log_n, cm), ref.backward(x2, log_n, cm))
+    a, b = _words(seed + 2, n, p), _words(seed + 3, n, p)
+    assert np.array_equal(orc.mulmod(a, b, cm), ref.mulmod(a, b, cm))
+    assert np.array_equal(orc.addmod(a, b, cm), ref.addmod(a, b, cm))
+    assert np.array_equal(orc.submod(a, b, cm), ref.submod(a, b, cm))
+    a4, b4 = _words(seed + 4, n, 4 * p), _words(seed + 5, n, 4 * p)
+    assert np.array_equal(orc.muladd(a, a4, b4, cm), ref.muladd(a, a4, b4, cm))
+
+
+@SETTINGS
+@given(log_n=st.integers(3, 9), cm=st.integers(0, 999), seed=st.integers(0, 2**32))
+def test_polymul_is_the_negacyclic_product(orc, log_n, cm, seed):
+    p = orc.prime(cm)
+    n = 1 << log_n
+    a, b = _words(seed, n, p), _words(seed + 7, n, p)
+    got = orc.polymul(a[None], b[None], log_n, cm)[0]
+    assert np.array_equal(got, orc.schoolbook(a, b, log_n, cm))
+
+
+@SETTINGS
+@given(log_n=st.integers(3, 12), cm=st.integers(0, 999), seed=st.integers(0, 2**32))
+def test_forward_is_linear_and_backward_inverts_it(orc, log_n, cm, seed):
+    p = orc.prime(cm)
+    n = 1 << log_n
+    a, b = _words(seed, n, p), _words(seed + 11, n, p)
+    fa, fb = orc.forward(a, log_n, cm), orc.forward(b, log_n, cm)
+    assert np.array_equal(orc.forward(orc.addmod(a, b, cm), log_n, cm), orc.addmod(fa, fb, cm))
+    assert np.array_equal(orc.backward(fa, log_n, cm), a)
+    assert int(fa.max()) < p
