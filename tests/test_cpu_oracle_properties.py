@@ -1,5 +1,6 @@
-"""Property checks of the oracle (the C restatement of the reference) on
-randomly drawn degrees, moduli and words, beside the fixed golden vectors:
+"""Property checks of the oracle (the C restatement of the reference, and of
+its 32-bit moduli build) on randomly drawn degrees, moduli and words, beside
+the fixed golden vectors:
 word-for-word equality with the reference's own compiled sources where that
 build is present, the negacyclic convolution theorem against the schoolbook
 product, linearity of the forward transform, and forward -> backward as the
@@ -64,3 +65,31 @@ def test_forward_is_linear_and_backward_inverts_it(orc, log_n, cm, seed):
     assert np.array_equal(orc.forward(orc.addmod(a, b, cm), log_n, cm), orc.addmod(fa, fb, cm))
     assert np.array_equal(orc.backward(fa, log_n, cm), a)
     assert int(fa.max()) < p
+
+
+def _words32(seed, n, bound):
+    x = (splitmix64(seed, n) % np.uint64(bound)).astype(np.uint32)
+    x[0] = 0
+    x[-1] = bound - 1
+    return x
+
+
+@pytest.mark.skipif(not oracle.ref32_available(), reason="reference 32-bit build not present")
+@SETTINGS
+@given(log_n=st.integers(3, 15), cm=st.integers(0, 290), seed=st.integers(0, 2**32))
+def test_port32_equals_reference_build(log_n, cm, seed):
+    """The 32-bit moduli restatement against the reference's own sources built
+    with -DYELL_USE_32BITS_MODULI: NTTs and element-wise ops word for word."""
+    port, ref = oracle.Oracle32("port"), oracle.Oracle32("ref")
+    p = port.prime(cm)
+    n = 1 << log_n
+    x4 = _words32(seed, n, 4 * p)
+    assert np.array_equal(port.forward_lazy(x4, log_n, cm), ref.forward_lazy(x4, log_n, cm))
+    assert np.array_equal(port.forward(x4, log_n, cm), ref.forward(x4, log_n, cm))
+    x2 = _words32(seed + 1, n, 2 * p)
+    assert np.array_equal(port.backward(x2, log_n, cm), ref.backward(x2, log_n, cm))
+    a, b = _words32(seed + 2, n, p), _words32(seed + 3, n, p)
+    for op in ("mulmod", "addmod", "submod"):
+        assert np.array_equal(getattr(port, op)(a, b, cm), getattr(ref, op)(a, b, cm)), op
+    a4, b4 = _words32(seed + 4, n, 4 * p), _words32(seed + 5, n, 4 * p)
+    assert np.array_equal(port.muladd(a, a4, b4, cm), ref.muladd(a, a4, b4, cm))
