@@ -2,9 +2,10 @@
 its 32-bit moduli build) on randomly drawn degrees, moduli and words, beside
 the fixed golden vectors:
 word-for-word equality with the reference's own compiled sources where that
-build is present, the negacyclic convolution theorem against the schoolbook
-product, linearity of the forward transform, and forward -> backward as the
-identity.  CPU only; hypothesis drives the draws."""
+build is present (NTTs, element-wise ops, the uniform / ZO / HWT samplers),
+the negacyclic convolution theorem against the schoolbook product, linearity
+of the forward transform, and forward -> backward as the identity.  CPU only;
+hypothesis drives the draws."""
 import numpy as np
 import pytest
 
@@ -93,3 +94,21 @@ def test_port32_equals_reference_build(log_n, cm, seed):
         assert np.array_equal(getattr(port, op)(a, b, cm), getattr(ref, op)(a, b, cm)), op
     a4, b4 = _words32(seed + 4, n, 4 * p), _words32(seed + 5, n, 4 * p)
     assert np.array_equal(port.muladd(a, a4, b4, cm), ref.muladd(a, a4, b4, cm))
+
+
+@pytest.mark.skipif(not oracle.ref_samplers_available(), reason="reference sampler build absent")
+@SETTINGS
+@given(log_n=st.integers(3, 12), count=st.integers(1, 3), L=st.integers(1, 3),
+       rho=st.integers(0, 255), hfrac=st.floats(0.0, 1.0), seed=st.integers(0, 2**40))
+def test_samplers_equal_reference_on_drawn_shapes(orc, log_n, count, L, rho, hfrac, seed):
+    """uniform, ZO(rho) and HWT(h) of the sampler oracle against the
+    reference's own poly<N>::set(...) on the same counter stream, at drawn
+    shapes, rho, Hamming weights (1 .. N) and seeds."""
+    ref = oracle.RefSamplers()
+    n = 1 << log_n
+    h = max(1, min(n, int(round(hfrac * n))))
+    assert np.array_equal(ref.sample_uniform(count, L, log_n, seed), orc.sample_uniform(count, L, log_n, seed=seed))
+    assert np.array_equal(ref.sample_zo(count, L, log_n, rho, seed + 1),
+                          orc.sample_zo(count, L, log_n, rho=rho, seed=seed + 1))
+    assert np.array_equal(ref.sample_hwt(count, L, log_n, h, seed + 2),
+                          orc.sample_hwt(count, L, log_n, h, seed=seed + 2))
