@@ -112,3 +112,26 @@ def test_samplers_equal_reference_on_drawn_shapes(orc, log_n, count, L, rho, hfr
                           orc.sample_zo(count, L, log_n, rho=rho, seed=seed + 1))
     assert np.array_equal(ref.sample_hwt(count, L, log_n, h, seed + 2),
                           orc.sample_hwt(count, L, log_n, h, seed=seed + 2))
+
+
+@pytest.mark.skipif(not oracle.ref_samplers_available(), reason="reference sampler build absent")
+@SETTINGS
+@given(L=st.integers(1, 40), seed=st.integers(0, 2**40))
+def test_crt_equals_reference_poly2mpz_on_drawn_residues(orc, L, seed):
+    """oracle/crt.py against the reference's gmp::poly2mpz on residues of L
+    moduli drawn from the counter stream, with 0, p - 1 and a small integer's
+    residues planted."""
+    from oracle.crt import CrtTable, poly2bigint, to_words
+
+    log_n = 4
+    n = 1 << log_n
+    primes = [orc.prime(j) for j in range(L)]
+    limbs = np.stack([splitmix64(seed + j, n) % np.uint64(p) for j, p in enumerate(primes)])
+    limbs[:, 0] = 0
+    limbs[:, 1] = [p - 1 for p in primes]  # Q - 1
+    limbs[:, 2] = [12345 % p for p in primes]
+    W = CrtTable(primes).words()
+    want = oracle.RefSamplers().poly2mpz(limbs, log_n, W)
+    got = poly2bigint(limbs, primes)
+    assert np.array_equal(to_words(got, W), want)
+    assert got[0] == 0 and got[2] == 12345
